@@ -1,0 +1,202 @@
+"""ctypes front of the C oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module; the product path never does. It drives the plain-C restatement
+(oracle/oofem_oracle.c) through the same steps as the reference's LinearStatic
+(src/sm/EngineeringModels/linearstatic.C:177-253) and NonLinearStatic + NRSolver
+(src/core/nrsolver.C:204-402).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboofem_oracle.so")
+NSTATE = 24
+
+_lib = None
+
+
+def build() -> str:
+    src = os.path.join(HERE, "oofem_oracle.c")
+    if (not os.path.exists(LIB)) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", LIB, src, "-lm"])
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def nnpe(et):
+    return 8 if et == 1 else 4
+
+
+def ndofpn(et):
+    return 2 if et == 2 else 3
+
+
+def ngp(et):
+    return {1: 8, 2: 4, 3: 1}[et]
+
+
+def nstress(et):
+    return 3 if et == 2 else 6
+
+
+def number_equations(bc_mask: np.ndarray):
+    nn, nd = bc_mask.shape
+    eq = np.zeros((nn, nd), np.int32)
+    npeq = C.c_int(0)
+    m = np.ascontiguousarray(bc_mask, dtype=np.uint8)
+    neq = lib().oro_number_equations(nn, nd, _p(m), _p(eq), C.byref(npeq))
+    return neq, npeq.value, eq
+
+
+def location_arrays(conn: np.ndarray, eq: np.ndarray):
+    ne, npe = conn.shape
+    nd = eq.shape[1]
+    loc = np.zeros((ne, npe * nd), np.int32)
+    c = np.ascontiguousarray(conn, dtype=np.int32)
+    lib().oro_location_arrays(ne, npe, _p(c), nd, _p(eq), _p(loc))
+    return loc
+
+
+def build_pattern(neq: int, loc: np.ndarray):
+    ne, nl = loc.shape
+    L = lib()
+    L.oro_build_pattern.restype = C.c_int64
+    rowptr = np.zeros(neq + 1, np.int64)
+    nnz = L.oro_build_pattern(neq, ne, nl, _p(loc), _p(rowptr), None)
+    colind = np.zeros(max(nnz, 1), np.int32)
+    L.oro_build_pattern(neq, ne, nl, _p(loc), _p(rowptr), _p(colind))
+    return rowptr, colind[:nnz]
+
+
+def elem_stiffness(et, xe, D, thickness=1.0, per_gp=False, symmetric=True):
+    nl = nnpe(et) * ndofpn(et)
+    Ke = np.zeros((nl, nl))
+    xe = np.ascontiguousarray(xe, dtype=np.float64)
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    lib().oro_elem_stiffness(et, _p(xe), _p(D), int(per_gp), C.c_double(thickness),
+                             int(symmetric), _p(Ke))
+    return Ke
+
+
+def isole_d(et, E, nu):
+    if et == 2:
+        D = np.zeros((3, 3))
+        lib().oro_isole_dps(C.c_double(E), C.c_double(nu), _p(D))
+    else:
+        D = np.zeros((6, 6))
+        lib().oro_isole_d3d(C.c_double(E), C.c_double(nu), _p(D))
+    return D
+
+
+def assemble_tangent(m: dict, loc, neq, rowptr, colind, state=None):
+    et = int(m["etype"])
+    coords = np.ascontiguousarray(m["coords"], dtype=np.float64)
+    conn = np.ascontiguousarray(m["conn"], dtype=np.int32)
+    emat = np.ascontiguousarray(m["elem_mat"], dtype=np.int32)
+    mats = np.ascontiguousarray(m["mats"], dtype=np.float64)
+    val = np.zeros(colind.size)
+    st = None if state is None else _p(state)
+    lib().oro_assemble_tangent(et, coords.shape[1], coords.shape[0], _p(coords), conn.shape[0],
+                               _p(conn), _p(emat), _p(mats), C.c_double(float(m["thickness"])),
+                               st, loc.shape[1], _p(loc), neq, _p(rowptr), _p(colind), _p(val))
+    return val
+
+
+def internal_forces(m: dict, u_node: np.ndarray, state=None):
+    """Node-indexed internal forces for the total displacement field; updates
+    the temp part of ``state`` in place. Returns (f_node, gp_stress, gp_strain)."""
+    et = int(m["etype"])
+    coords = np.ascontiguousarray(m["coords"], dtype=np.float64)
+    conn = np.ascontiguousarray(m["conn"], dtype=np.int32)
+    emat = np.ascontiguousarray(m["elem_mat"], dtype=np.int32)
+    mats = np.ascontiguousarray(m["mats"], dtype=np.float64)
+    nn, ne = coords.shape[0], conn.shape[0]
+    f = np.zeros((nn, ndofpn(et)))
+    sig = np.zeros((ne, ngp(et), nstress(et)))
+    eps = np.zeros_like(sig)
+    u = np.ascontiguousarray(u_node, dtype=np.float64)
+    st = None if state is None else _p(state)
+    lib().oro_internal_forces(et, coords.shape[1], nn, _p(coords), ne, _p(conn), _p(emat),
+                              _p(mats), C.c_double(float(m["thickness"])), _p(u), st, _p(f),
+                              _p(sig), _p(eps))
+    return f, sig, eps
+
+
+def commit_state(m: dict, state: np.ndarray):
+    et = int(m["etype"])
+    mats = np.ascontiguousarray(m["mats"], dtype=np.float64)
+    emat = np.asarray(m["elem_mat"])
+    g = ngp(et)
+    L = lib()
+    for e in range(emat.size):
+        mp = mats[emat[e]]
+        for k in range(g):
+            row = state[e * g + k]
+            L.oro_commit_state(et, _p(mp), _p(row))
+
+
+def spmv(rowptr, colind, val, x):
+    y = np.zeros(rowptr.size - 1)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    lib().oro_spmv(rowptr.size - 1, _p(rowptr), _p(colind), _p(val), _p(x), _p(y))
+    return y
+
+
+def pcg(rowptr, colind, val, b, rtol=1e-12, maxit=100000, x0=None):
+    n = rowptr.size - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    it = C.c_int(0)
+    ach = C.c_double(0)
+    st = lib().oro_pcg(n, _p(rowptr), _p(colind), _p(val), _p(b), _p(x), C.c_double(rtol),
+                       maxit, C.byref(it), C.byref(ach))
+    return x, st, it.value, ach.value
+
+
+def mesh_dict(mesh) -> dict:
+    """Arrays of a meshgen.Mesh in the fixture layout."""
+    return dict(etype=mesh.elem_type, coords=mesh.coords, conn=mesh.conn, elem_mat=mesh.elem_mat,
+                mats=mesh.material_table(), bc_mask=mesh.bc_mask, bc_value=mesh.bc_value,
+                nodal_load=mesh.nodal_load, thickness=mesh.thickness)
+
+
+def linear_static(m: dict, rtol=1e-12, maxit=100000, load_factor=1.0, bc_factor=1.0):
+    """LinearStatic::solveYourselfAt (linearstatic.C:177-253): K, load vector
+    f_ext - f_int(prescribed u), Jacobi-PCG, then reactions
+    (StructuralEngngModel::computeReaction, structengngmodel.C:183-201)."""
+    et = int(m["etype"])
+    bc_mask = np.asarray(m["bc_mask"])
+    neq, npeq, eq = number_equations(bc_mask)
+    loc = location_arrays(np.asarray(m["conn"]), eq)
+    rowptr, colind = build_pattern(neq, loc)
+    val = assemble_tangent(m, loc, neq, rowptr, colind)
+    u_node = np.where(bc_mask == 1, np.asarray(m["bc_value"]) * bc_factor, 0.0)
+    fint, _, _ = internal_forces(m, u_node)
+    fext = np.asarray(m["nodal_load"]) * load_factor
+    free = eq > 0
+    b = np.zeros(neq)
+    b[eq[free] - 1] = fext[free] - fint[free]
+    x, status, iters, ach = pcg(rowptr, colind, val, b, rtol, maxit)
+    u_node[free] = x[eq[free] - 1]
+    fint, sig, eps = internal_forces(m, u_node)
+    reac = np.where(bc_mask == 1, fint - fext, 0.0)
+    return dict(neq=neq, eq=eq, loc=loc, rowptr=rowptr, colind=colind, val=val, b=b, x=x,
+                u=u_node, reac=reac, stress=sig, strain=eps, status=status, iters=iters,
+                achieved=ach)

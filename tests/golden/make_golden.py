@@ -1,0 +1,189 @@
+"""Generate golden fixtures from the reference executable itself.
+
+Writes seeded synthetic meshes as OOFEM decks (tests/golden/decks.py), runs them
+through oracle/_ref/ref_harness (which links the reference's liboofem and dumps
+full-precision results), and stores mesh + results as tests/golden/<case>.npz.
+It also extracts the golden values embedded in the reference's own patch deck
+tests/sm/patch300.in into tests/golden/patch300.json.
+
+Needs a reference build (``make -C oracle ref REF_SRC=... REF_BUILD=...``);
+the committed fixtures are what the tests read, so this runs only when the
+fixtures are regenerated:
+
+    python tests/golden/make_golden.py [--ref-src DIR] [--work DIR]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from oofem_gb300 import meshgen as mg  # noqa: E402
+from decks import write_deck  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def parse_dump(path):
+    steps = []
+    K = None
+    kes = {}
+    cur = None
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    i = 0
+    while i < len(lines):
+        ln = lines[i]
+        i += 1
+        if not ln:
+            continue
+        t = ln.split()
+        if t[0] == "step":
+            cur = {"step": int(t[1]), "time": float(t[2]), "u": [], "gp": [], "reac": []}
+            steps.append(cur)
+        elif t[0] == "u":
+            cur["u"].append((int(t[1]), int(t[2]), int(t[3]), float(t[4])))
+        elif t[0] == "gp":
+            si = t.index("s")
+            ei = t.index("e")
+            ki = t.index("k")
+            s = [float(v) for v in t[si + 1:ei]]
+            e = [float(v) for v in t[ei + 1:ki]]
+            cur["gp"].append((int(t[1]), int(t[2]), s, e, float(t[ki + 1]), float(t[ki + 3]),
+                              float(t[ki + 5])))
+        elif t[0] == "reac":
+            cur["reac"].append((int(t[1]), int(t[2]), float(t[3])))
+        elif t[0] == "K":
+            neq, nnz = int(t[1]), int(t[2])
+            colptr = np.array(lines[i].split()[1:], dtype=np.int64)
+            rowind = np.array(lines[i + 1].split()[1:], dtype=np.int32)
+            val = np.array(lines[i + 2].split()[1:], dtype=np.float64)
+            i += 3
+            assert colptr.size == neq + 1 and rowind.size == nnz == val.size
+            K = (neq, colptr, rowind, val)
+        elif t[0] == "ke":
+            n = int(t[2])
+            kes[int(t[1])] = np.array(t[3:], dtype=np.float64).reshape(n, n)
+    return steps, K, kes
+
+
+def mesh_arrays(mesh: mg.Mesh) -> dict:
+    return dict(etype=np.int32(mesh.elem_type), coords=mesh.coords, conn=mesh.conn,
+                elem_mat=mesh.elem_mat, mats=mesh.material_table(), bc_mask=mesh.bc_mask,
+                bc_value=mesh.bc_value, nodal_load=mesh.nodal_load,
+                thickness=np.float64(mesh.thickness))
+
+
+def step_arrays(mesh: mg.Mesh, step: dict, prefix: str) -> dict:
+    nn, nd = mesh.nnodes, mesh.ndofpn
+    u = np.zeros((nn, nd))
+    eq = np.zeros((nn, nd), np.int32)
+    for node, dof, e, v in step["u"]:
+        u[node - 1, dof - 1] = v
+        eq[node - 1, dof - 1] = e
+    ngp = {1: 8, 2: 4, 3: 1}[mesh.elem_type]
+    ns = 3 if mesh.elem_type == mg.ELEM_PLANESTRESS2D else 6
+    sig = np.zeros((mesh.nelem, ngp, ns))
+    eps = np.zeros((mesh.nelem, ngp, ns))
+    kap = np.zeros((mesh.nelem, ngp))
+    om = np.zeros((mesh.nelem, ngp))
+    le = np.zeros((mesh.nelem, ngp))
+    for el, g, s, e, k, w, l in step["gp"]:
+        sig[el - 1, g - 1] = s
+        eps[el - 1, g - 1] = e
+        kap[el - 1, g - 1] = k
+        om[el - 1, g - 1] = w
+        le[el - 1, g - 1] = l
+    reac = np.zeros((nn, nd))
+    for node, dof, v in step["reac"]:
+        reac[node - 1, dof - 1] = v
+    return {f"{prefix}u": u, f"{prefix}eq": eq, f"{prefix}stress": sig, f"{prefix}strain": eps,
+            f"{prefix}kappa": kap, f"{prefix}omega": om, f"{prefix}le": le,
+            f"{prefix}reac": reac, f"{prefix}time": np.float64(step["time"])}
+
+
+def run_case(name, mesh, work, analysis="LinearStatic nsteps 1", dumpK=True, **deck_kw):
+    deck = os.path.join(work, name + ".in")
+    dump = os.path.join(work, name + ".dump")
+    write_deck(mesh, deck, analysis, **deck_kw)
+    cmd = [HARNESS, "-f", deck, "-o", dump] + (["-K"] if dumpK else [])
+    res = subprocess.run(cmd, cwd=work, capture_output=True, text=True)
+    if res.returncode != 0:
+        print(res.stdout[-3000:], res.stderr[-3000:])
+        raise RuntimeError(f"reference run failed for {name}")
+    log = res.stdout
+    steps, K, kes = parse_dump(dump)
+    out = mesh_arrays(mesh)
+    out["nsteps"] = np.int32(len(steps))
+    for k, st in enumerate(steps):
+        out.update(step_arrays(mesh, st, f"s{k + 1}_"))
+    if K is not None:
+        neq, colptr, rowind, val = K
+        out.update(K_colptr=colptr, K_rowind=rowind, K_val=val, neq=np.int32(neq))
+    for e, ke in kes.items():
+        out[f"ke{e}"] = ke
+    cg = re.findall(r"CG\(\w+\): flag=(\d+), nite (\d+), achieved tol\. (\S+)", log)
+    if cg:
+        out["cg_nite"] = np.array([int(c[1]) for c in cg], np.int32)
+    nr = re.findall(r"Equilibrium reached in\s+(\d+) iterations", log)
+    if nr:
+        out["nr_iters"] = np.array([int(v) for v in nr], np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: steps={len(steps)} neq={K[0] if K else '-'}")
+
+
+def patch300(ref_src):
+    """Golden values embedded in the reference's LTRSpace patch test deck."""
+    path = os.path.join(ref_src, "tests", "sm", "patch300.in")
+    rules = {"nodes": [], "reactions": []}
+    for ln in open(path):
+        m = re.match(r"#NODE tStep 1 number (\d+) dof (\d+) unknown d value (\S+)", ln)
+        if m:
+            rules["nodes"].append([int(m[1]), int(m[2]), float(m[3])])
+        m = re.match(r"#REACTION tStep 1 number (\d+) dof (\d+) value (\S+)", ln)
+        if m:
+            rules["reactions"].append([int(m[1]), int(m[2]), float(m[3])])
+        m = re.match(r"#%BEGIN_CHECK% tolerance (\S+)", ln)
+        if m:
+            rules["tolerance"] = float(m[1])
+    rules["source"] = "tests/sm/patch300.in"
+    with open(os.path.join(HERE, "patch300.json"), "w") as fh:
+        json.dump(rules, fh, indent=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-src", default="/root/reference")
+    ap.add_argument("--work", default=os.path.join(ROOT, "_work", "golden"))
+    ap.add_argument("--only", default="")
+    args = ap.parse_args()
+    os.makedirs(args.work, exist_ok=True)
+    patch300(args.ref_src)
+    cases = {
+        "hex_cantilever_20x4x4": lambda: run_case(
+            "hex_cantilever_20x4x4", mg.hex_cantilever(20, 4, 4), args.work),
+        "hex_cantilever_6x3x3_jit": lambda: run_case(
+            "hex_cantilever_6x3x3_jit", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work),
+        "quad_rve_8_s3": lambda: [run_case(
+            f"quad_rve_8_s3_lc{lc}", mg.quad_rve(8, seed=3, load_case=lc), args.work) for lc in range(3)],
+        "tet_cube_3_jit": lambda: run_case(
+            "tet_cube_3_jit", mg.tet_cube_linear(3, jitter=0.15, seed=5), args.work),
+    }
+    for name, fn in cases.items():
+        if args.only and args.only not in name:
+            continue
+        fn()
+
+
+if __name__ == "__main__":
+    main()
