@@ -1,0 +1,365 @@
+"""Benchmark: linear-static solve of the large jittered LSpace cantilever.
+
+Workload (one step): the 290x58x58 LSpace hex cantilever (h = 0.05 m, interior
+nodes jittered +-0.2h, seed 0; E = 210e9, nu = 0.3; x = 0 face fixed; 1e5 N in
+-z over the x = L face), 3,028,470 free DOFs. A step is the LinearStatic
+sequence on the GPU: element stiffness + deterministic assembly, load vector
+(f_ext - f_int of the prescribed field), mixed-precision Jacobi-PCG with FP64
+iterative refinement to ||f - K u||/||f|| <= 1e-8 (FP64 residual), solution
+scatter and reactions. value = free DOFs / step time (DOF/s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs independent replicas, one per GPU (the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
+WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
+RTOL = 1e-8
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per SpMV launch from the committed ncu summary (if any)."""
+    p = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except ValueError:
+            return None
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU side
+def cpu_sample(iters_full: int, nfree_full: int, nelem_full: int, nnz_full: int):
+    """Time the oracle (a serial C restatement of the reference path: location
+    arrays, CompCol-style pattern, element stiffness + scatter assembly, IML CG
+    with Jacobi) on a 58x12x12 cantilever of the same family, and scale per-unit
+    costs to the full workload: pattern + assembly per element, CG per nnz per
+    iteration times the FP64 iteration count of the full workload."""
+    from oofem_gb300 import meshgen as mg
+    from oracle import oracle as O
+    sm = mg.hex_cantilever(58, 12, 12, h=WORKLOAD["h"], jitter=WORKLOAD["jitter"], seed=1)
+    md = O.mesh_dict(sm)
+    t0 = time.perf_counter()
+    neq, _, eq = O.number_equations(sm.bc_mask)
+    loc = O.location_arrays(sm.conn, eq)
+    rp, ci = O.build_pattern(neq, loc)
+    val = O.assemble_tangent(md, loc, neq, rp, ci)
+    t_asm = time.perf_counter() - t0
+    b = np.zeros(neq)
+    free = eq > 0
+    b[eq[free] - 1] = sm.nodal_load[free]
+    n_it = 60
+    t0 = time.perf_counter()
+    O.pcg(rp, ci, val, b, rtol=1e-30, maxit=n_it)
+    t_cg = time.perf_counter() - t0
+    t_elem = t_asm / sm.nelem
+    t_nnz_it = t_cg / (n_it * ci.size)
+    t_full = t_elem * nelem_full + t_nnz_it * nnz_full * iters_full
+    return {"value": nfree_full / t_full, "unit": "DOF/s", "cores": 1, "kind": "port",
+            "sample": (f"oracle (serial C restatement) on a 58x12x12 cantilever ({neq} DOFs): "
+                       f"pattern+assembly {t_elem * 1e6:.1f} us/element, CG {t_nnz_it * 1e9:.3f} ns/nnz/iteration "
+                       f"({n_it} iterations); scaled to {nelem_full} elements, {nnz_full} nnz and the "
+                       f"{iters_full} FP64 PCG iterations the full workload needs to 1e-8"),
+            "seconds": t_asm + t_cg}
+
+
+def fp64_iterations():
+    """FP64 Jacobi-PCG iterations to 1e-8 on the full workload, as measured on a
+    GB300 by this bench (same algorithm as the reference's IML CG)."""
+    p = os.path.join(ROOT, "profiles", "bench_workload.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return int(d["fp64_iterations"]), "measured"
+    return 6000, "assumed"
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from oofem_gb300 import meshgen as mg
+    nx, ny, nz = WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"]
+    nelem = nx * ny * nz
+    nfree = nx * (ny + 1) * (nz + 1) * 3
+    # full-pattern nnz of the structured grid with the x=0 nodes fixed:
+    # 9 * sum_i cx(i) * sum_j cy(j) * sum_k cz(k) (3 DOFs per node, 3x3 node blocks)
+    nnz = 9 * (3 * nx - 2) * (3 * ny + 1) * (3 * nz + 1)
+    iters, src = fp64_iterations()
+    vals, secs = [], []
+    for k in range(args.warmup + args.steps):
+        s = cpu_sample(iters, nfree, nelem, nnz)
+        if k >= args.warmup:
+            vals.append(s["value"])
+            secs.append(s["seconds"])
+    v = statistics.median(vals)
+    cb = dict(s)
+    cb["value"] = v
+    cb.pop("seconds", None)
+    cb["sample"] += f" (iteration count {src})"
+    out = {"metric": METRIC, "value": v, "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": "hex_cantilever_%dx%dx%d_jitter0.2_seed0" % (WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"]),
+                   "free_dofs": nfree,
+                      "elements": nelem, "rtol": RTOL},
+           "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ----------------------------------------------------------------------------- GPU side
+def run_gpu(args):
+    import torch
+    from oofem_gb300 import meshgen as mg, native
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    if args.nx:
+        WORKLOAD.update(nx=args.nx, ny=args.ny, nz=args.nz)
+    mesh = mg.hex_cantilever(WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"], h=WORKLOAD["h"],
+                             jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"] + rank)
+    nfree = mesh.nfree
+    ctx = native.Context(local)
+    model = native.GpuModel(ctx, mesh)
+    A = native.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    nnz = A.nnz
+    bcv = torch.from_numpy(mesh.bc_value.ravel()).to(dev)
+    load = torch.from_numpy(mesh.nodal_load.ravel()).to(dev)
+    u = torch.zeros_like(bcv)
+    reac = torch.zeros_like(bcv)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    lib = ctx.lib
+    import ctypes as C
+
+    def step(prec):
+        info = native.SolveInfo()
+        code = lib.ogb_linear_static_dev(model.h, A.h, C.c_void_p(bcv.data_ptr()), C.c_void_p(load.data_ptr()),
+                                         RTOL, 200000, prec, C.c_void_p(u.data_ptr()),
+                                         C.c_void_p(reac.data_ptr()), C.byref(info))
+        if code != 0:
+            raise native.OgbError(code, lib.ogb_last_error().decode())
+        return info
+
+    def timed(prec, k, w, profile=False):
+        for _ in range(w):
+            step(prec)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        if profile:
+            ctx.profile(True)
+            ctx.profile_read()
+        l0 = ctx.kernel_launches()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        infos = []
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(k):
+                infos.append(step(prec))
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / k
+        launches = (ctx.kernel_launches() - l0) / k
+        prof = ctx.profile_read() if profile else None
+        if profile:
+            ctx.profile(False)
+        return ms, infos, launches, prof
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, infos, launches, prof = timed(native.PREC_MIXED, args.steps, args.warmup, profile=True)
+    clk = clocks.stop()
+    # FP64 drop-in path: iteration count and DOF/s for the mixed/FP64 ratio
+    ms64, infos64, _, _ = timed(native.PREC_FP64, 1, 1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * nfree / (ms * 1e-3)
+
+    # end to end through the host API: mesh upload, pattern, assembly, solve, copy back
+    def e2e_once():
+        c2 = native.Context(local)
+        m2 = native.GpuModel(c2, mesh)
+        A2 = native.GpuCsrMtrx(c2)
+        uh, rh, info = m2.linear_static(A2, rtol=RTOL, maxit=200000, precision=native.PREC_MIXED)
+        A2.close()
+        m2.close()
+        c2.close()
+        return info
+    e2e_s = float("nan")
+    if not args.no_e2e:
+        e2e_once()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_e2e = 2
+        for _ in range(n_e2e):
+            e2e_once()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+    h2d = (mesh.coords.nbytes + mesh.conn.nbytes + mesh.elem_mat.nbytes + mesh.material_table().nbytes
+           + mesh.bc_mask.nbytes + mesh.bc_value.nbytes + mesh.nodal_load.nbytes)
+    d2h = 2 * mesh.bc_value.nbytes
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    sp_ms, sp_n, sp_bytes = prof
+    achieved = (sp_bytes / sp_n) / (sp_ms / sp_n * 1e-3) / 1e9 if sp_n else None
+    traffic = profile_traffic()
+    info = infos[-1]
+    cb = None
+    if ws == 1 and not args.no_cpu:
+        cb = cpu_sample(infos64[-1].iterations, nfree, mesh.nelem, nnz)
+        cb.pop("seconds", None)
+    out = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "config": {"workload": "hex_cantilever_%dx%dx%d_jitter0.2_seed0" % (WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"]),
+                   "free_dofs": nfree,
+                   "elements": mesh.nelem, "nnz": nnz, "rtol": RTOL, "precision": "mixed FP32 PCG + FP64 IR",
+                   "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9),
+                   "parallelism": f"replicas x{ws}"},
+        "solve": {"inner_iterations": info.iterations, "outer": info.outer, "achieved": info.achieved},
+        "fp64": {"value": nfree / (ms64 * 1e-3), "ms_per_step": ms64, "iterations": infos64[-1].iterations,
+                 "achieved": infos64[-1].achieved},
+        "mixed_over_fp64": ms64 / ms,
+        "roofline": {"bound": "hbm", "kernel": "k_spmv (CSR, FP32 values, fused p.q)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_kind": peak_kind,
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "spmv_launches_per_step": sp_n / args.steps if sp_n else 0,
+                     "spmv_ms_per_step": sp_ms / args.steps if sp_n else 0},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "e2e": {"value": ws * nfree / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "seconds": e2e_s},
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nx", type=int, default=0, help="profiling only: smaller cantilever")
+    ap.add_argument("--ny", type=int, default=0)
+    ap.add_argument("--nz", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * oofem_gb300 -- GB300-native (sm_103a) structural hot path of OOFEM behind a C ABI.
+ *
+ * Plain C types only (pointers, sizes, int status codes); no exception crosses
+ * this boundary. Every call returns OGB_OK (0) or a negative OGB_E* code; the
+ * message of the last failure on the calling thread is ogb_last_error().
+ *
+ * Conventions (follow the reference):
+ *   - element types: OGB_LSPACE (8-node hex, 2x2x2 Gauss), OGB_PLANESTRESS2D
+ *     (4-node quad, 2x2 Gauss, thickness), OGB_LTRSPACE (4-node tet, 1 point).
+ *   - element node order as FEI3dHexaLin / FEI2dQuadLin / FEI3dTetLin
+ *     (src/core/fei3dhexalin.C:45-63, fei2dquadlin.C:60-72, fei3dtetlin.C:45-55).
+ *   - equation numbers: nodes in input order, DOFs in node order (u,v[,w]);
+ *     free DOFs 1..neq, prescribed DOFs -1..-npeq (engngm.C:469-530,
+ *     masterdof.C:105-120). Location arrays are 1-based, 0 = prescribed.
+ *   - CSR (row pointers int64, column indices int32, 0-based, sorted) of the full
+ *     symmetric pattern == CompCol colptr/rowind (compcol.C:174-272).
+ *   - Voigt order xx,yy,zz,yz,zx,xy (3-D) / xx,yy,xy (plane stress).
+ *   - material table: rows of 8 doubles {kind, E, nu, sig0, H, e0, gf, 0},
+ *     kind OGB_MAT_ISOLE / OGB_MAT_MISES / OGB_MAT_IDM1.
+ *   - "host" entry points take host pointers and copy; "_dev" entry points take
+ *     device pointers of the library's device and never copy to the host.
+ *
+ * Streams: every handle owns one CUDA stream (ogb_ctx_stream); calls are
+ * asynchronous on it unless they return host data.
+ */
+#ifndef OOFEM_GB300_H
+#define OOFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define OGB_API __attribute__((visibility("default")))
+#else
+#define OGB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OGB_OK 0
+#define OGB_E_ARG -1        /* bad argument / size mismatch */
+#define OGB_E_CUDA -2       /* CUDA runtime error */
+#define OGB_E_STATE -3      /* call out of order (e.g. no structure yet) */
+#define OGB_E_PATTERN -4    /* location outside the sparsity pattern */
+#define OGB_E_NOTCONV -5    /* solver did not converge (CR_DIVERGED_ITS) */
+#define OGB_E_BREAKDOWN -6  /* PCG breakdown: rho or p'q <= 0 or not finite */
+#define OGB_E_ZERODIAG -7   /* zero diagonal (DiagPreconditioner::init error) */
+#define OGB_E_MESH -8       /* invalid mesh (e.g. negative tet volume) */
+#define OGB_E_LIMIT -9      /* a fixed capacity of the library was exceeded */
+
+#define OGB_LSPACE 1
+#define OGB_PLANESTRESS2D 2
+#define OGB_LTRSPACE 3
+
+#define OGB_MAT_ISOLE 1
+#define OGB_MAT_MISES 2
+#define OGB_MAT_IDM1 3
+
+/* Precision of a solve. FP64 is the drop-in (IML CG + DiagPreconditioner
+ * semantics); MIXED stores and applies an FP32 matrix inside an FP64
+ * iterative-refinement loop whose residual is evaluated in FP64. */
+#define OGB_PREC_FP64 0
+#define OGB_PREC_MIXED 1
+
+typedef struct ogb_ctx ogb_ctx;       /* device + stream */
+typedef struct ogb_mtrx ogb_mtrx;     /* GPU compressed sparse matrix (SparseMtrx) */
+typedef struct ogb_model ogb_model;   /* GPU element backend for one mesh */
+
+/* ---- library / context ---------------------------------------------------- */
+OGB_API const char *ogb_last_error(void);
+OGB_API int ogb_version(void);
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+OGB_API int ogb_ctx_create(int device, ogb_ctx **out);
+OGB_API int ogb_ctx_destroy(ogb_ctx *ctx);
+OGB_API void *ogb_ctx_stream(ogb_ctx *ctx);                 /* cudaStream_t */
+OGB_API int ogb_ctx_synchronize(ogb_ctx *ctx);
+/* Number of kernels this library launched on the context since creation. */
+OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
+/* Kernel timing: when enabled, every SpMV launch (the dominant kernel of the
+ * solve) is bracketed by CUDA events on the context stream; ogb_ctx_profile_read
+ * returns the summed device time (ms), the launch count and the algorithmic
+ * bytes of those launches (values + column indices + row pointers + x + y),
+ * and resets the counters. No reference counterpart (instrumentation). */
+OGB_API int ogb_ctx_profile_enable(ogb_ctx *ctx, int enable);
+OGB_API int ogb_ctx_profile_read(ogb_ctx *ctx, double *total_ms, int64_t *launches, double *bytes);
+
+/* ---- sparse matrix: replaces SparseMtrx (src/core/sparsemtrx.h:62-303) ------ */
+/* CTOR<SparseMtrx,T> / classFactory.createSparseMtrx (classfactory.h:125,149). */
+OGB_API int ogb_mtrx_create(ogb_ctx *ctx, ogb_mtrx **out);
+OGB_API int ogb_mtrx_destroy(ogb_mtrx *m);
+/* SparseMtrx::buildInternalStructure (sparsemtrx.h:198; CompCol compcol.C:174-272):
+ * pattern from element location arrays (1-based, 0 = skip), element e owning
+ * loc[loc_ptr[e] .. loc_ptr[e+1]). Host pointers. Values are zeroed. */
+OGB_API int ogb_mtrx_build_structure(ogb_mtrx *m, int neq, int nelem, const int64_t *loc_ptr,
+                             const int *loc);
+OGB_API int ogb_mtrx_neq(ogb_mtrx *m, int *neq);
+OGB_API int ogb_mtrx_nnz(ogb_mtrx *m, int64_t *nnz);
+/* Copy the pattern out (host buffers of neq+1 and nnz entries). */
+OGB_API int ogb_mtrx_pattern(ogb_mtrx *m, int64_t *rowptr, int *colind);
+/* Copy the values out (host, nnz doubles, CSR order). */
+OGB_API int ogb_mtrx_values(ogb_mtrx *m, double *val);
+/* SparseMtrx::zero (sparsemtrx.h:254). */
+OGB_API int ogb_mtrx_zero(ogb_mtrx *m);
+/* SparseMtrx::assembleBegin (sparsemtrx.h:234). */
+OGB_API int ogb_mtrx_assemble_begin(ogb_mtrx *m);
+/* SparseMtrx::assemble(loc, mat) (sparsemtrx.h:220; CompCol::assemble compcol.C:275-316):
+ * stage one n x n element matrix; `ke_colmajor` is FloatMatrix storage (column-major).
+ * Host pointers, copied; applied in call order at ogb_mtrx_assemble_end. */
+OGB_API int ogb_mtrx_assemble(ogb_mtrx *m, int n, const int *loc, const double *ke_colmajor);
+/* SparseMtrx::assembleEnd (sparsemtrx.h:236; called by EngngModel::assemble,
+ * engngm.C:1035-1036): adds every staged element matrix on the device in a fixed
+ * order (deterministic, no floating-point atomics). */
+OGB_API int ogb_mtrx_assemble_end(ogb_mtrx *m);
+/* SparseMtrx::times (sparsemtrx.h:137): y = A x, host vectors of neq. */
+OGB_API int ogb_mtrx_times(ogb_mtrx *m, const double *x, double *y);
+OGB_API int ogb_mtrx_times_dev(ogb_mtrx *m, const double *x_dev, double *y_dev);
+/* SparseMtrx::at(i,j) (sparsemtrx.h:265-267), 1-based; read and scale-in-place
+ * (NRSolver::applyConstraintsToStiffness does at(i,i) *= 1e6, nrsolver.C:501-503). */
+OGB_API int ogb_mtrx_at(ogb_mtrx *m, int i, int j, double *value);
+OGB_API int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value);
+/* SparseMtrx::giveVersion (sparsemtrx.h:82): bumped on every mutation. */
+OGB_API int ogb_mtrx_version(ogb_mtrx *m, int64_t *version);
+
+/* ---- linear solver: replaces SparseLinearSystemNM::solve
+ *      (src/core/sparselinsystemnm.h:81; IMLSolver::solve imlsolver.C:101-147,
+ *      IML++ CG iml/cg.h:22-71, DiagPreconditioner diagpre.C:40-67) --------- */
+typedef struct ogb_solve_info {
+    int iterations;       /* PCG iterations (sum of inner iterations for MIXED) */
+    int outer;            /* iterative-refinement sweeps (MIXED), 0 for FP64 */
+    double achieved;      /* final relative residual ||r||/||b|| (FP64 for MIXED) */
+    int status;           /* OGB_OK / OGB_E_NOTCONV / OGB_E_BREAKDOWN / OGB_E_ZERODIAG */
+} ogb_solve_info;
+
+/* Solve A x = b to ||r||/||b|| <= rtol within maxit iterations; x holds the
+ * initial guess on entry (IML CG semantics). Host vectors of neq doubles. */
+OGB_API int ogb_pcg_solve(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit,
+                  int precision, ogb_solve_info *info);
+OGB_API int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b_dev, double *x_dev, double rtol,
+                      int maxit, int precision, ogb_solve_info *info);
+
+/* ---- element backend: LSpace / PlaneStress2d / LTRSpace element loops
+ *      (NLStructuralElement::computeStiffnessMatrix nlstructuralelement.C:332-446,
+ *      ::giveInternalForcesVector :151-240; EngngModel::assemble engngm.C:889-1037,
+ *      assembleVectorFromElements :1351-1533) ----------------------------------- */
+/* coords: nnodes x ndim; conn: nelem x nnpe (0-based); elem_mat: nelem;
+ * mats: nmat x 8; bc_mask: nnodes x ndofpn (1 = prescribed). Host pointers. */
+OGB_API int ogb_model_create(ogb_ctx *ctx, int etype, int nnodes, const double *coords, int nelem,
+                     const int *conn, const int *elem_mat, int nmat, const double *mats,
+                     double thickness, const uint8_t *bc_mask, ogb_model **out);
+OGB_API int ogb_model_destroy(ogb_model *md);
+OGB_API int ogb_model_neq(ogb_model *md, int *neq, int *npeq);
+/* Equation numbers (nnodes x ndofpn, +free / -prescribed), host copy. */
+OGB_API int ogb_model_equations(ogb_model *md, int *eq);
+/* Build the CSR pattern of this mesh into m and the element-to-CSR scatter map
+ * (replaces buildInternalStructure for a mesh whose elements live on the GPU). */
+OGB_API int ogb_model_build_matrix(ogb_model *md, ogb_mtrx *m);
+/* Tangent stiffness K = sum_e sum_gp B^T D B dV into m (K1 element kernel + K4
+ * deterministic gather assembly). Uses the material state of the last stress
+ * evaluation (temp values), like TangentAssembler after InternalRhs. */
+OGB_API int ogb_model_assemble_stiffness(ogb_model *md, ogb_mtrx *m);
+/* Internal forces f = sum_e sum_gp B^T sigma dV for the total node displacement
+ * field u_node (nnodes x ndofpn, prescribed values included); node-indexed
+ * output, deterministic. Updates the temp material state. */
+OGB_API int ogb_model_internal_forces(ogb_model *md, const double *u_node, double *f_node);
+OGB_API int ogb_model_internal_forces_dev(ogb_model *md, const double *u_node_dev, double *f_node_dev);
+/* Gauss-point stresses / strains of the last internal-force evaluation
+ * (nelem x ngp x nstress), host copy. */
+OGB_API int ogb_model_gp_stress(ogb_model *md, double *stress, double *strain);
+/* Material state: accept temp values as committed (MaterialStatus::updateYourself). */
+OGB_API int ogb_model_commit_state(ogb_model *md);
+/* Per-GP state (nelem x ngp x 4): kappa, omega, Le, spare (committed). */
+OGB_API int ogb_model_gp_state(ogb_model *md, double *state4);
+
+/* LinearStatic::solveYourselfAt (linearstatic.C:177-253) in one call: build
+ * the pattern (once), assemble K, load = f_ext - f_int(prescribed), PCG, node
+ * displacements and reactions (structengngmodel.C:183-201). Host arrays:
+ * bc_value/nodal_load/u_node/reactions are nnodes x ndofpn. */
+OGB_API int ogb_linear_static(ogb_model *md, ogb_mtrx *m, const double *bc_value,
+                      const double *nodal_load, double rtol, int maxit, int precision,
+                      double *u_node, double *reactions, ogb_solve_info *info);
+/* Same with device-resident inputs/outputs (no host copies). */
+OGB_API int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bc_value_dev,
+                          const double *nodal_load_dev, double rtol, int maxit,
+                          int precision, double *u_node_dev, double *reactions_dev,
+                          ogb_solve_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

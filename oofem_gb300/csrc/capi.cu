@@ -1,0 +1,838 @@
+// C ABI of liboofem_gb300 (declared in include/oofem_gb300.h): handle
+// management, host<->device staging, and the LinearStatic driver sequence.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace ogb {
+
+static thread_local std::string g_last_error;
+}  // namespace ogb
+extern "C" void ogb_ctx_free_impl(ogb_ctx *ctx);
+namespace ogb {
+static void ctx_free(ogb_ctx *ctx) { ogb_ctx_free_impl(ctx); }
+
+void ctx_release(ogb_ctx *ctx)
+{
+    if (--ctx->refs == 0 && ctx->closing) ctx_free(ctx);
+}
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg)
+{
+    set_error(msg);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return OGB_E_CUDA;
+}
+
+int check_device_status(ogb_ctx *ctx, const char *where)
+{
+    OGB_CUDA(cudaMemcpyAsync(ctx->h_status.p, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    int s = *ctx->h_status.p;
+    if (s == DS_OK) return OGB_OK;
+    OGB_CUDA(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+    std::string w(where);
+    switch (s) {
+    case DS_LIMIT: return fail(OGB_E_LIMIT, w + ": a per-node/per-row capacity was exceeded");
+    case DS_PATTERN: return fail(OGB_E_PATTERN, w + ": location outside the sparsity pattern");
+    case DS_NEGVOL: return fail(OGB_E_MESH, w + ": negative volume (tetrahedron with detJ <= 0)");
+    }
+    return fail(OGB_E_STATE, w + ": device error");
+}
+
+static cudaEvent_t take_event(ogb_ctx *ctx)
+{
+    if (ctx->ev_pool.empty()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        return e;
+    }
+    cudaEvent_t e = ctx->ev_pool.back();
+    ctx->ev_pool.pop_back();
+    return e;
+}
+
+void prof_begin(ogb_ctx *ctx)
+{
+    if (!ctx->prof) return;
+    cudaEvent_t e = take_event(ctx);
+    if (!e) return;
+    cudaEventRecord(e, ctx->stream);
+    ctx->ev_pending.push_back(e);
+}
+
+void prof_end(ogb_ctx *ctx, double bytes)
+{
+    if (!ctx->prof || ctx->ev_pending.size() % 2 == 0) return;
+    cudaEvent_t e = take_event(ctx);
+    if (!e) {
+        ctx->ev_pool.push_back(ctx->ev_pending.back());
+        ctx->ev_pending.pop_back();
+        return;
+    }
+    cudaEventRecord(e, ctx->stream);
+    ctx->ev_pending.push_back(e);
+    ctx->pending_bytes += bytes;
+    ctx->prof_count++;
+}
+
+// Sum the elapsed time of completed start/stop pairs (call after a stream sync).
+void prof_harvest(ogb_ctx *ctx)
+{
+    size_t n = ctx->ev_pending.size() & ~(size_t)1;
+    for (size_t k = 0; k < n; k += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->ev_pending[k], ctx->ev_pending[k + 1]) == cudaSuccess) ctx->prof_ms += ms;
+        ctx->ev_pool.push_back(ctx->ev_pending[k]);
+        ctx->ev_pool.push_back(ctx->ev_pending[k + 1]);
+    }
+    ctx->ev_pending.erase(ctx->ev_pending.begin(), ctx->ev_pending.begin() + n);
+    ctx->prof_bytes += ctx->pending_bytes;
+    ctx->pending_bytes = 0.0;
+}
+
+namespace {
+
+__global__ void k_u_from_bc(int n, const int *eq, const double *bcval, double *u)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[i] = eq[i] < 0 ? bcval[i] : 0.0;
+}
+
+// b[eq-1] = f_ext - f_int at free DOFs; padding untouched (zero).
+__global__ void k_build_rhs(int n, const int *eq, const double *fext, const double *fint, double *b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && eq[i] > 0) b[eq[i] - 1] = (fext ? fext[i] : 0.0) - fint[i];
+}
+
+__global__ void k_scatter_solution(int n, const int *eq, const double *x, double *u)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && eq[i] > 0) u[i] = x[eq[i] - 1];
+}
+
+// StructuralEngngModel::computeReaction (structengngmodel.C:183-201): internal
+// minus external forces at prescribed DOFs.
+__global__ void k_reactions(int n, const int *eq, const double *fint, const double *fext, double *reac)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) reac[i] = eq[i] < 0 ? fint[i] - (fext ? fext[i] : 0.0) : 0.0;
+}
+
+__global__ void k_commit_state(int64_t ngp_total, const int *emat, const double *mats, int ngp, double *state)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ngp_total) return;
+    int e = (int)(t / ngp);
+    int kind = (int)mats[8 * emat[e]];
+    double *st = state + t * NSTATE;
+    if (kind == OGB_MAT_MISES) {
+        for (int i = 0; i < 7; ++i) st[i] = st[8 + i];
+    } else if (kind == OGB_MAT_IDM1) {
+        st[0] = st[8];
+        st[1] = st[9];
+    }
+}
+
+__global__ void k_gp_state(int64_t ngp_total, const int *emat, const double *mats, int ngp, const double *state,
+                           double *out4)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ngp_total) return;
+    int e = (int)(t / ngp);
+    int kind = (int)mats[8 * emat[e]];
+    const double *st = state + t * NSTATE;
+    double k = 0, w = 0, le = 0;
+    if (kind == OGB_MAT_MISES) {
+        k = st[6];
+    } else if (kind == OGB_MAT_IDM1) {
+        k = st[0];
+        w = st[1];
+        le = st[2];
+    }
+    out4[t * 4 + 0] = k;
+    out4[t * 4 + 1] = w;
+    out4[t * 4 + 2] = le;
+    out4[t * 4 + 3] = 0.0;
+}
+
+inline unsigned nb(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
+
+// General inverse (Gauss-Jordan, partial pivoting), n <= 6.
+void inv_n(int n, const double *A, double *Ai)
+{
+    double M[6][12];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < 2 * n; ++j) M[i][j] = j < n ? A[i * n + j] : (j - n == i ? 1.0 : 0.0);
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+        if (p != c)
+            for (int j = 0; j < 2 * n; ++j) std::swap(M[c][j], M[p][j]);
+        double piv = M[c][c];
+        for (int j = 0; j < 2 * n; ++j) M[c][j] /= piv;
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            double f = M[r][c];
+            if (f != 0.0)
+                for (int j = 0; j < 2 * n; ++j) M[r][j] -= f * M[c][j];
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) Ai[i * n + j] = M[i][j + n];
+}
+
+// IsotropicLinearElasticMaterial::initTangents (isolinearelasticmaterial.C:80-88):
+// D = 2G I_dev6 + K I6(x)I6; plane stress = inverse of the (xx,yy,xy) block of
+// the 3-D compliance (linearelasticmaterial.C:62-79).
+void isotropic_D(int etype, double E, double nu, double *D)
+{
+    double G = E / (2.0 * (1. + nu));
+    double K = E / (3.0 * (1. - 2. * nu));
+    double D6[36];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double idev = (i < 3 && j < 3) ? (i == j ? 2. / 3. : -1. / 3.) : (i == j ? 0.5 : 0.0);
+            double ii = (i < 3 && j < 3) ? 1.0 : 0.0;
+            D6[i * 6 + j] = 2 * G * idev + K * ii;
+        }
+    if (etype != OGB_PLANESTRESS2D) {
+        memcpy(D, D6, sizeof(D6));
+        return;
+    }
+    double C[36], R[9];
+    inv_n(6, D6, C);
+    const int idx[3] = {0, 1, 5};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) R[i * 3 + j] = C[idx[i] * 6 + idx[j]];
+    memset(D, 0, 36 * sizeof(double));
+    inv_n(3, R, D);
+}
+
+int upload_padded(ogb_mtrx *m, const double *src, double *dst, bool from_host)
+{
+    cudaStream_t s = m->ctx->stream;
+    OGB_CUDA(cudaMemcpyAsync(dst, src, (size_t)m->neq * sizeof(double),
+                             from_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    if (m->npad > m->neq)
+        OGB_CUDA(cudaMemsetAsync(dst + m->neq, 0, (size_t)(m->npad - m->neq) * sizeof(double), s));
+    return OGB_OK;
+}
+
+int solve_padded(ogb_mtrx *m, double rtol, int maxit, int precision, ogb_solve_info *info)
+{
+    ogb_solve_info tmp{};
+    ogb_solve_info *inf = info ? info : &tmp;
+    int r = precision == OGB_PREC_MIXED ? pcg_mixed(m, m->w_b.p, m->w_x.p, rtol, maxit, inf)
+                                        : pcg_fp64(m, m->w_b.p, m->w_x.p, rtol, maxit, inf);
+    if (r != OGB_OK) return r;
+    if (inf->status != OGB_OK) {
+        const char *why = inf->status == OGB_E_ZERODIAG ? "zero diagonal detected"
+                          : inf->status == OGB_E_BREAKDOWN ? "PCG breakdown (rho or p'q not positive/finite)"
+                                                          : "PCG did not converge within maxit";
+        set_error(why);
+    }
+    return inf->status;
+}
+
+int ensure_solver_vectors(ogb_mtrx *m)
+{
+    OGB_CHECK(m->w_x.alloc(m->npad));
+    OGB_CHECK(m->w_b.alloc(m->npad));
+    return OGB_OK;
+}
+
+}  // namespace
+}  // namespace ogb
+
+using namespace ogb;
+
+extern "C" {
+
+const char *ogb_last_error(void) { return g_last_error.c_str(); }
+
+int ogb_version(void) { return 1; }
+
+int ogb_ctx_create(int device, ogb_ctx **out)
+{
+    if (!out) return fail(OGB_E_ARG, "null output");
+    OGB_CUDA(cudaSetDevice(device));
+    ogb_ctx *c = new ogb_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    int r = c->status.alloc(1);
+    if (r == OGB_OK) r = c->h_status.alloc(1);
+    if (r != OGB_OK) {
+        delete c;
+        return r;
+    }
+    OGB_CUDA(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+    *out = c;
+    return OGB_OK;
+}
+
+void ogb_ctx_free_impl(ogb_ctx *ctx)
+{
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    prof_harvest(ctx);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ev_pending) cudaEventDestroy(e);
+    ctx->status.release();
+    ctx->h_status.release();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+// A context outlives its matrices and models: destroying it while some are
+// alive only marks it; the last child to go frees it.
+int ogb_ctx_destroy(ogb_ctx *ctx)
+{
+    if (!ctx) return OGB_OK;
+    if (ctx->refs > 0) {
+        ctx->closing = true;
+        return OGB_OK;
+    }
+    ogb_ctx_free_impl(ctx);
+    return OGB_OK;
+}
+
+void *ogb_ctx_stream(ogb_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int ogb_ctx_synchronize(ogb_ctx *ctx)
+{
+    if (!ctx) return fail(OGB_E_ARG, "null context");
+    OGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OGB_OK;
+}
+
+int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int ogb_ctx_profile_enable(ogb_ctx *ctx, int enable)
+{
+    if (!ctx) return fail(OGB_E_ARG, "null context");
+    OGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    prof_harvest(ctx);
+    ctx->prof = enable != 0;
+    return OGB_OK;
+}
+
+int ogb_ctx_profile_read(ogb_ctx *ctx, double *total_ms, int64_t *launches, double *bytes)
+{
+    if (!ctx) return fail(OGB_E_ARG, "null context");
+    OGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    prof_harvest(ctx);
+    if (total_ms) *total_ms = ctx->prof_ms;
+    if (launches) *launches = ctx->prof_count;
+    if (bytes) *bytes = ctx->prof_bytes;
+    ctx->prof_ms = 0.0;
+    ctx->prof_bytes = 0.0;
+    ctx->prof_count = 0;
+    return OGB_OK;
+}
+
+// ------------------------------------------------------------------ matrix
+int ogb_mtrx_create(ogb_ctx *ctx, ogb_mtrx **out)
+{
+    if (!ctx || !out) return fail(OGB_E_ARG, "null argument");
+    ogb_mtrx *m = new ogb_mtrx();
+    m->ctx = ctx;
+    m->st_ptr.assign(1, 0);
+    ctx->refs++;
+    *out = m;
+    return OGB_OK;
+}
+
+int ogb_mtrx_destroy(ogb_mtrx *m)
+{
+    if (!m) return OGB_OK;
+    ogb_ctx *ctx = m->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete m;
+    ctx_release(ctx);
+    return OGB_OK;
+}
+
+int ogb_mtrx_build_structure(ogb_mtrx *m, int neq, int nelem, const int64_t *loc_ptr, const int *loc)
+{
+    if (!m || neq < 0 || nelem < 0 || (nelem > 0 && (!loc_ptr || !loc))) return fail(OGB_E_ARG, "bad argument");
+    for (int e = 0; e < nelem; ++e) {
+        if (loc_ptr[e + 1] < loc_ptr[e]) return fail(OGB_E_ARG, "loc_ptr not monotone");
+    }
+    for (int64_t k = 0; k < (nelem > 0 ? loc_ptr[nelem] : 0); ++k)
+        if (loc[k] < 0 || loc[k] > neq) return fail(OGB_E_ARG, "location outside 0..neq");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    int64_t zero_ptr = 0;
+    OGB_CHECK(build_loc_pattern(m, neq, nelem, nelem > 0 ? loc_ptr : &zero_ptr, loc));
+    m->spmv_tpr = pick_tpr(m);
+    m->st_ptr.assign(1, 0);
+    return OGB_OK;
+}
+
+int ogb_mtrx_neq(ogb_mtrx *m, int *neq)
+{
+    if (!m || !neq) return fail(OGB_E_ARG, "null argument");
+    *neq = m->neq;
+    return OGB_OK;
+}
+
+int ogb_mtrx_nnz(ogb_mtrx *m, int64_t *nnz)
+{
+    if (!m || !nnz) return fail(OGB_E_ARG, "null argument");
+    *nnz = m->nnz;
+    return OGB_OK;
+}
+
+int ogb_mtrx_pattern(ogb_mtrx *m, int64_t *rowptr, int *colind)
+{
+    if (!m || !rowptr || !colind) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    cudaStream_t s = m->ctx->stream;
+    OGB_CUDA(cudaMemcpyAsync(rowptr, m->rowptr.p, (m->neq + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaMemcpyAsync(colind, m->colind.p, m->nnz * sizeof(int), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_mtrx_values(ogb_mtrx *m, double *val)
+{
+    if (!m || !val) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaMemcpyAsync(val, m->val.p, m->nnz * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return OGB_OK;
+}
+
+int ogb_mtrx_zero(ogb_mtrx *m)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaMemsetAsync(m->val.p, 0, m->nnz * sizeof(double), m->ctx->stream));
+    m->version++;
+    return OGB_OK;
+}
+
+int ogb_mtrx_assemble_begin(ogb_mtrx *m)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    m->st_ptr.assign(1, 0);
+    m->st_loc.clear();
+    m->st_keoff.clear();
+    m->st_ke.clear();
+    return OGB_OK;
+}
+
+int ogb_mtrx_assemble(ogb_mtrx *m, int n, const int *loc, const double *ke)
+{
+    if (!m || n < 0 || (n > 0 && (!loc || !ke))) return fail(OGB_E_ARG, "bad argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    for (int i = 0; i < n; ++i)
+        if (loc[i] < 0 || loc[i] > m->neq) return fail(OGB_E_ARG, "location outside 0..neq");
+    m->st_keoff.push_back((int64_t)m->st_ke.size());
+    m->st_loc.insert(m->st_loc.end(), loc, loc + n);
+    m->st_ptr.push_back((int64_t)m->st_loc.size());
+    m->st_ke.insert(m->st_ke.end(), ke, ke + (size_t)n * n);
+    return OGB_OK;
+}
+
+int ogb_mtrx_assemble_end(ogb_mtrx *m)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    return staged_assemble(m);
+}
+
+int ogb_mtrx_times(ogb_mtrx *m, const double *x, double *y)
+{
+    if (!m || !x || !y) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    OGB_CHECK(ensure_solver_vectors(m));
+    OGB_CHECK(upload_padded(m, x, m->w_x.p, true));
+    OGB_CHECK(spmv64(m, m->w_x.p, m->w_b.p));
+    OGB_CUDA(cudaMemcpyAsync(y, m->w_b.p, m->neq * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return OGB_OK;
+}
+
+int ogb_mtrx_times_dev(ogb_mtrx *m, const double *x, double *y)
+{
+    if (!m || !x || !y) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CHECK(ensure_solver_vectors(m));
+    OGB_CHECK(upload_padded(m, x, m->w_x.p, false));
+    OGB_CHECK(spmv64(m, m->w_x.p, m->w_b.p));
+    OGB_CUDA(cudaMemcpyAsync(y, m->w_b.p, m->neq * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream));
+    return OGB_OK;
+}
+
+static int locate(ogb_mtrx *m, int i, int j, int64_t *pos)
+{
+    if (i < 1 || j < 1 || i > m->neq || j > m->neq) return fail(OGB_E_ARG, "index out of range");
+    int64_t rp[2];
+    cudaStream_t s = m->ctx->stream;
+    OGB_CUDA(cudaMemcpyAsync(rp, m->rowptr.p + (i - 1), 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> cols(rp[1] - rp[0]);
+    OGB_CUDA(cudaMemcpyAsync(cols.data(), m->colind.p + rp[0], cols.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    auto it = std::lower_bound(cols.begin(), cols.end(), j - 1);
+    if (it == cols.end() || *it != j - 1) return fail(OGB_E_PATTERN, "entry not in the sparsity pattern");
+    *pos = rp[0] + (it - cols.begin());
+    return OGB_OK;
+}
+
+int ogb_mtrx_at(ogb_mtrx *m, int i, int j, double *value)
+{
+    if (!m || !value) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    int64_t p;
+    int r = locate(m, i, j, &p);
+    if (r == OGB_E_PATTERN) {   // SparseMtrx::at of a structural zero reads 0
+        *value = 0.0;
+        return OGB_OK;
+    }
+    OGB_CHECK(r);
+    OGB_CUDA(cudaMemcpyAsync(value, m->val.p + p, sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return OGB_OK;
+}
+
+int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    int64_t p;
+    OGB_CHECK(locate(m, i, j, &p));
+    OGB_CUDA(cudaMemcpyAsync(m->val.p + p, &value, sizeof(double), cudaMemcpyHostToDevice, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    m->version++;
+    return OGB_OK;
+}
+
+int ogb_mtrx_version(ogb_mtrx *m, int64_t *version)
+{
+    if (!m || !version) return fail(OGB_E_ARG, "null argument");
+    *version = m->version;
+    return OGB_OK;
+}
+
+// ------------------------------------------------------------------ solver
+int ogb_pcg_solve(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, int precision,
+                  ogb_solve_info *info)
+{
+    if (!m || !b || !x) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    OGB_CHECK(ensure_solver_vectors(m));
+    OGB_CHECK(upload_padded(m, b, m->w_b.p, true));
+    OGB_CHECK(upload_padded(m, x, m->w_x.p, true));
+    int r = solve_padded(m, rtol, maxit, precision, info);
+    OGB_CUDA(cudaMemcpyAsync(x, m->w_x.p, m->neq * sizeof(double), cudaMemcpyDeviceToHost, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return r;
+}
+
+int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, int precision,
+                      ogb_solve_info *info)
+{
+    if (!m || !b || !x) return fail(OGB_E_ARG, "null argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CHECK(ensure_solver_vectors(m));
+    OGB_CHECK(upload_padded(m, b, m->w_b.p, false));
+    OGB_CHECK(upload_padded(m, x, m->w_x.p, false));
+    int r = solve_padded(m, rtol, maxit, precision, info);
+    OGB_CUDA(cudaMemcpyAsync(x, m->w_x.p, m->neq * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream));
+    return r;
+}
+
+// ------------------------------------------------------------------ element backend
+int ogb_model_create(ogb_ctx *ctx, int etype, int nnodes, const double *coords, int nelem, const int *conn,
+                     const int *elem_mat, int nmat, const double *mats, double thickness, const uint8_t *bc_mask,
+                     ogb_model **out)
+{
+    if (!ctx || !out || !coords || !conn || !elem_mat || !mats || !bc_mask || nnodes <= 0 || nelem <= 0 || nmat <= 0)
+        return fail(OGB_E_ARG, "bad argument");
+    if (etype != OGB_LSPACE && etype != OGB_PLANESTRESS2D && etype != OGB_LTRSPACE)
+        return fail(OGB_E_ARG, "unknown element type");
+    const int nnpe = etype == OGB_LSPACE ? 8 : 4;
+    const int ndofpn = etype == OGB_PLANESTRESS2D ? 2 : 3;
+    if ((int64_t)nelem >= (1LL << 26)) return fail(OGB_E_LIMIT, "more than 2^26 elements");
+    for (int64_t k = 0; k < (int64_t)nelem * nnpe; ++k)
+        if (conn[k] < 0 || conn[k] >= nnodes) return fail(OGB_E_ARG, "connectivity outside 0..nnodes-1");
+    bool nonlinear = false;
+    for (int i = 0; i < nmat; ++i) {
+        int kind = (int)mats[8 * i];
+        if (kind != OGB_MAT_ISOLE && kind != OGB_MAT_MISES && kind != OGB_MAT_IDM1)
+            return fail(OGB_E_ARG, "unknown material kind");
+        if (kind != OGB_MAT_ISOLE) {
+            if (etype == OGB_PLANESTRESS2D)
+                return fail(OGB_E_ARG, "misesmat/idm1 are supported for 3-D elements only");
+            nonlinear = true;
+        }
+    }
+    for (int e = 0; e < nelem; ++e)
+        if (elem_mat[e] < 0 || elem_mat[e] >= nmat) return fail(OGB_E_ARG, "element material out of range");
+    OGB_CUDA(cudaSetDevice(ctx->device));
+    ogb_model *md = new ogb_model();
+    md->ctx = ctx;
+    md->etype = etype;
+    md->nnodes = nnodes;
+    md->nelem = nelem;
+    md->nnpe = nnpe;
+    md->ndofpn = ndofpn;
+    md->ndim = etype == OGB_PLANESTRESS2D ? 2 : 3;
+    md->ngp = etype == OGB_LSPACE ? 8 : (etype == OGB_PLANESTRESS2D ? 4 : 1);
+    md->nstress = etype == OGB_PLANESTRESS2D ? 3 : 6;
+    md->nmat = nmat;
+    md->thickness = thickness;
+    md->nonlinear = nonlinear;
+    // a1: equation numbering (engngm.C:469-530, masterdof.C:105-120)
+    md->h_eq.resize((size_t)nnodes * ndofpn);
+    int neq = 0, npeq = 0;
+    for (size_t k = 0; k < md->h_eq.size(); ++k) md->h_eq[k] = bc_mask[k] ? -(++npeq) : ++neq;
+    md->neq = neq;
+    md->npeq = npeq;
+    std::vector<double> D((size_t)nmat * 36, 0.0);
+    for (int i = 0; i < nmat; ++i) isotropic_D(etype, mats[8 * i + 1], mats[8 * i + 2], &D[(size_t)36 * i]);
+    cudaStream_t s = ctx->stream;
+    int r = OGB_OK;
+    auto up = [&](auto &buf, const auto *src, size_t n) {
+        if (r != OGB_OK) return;
+        r = buf.alloc(n);
+        if (r == OGB_OK) {
+            cudaError_t e = cudaMemcpyAsync(buf.p, src, n * sizeof(*src), cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync");
+        }
+    };
+    up(md->coords, coords, (size_t)nnodes * md->ndim);
+    up(md->conn, conn, (size_t)nelem * nnpe);
+    up(md->emat, elem_mat, (size_t)nelem);
+    up(md->mats, mats, (size_t)nmat * 8);
+    up(md->Dmat, D.data(), D.size());
+    up(md->eq, md->h_eq.data(), md->h_eq.size());
+    size_t ngpt = (size_t)nelem * md->ngp;
+    if (r == OGB_OK) r = md->ke.alloc((size_t)nelem * nnpe * nnpe * ndofpn * ndofpn);
+    if (r == OGB_OK) r = md->fe.alloc((size_t)nelem * nnpe * ndofpn);
+    if (r == OGB_OK) r = md->gp_stress.alloc(ngpt * md->nstress);
+    if (r == OGB_OK) r = md->gp_strain.alloc(ngpt * md->nstress);
+    if (r == OGB_OK && nonlinear) {
+        r = md->state.alloc(ngpt * NSTATE);
+        if (r == OGB_OK) {
+            cudaError_t e = cudaMemsetAsync(md->state.p, 0, ngpt * NSTATE * sizeof(double), s);
+            if (e != cudaSuccess) r = cuda_fail(e, "cudaMemsetAsync");
+        }
+    }
+    if (r == OGB_OK) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) r = cuda_fail(e, "model upload");
+    }
+    if (r != OGB_OK) {
+        delete md;
+        return r;
+    }
+    ctx->refs++;
+    *out = md;
+    return OGB_OK;
+}
+
+int ogb_model_destroy(ogb_model *md)
+{
+    if (!md) return OGB_OK;
+    ogb_ctx *ctx = md->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete md;
+    ctx_release(ctx);
+    return OGB_OK;
+}
+
+int ogb_model_neq(ogb_model *md, int *neq, int *npeq)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (neq) *neq = md->neq;
+    if (npeq) *npeq = md->npeq;
+    return OGB_OK;
+}
+
+int ogb_model_equations(ogb_model *md, int *eq)
+{
+    if (!md || !eq) return fail(OGB_E_ARG, "null argument");
+    memcpy(eq, md->h_eq.data(), md->h_eq.size() * sizeof(int));
+    return OGB_OK;
+}
+
+int ogb_model_build_matrix(ogb_model *md, ogb_mtrx *m)
+{
+    if (!md || !m) return fail(OGB_E_ARG, "null argument");
+    if (md->ctx != m->ctx) return fail(OGB_E_ARG, "model and matrix on different contexts");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    OGB_CHECK(build_model_pattern(md, m));
+    m->spmv_tpr = pick_tpr(m);
+    md->bound = m;
+    return OGB_OK;
+}
+
+static int assemble_stiffness_async(ogb_model *md, ogb_mtrx *m)
+{
+    if (md->bound != m || !m->has_structure)
+        return fail(OGB_E_STATE, "matrix was not built from this model (ogb_model_build_matrix)");
+    OGB_CHECK(launch_elem_stiffness(md));
+    OGB_CHECK(launch_gather_matrix(md, m));
+    return OGB_OK;
+}
+
+int ogb_model_assemble_stiffness(ogb_model *md, ogb_mtrx *m)
+{
+    if (!md || !m) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    OGB_CHECK(assemble_stiffness_async(md, m));
+    return check_device_status(md->ctx, "element stiffness");
+}
+
+static int internal_forces_async(ogb_model *md, const double *u_dev, double *f_dev)
+{
+    if (!md->inc.p) {
+        OGB_CHECK(build_incidence(md->ctx, md->nnodes, md->nelem, md->nnpe, md->conn.p, md->inc_ptr, md->inc));
+    }
+    OGB_CHECK(launch_elem_internal_forces(md, u_dev));
+    OGB_CHECK(launch_gather_vector(md, f_dev));
+    return OGB_OK;
+}
+
+int ogb_model_internal_forces_dev(ogb_model *md, const double *u, double *f)
+{
+    if (!md || !u || !f) return fail(OGB_E_ARG, "null argument");
+    OGB_CHECK(internal_forces_async(md, u, f));
+    return OGB_OK;
+}
+
+int ogb_model_internal_forces(ogb_model *md, const double *u, double *f)
+{
+    if (!md || !u || !f) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    size_t n = (size_t)md->nnodes * md->ndofpn;
+    OGB_CHECK(md->v_unode.alloc(n));
+    OGB_CHECK(md->v_fnode.alloc(n));
+    cudaStream_t s = md->ctx->stream;
+    OGB_CUDA(cudaMemcpyAsync(md->v_unode.p, u, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    OGB_CHECK(internal_forces_async(md, md->v_unode.p, md->v_fnode.p));
+    OGB_CUDA(cudaMemcpyAsync(f, md->v_fnode.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    return check_device_status(md->ctx, "internal forces");
+}
+
+int ogb_model_gp_stress(ogb_model *md, double *stress, double *strain)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    size_t n = (size_t)md->nelem * md->ngp * md->nstress;
+    cudaStream_t s = md->ctx->stream;
+    if (stress) OGB_CUDA(cudaMemcpyAsync(stress, md->gp_stress.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (strain) OGB_CUDA(cudaMemcpyAsync(strain, md->gp_strain.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_model_commit_state(ogb_model *md)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (!md->nonlinear) return OGB_OK;
+    int64_t n = (int64_t)md->nelem * md->ngp;
+    k_commit_state<<<nb(n), NTHREADS, 0, md->ctx->stream>>>(n, md->emat.p, md->mats.p, md->ngp, md->state.p);
+    count_launch(md->ctx);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+int ogb_model_gp_state(ogb_model *md, double *state4)
+{
+    if (!md || !state4) return fail(OGB_E_ARG, "null argument");
+    int64_t n = (int64_t)md->nelem * md->ngp;
+    if (!md->nonlinear) {
+        memset(state4, 0, n * 4 * sizeof(double));
+        return OGB_OK;
+    }
+    DBuf<double> tmp;
+    OGB_CHECK(tmp.alloc(n * 4));
+    k_gp_state<<<nb(n), NTHREADS, 0, md->ctx->stream>>>(n, md->emat.p, md->mats.p, md->ngp, md->state.p, tmp.p);
+    count_launch(md->ctx);
+    OGB_CUDA(cudaMemcpyAsync(state4, tmp.p, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, md->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(md->ctx->stream));
+    return OGB_OK;
+}
+
+int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtol, int maxit,
+                          int precision, double *u_node, double *reac, ogb_solve_info *info)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    ogb_ctx *ctx = md->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = md->nnodes * md->ndofpn;
+    if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
+    OGB_CHECK(md->v_fnode.alloc(n));
+    OGB_CHECK(ensure_solver_vectors(m));
+    // K (K1 + K4)
+    OGB_CHECK(assemble_stiffness_async(md, m));
+    // prescribed displacement field and its internal forces (linearstatic.C:224-230)
+    k_u_from_bc<<<nb(n), NTHREADS, 0, s>>>(n, md->eq.p, bcval, u_node);
+    count_launch(ctx);
+    OGB_CHECK(internal_forces_async(md, u_node, md->v_fnode.p));
+    OGB_CUDA(cudaMemsetAsync(m->w_b.p, 0, m->npad * sizeof(double), s));
+    OGB_CUDA(cudaMemsetAsync(m->w_x.p, 0, m->npad * sizeof(double), s));
+    k_build_rhs<<<nb(n), NTHREADS, 0, s>>>(n, md->eq.p, load, md->v_fnode.p, m->w_b.p);
+    count_launch(ctx);
+    OGB_CHECK(check_device_status(ctx, "assembly"));
+    int r = solve_padded(m, rtol, maxit, precision, info);
+    k_scatter_solution<<<nb(n), NTHREADS, 0, s>>>(n, md->eq.p, m->w_x.p, u_node);
+    count_launch(ctx);
+    if (reac) {
+        OGB_CHECK(internal_forces_async(md, u_node, md->v_fnode.p));
+        k_reactions<<<nb(n), NTHREADS, 0, s>>>(n, md->eq.p, md->v_fnode.p, load, reac);
+        count_launch(ctx);
+    }
+    OGB_CUDA(cudaGetLastError());
+    return r;
+}
+
+int ogb_linear_static(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtol, int maxit,
+                      int precision, double *u_node, double *reac, ogb_solve_info *info)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    const size_t n = (size_t)md->nnodes * md->ndofpn;
+    cudaStream_t s = md->ctx->stream;
+    OGB_CHECK(md->v_bcval.alloc(n));
+    OGB_CHECK(md->v_load.alloc(n));
+    OGB_CHECK(md->v_unode.alloc(n));
+    OGB_CHECK(md->v_reac.alloc(n));
+    OGB_CUDA(cudaMemcpyAsync(md->v_bcval.p, bcval, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (load) OGB_CUDA(cudaMemcpyAsync(md->v_load.p, load, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int r = ogb_linear_static_dev(md, m, md->v_bcval.p, load ? md->v_load.p : nullptr, rtol, maxit, precision,
+                                  md->v_unode.p, reac ? md->v_reac.p : nullptr, info);
+    if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
+    OGB_CUDA(cudaMemcpyAsync(u_node, md->v_unode.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (reac) OGB_CUDA(cudaMemcpyAsync(reac, md->v_reac.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return r;
+}
+
+}  // extern "C"

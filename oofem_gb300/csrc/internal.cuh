@@ -1,0 +1,233 @@
+// Internal declarations shared by the CUDA translation units of liboofem_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/oofem_gb300.h"
+
+namespace ogb {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define OGB_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t _e = (call);                                    \
+        if (_e != cudaSuccess) return ::ogb::cuda_fail(_e, #call);  \
+    } while (0)
+
+#define OGB_CHECK(call)                       \
+    do {                                      \
+        int _r = (call);                      \
+        if (_r != OGB_OK) return _r;          \
+    } while (0)
+
+// Rows of every system are processed in chunks of CHUNK rows; systems are
+// padded to a multiple of CHUNK with identity rows so that every chunk belongs
+// to one system and block-level reductions stay deterministic.
+constexpr int CHUNK = 1024;
+constexpr int NTHREADS = 256;
+constexpr int NUM_SMS = 152;
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------- device buffers
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        if (count <= n && p) return OGB_OK;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return cuda_fail(e, "cudaMalloc"); }
+        n = count;
+        return OGB_OK;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+};
+
+// Pinned host staging buffer.
+template <class T>
+struct HBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        if (count <= n && p) return OGB_OK;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMallocHost((void **)&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return cuda_fail(e, "cudaMallocHost"); }
+        n = count;
+        return OGB_OK;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~HBuf() { release(); }
+    HBuf() = default;
+    HBuf(const HBuf &) = delete;
+    HBuf &operator=(const HBuf &) = delete;
+};
+
+// Device-side status word written by kernels instead of trapping.
+enum DevStatus : int {
+    DS_OK = 0,
+    DS_LIMIT = 1,      // a fixed per-row / per-node capacity was exceeded
+    DS_PATTERN = 2,    // an assembled location is missing from the pattern
+    DS_NEGVOL = 3,     // tetrahedron with detJ <= 0 (fei3dtetlin.C:146)
+};
+
+// Per-system PCG scalars (one record per right-hand side / instance).
+struct PcgScal {
+    double bnorm2;    // ||b||^2
+    double rho;       // r.z of the current iteration
+    double rho_old;
+    double pq;        // p.q
+    double rnorm2;    // ||r||^2
+    double alpha, beta;
+    int done;         // 1 converged, 2 breakdown, 3 zero diagonal
+    int iters;
+};
+
+}  // namespace ogb
+
+// ---------------------------------------------------------------- handles
+struct ogb_ctx {
+    int device = 0;
+    int refs = 0;          // live matrices/models created on this context
+    bool closing = false;  // ogb_ctx_destroy called while refs > 0
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    // kernel timing (SpMV launches), see ogb_ctx_profile_enable
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<cudaEvent_t> ev_pending;   // start/stop pairs
+    double prof_ms = 0.0, prof_bytes = 0.0, pending_bytes = 0.0;
+    int64_t prof_count = 0;
+    ogb::DBuf<int> status;           // device status word
+    ogb::HBuf<int> h_status;
+};
+
+struct ogb_mtrx {
+    ogb_ctx *ctx = nullptr;
+    int neq = 0;          // equations
+    int npad = 0;         // rows incl. identity padding (multiple of CHUNK)
+    int64_t nnz = 0;      // pattern entries of the neq real rows
+    int64_t version = 0;
+    bool has_structure = false;
+    ogb::DBuf<int64_t> rowptr;   // npad+1
+    ogb::DBuf<int> colind;       // nnz + (npad-neq)
+    ogb::DBuf<double> val;       // same length
+    ogb::DBuf<float> val32;      // FP32 copy for the mixed-precision solve
+    int64_t val32_version = -1;
+    ogb::DBuf<int64_t> diagpos;  // position of (r,r) per row (npad)
+    // drop-in staging (SparseMtrx::assemble from host element loops)
+    std::vector<int64_t> st_ptr;     // per staged matrix: offset into st_loc
+    std::vector<int> st_loc;
+    std::vector<int64_t> st_keoff;   // per staged matrix: offset into st_ke
+    std::vector<double> st_ke;
+    // solver workspace
+    ogb::DBuf<double> w_r, w_z, w_p, w_q, w_dinv, w_x, w_b, w_part, w_d;
+    ogb::DBuf<float> w_r32, w_z32, w_p32, w_q32, w_dinv32, w_x32;
+    ogb::DBuf<ogb::PcgScal> w_scal;
+    ogb::HBuf<ogb::PcgScal> h_scal;
+    ogb::DBuf<unsigned int> w_count;
+    int spmv_tpr = 8;    // threads per row of the CSR SpMV (autotuned)
+};
+
+struct ogb_model {
+    ogb_ctx *ctx = nullptr;
+    int etype = 0, nnodes = 0, nelem = 0, nnpe = 0, ndofpn = 0, ndim = 0, ngp = 0, nstress = 0;
+    int nmat = 0;
+    double thickness = 1.0;
+    int neq = 0, npeq = 0;
+    std::vector<int> h_eq;
+    ogb::DBuf<double> coords, mats, Dmat;
+    ogb::DBuf<int> conn, emat, eq;
+    // node -> (element << 3 | local node), sorted by element
+    ogb::DBuf<int64_t> inc_ptr;
+    ogb::DBuf<uint32_t> inc;
+    // node adjacency (node blocks) of the pattern
+    ogb::DBuf<int64_t> nb_ptr;
+    ogb::DBuf<int> nb_col, nb_coloff, blk_node;
+    int64_t nblocks = 0;
+    // contributions per node block: (element << 6 | a << 3 | b), sorted by element
+    ogb::DBuf<int64_t> cb_ptr;
+    ogb::DBuf<uint32_t> cb;
+    ogb::DBuf<int64_t> node_rowbase;   // CSR position of the first row of each node
+    ogb::DBuf<int> node_rowlen;
+    // element buffers
+    ogb::DBuf<double> ke;       // nelem x nnpe x nnpe x ndofpn x ndofpn
+    ogb::DBuf<double> fe;       // nelem x nnpe x ndofpn
+    ogb::DBuf<double> state;    // nelem x ngp x NSTATE
+    ogb::DBuf<double> gp_stress, gp_strain;
+    // linear-static work vectors
+    ogb::DBuf<double> v_unode, v_fnode, v_bcval, v_load, v_b, v_x, v_reac;
+    ogb_mtrx *bound = nullptr;
+    bool nonlinear = false;
+};
+
+namespace ogb {
+
+constexpr int NSTATE = 24;
+
+// --------------------------------------------------------------- launchers
+// scan.cu
+int exclusive_scan_i64(ogb_ctx *ctx, const int64_t *in, int64_t *out, int64_t n, int64_t *total_host);
+
+// pattern.cu
+int build_incidence(ogb_ctx *ctx, int nnodes, int nelem, int nnpe, const int *conn,
+                    DBuf<int64_t> &inc_ptr, DBuf<uint32_t> &inc);
+int build_model_pattern(ogb_model *md, ogb_mtrx *m);
+int build_loc_pattern(ogb_mtrx *m, int neq, int nelem, const int64_t *loc_ptr_h, const int *loc_h);
+int staged_assemble(ogb_mtrx *m);
+int pad_matrix_rows(ogb_mtrx *m);
+
+// element.cu
+int launch_elem_stiffness(ogb_model *md);
+int launch_elem_internal_forces(ogb_model *md, const double *u_node);
+int launch_isotropic_tables(ogb_model *md);
+
+// assembly.cu
+int launch_gather_matrix(ogb_model *md, ogb_mtrx *m);
+int launch_gather_vector(ogb_model *md, double *f_node);
+
+// solver.cu
+int spmv64(ogb_mtrx *m, const double *x, double *y);
+int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info);
+int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info);
+int extract_diag(ogb_mtrx *m);
+int pick_tpr(const ogb_mtrx *m);
+
+// helpers in capi.cu
+inline void count_launch(ogb_ctx *ctx, int n = 1) { ctx->launches += n; }
+int check_device_status(ogb_ctx *ctx, const char *where);
+void ctx_release(ogb_ctx *ctx);
+// profiling helpers (capi.cu)
+void prof_begin(ogb_ctx *ctx);
+void prof_end(ogb_ctx *ctx, double bytes);
+void prof_harvest(ogb_ctx *ctx);
+
+}  // namespace ogb

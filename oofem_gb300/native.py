@@ -1,0 +1,371 @@
+"""ctypes binding of liboofem_gb300.so (include/oofem_gb300.h) and a thin
+Python mirror of the reference interfaces it replaces:
+
+* :class:`GpuCsrMtrx`   -- ``SparseMtrx`` (src/core/sparsemtrx.h:62-303)
+* :class:`GpuPcgSolver` -- ``SparseLinearSystemNM`` / ``IMLSolver``
+  (src/core/sparselinsystemnm.h:58-96, src/core/iml/imlsolver.C:101-147)
+* :class:`GpuModel`     -- the element loops of ``EngngModel::assemble`` /
+  ``assembleVectorFromElements`` for LSpace / PlaneStress2d / LTRSpace
+
+There is no CPU fallback: loading raises if the CUDA library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboofem_gb300.so")
+
+OGB_OK = 0
+ERRORS = {-1: "OGB_E_ARG", -2: "OGB_E_CUDA", -3: "OGB_E_STATE", -4: "OGB_E_PATTERN",
+          -5: "OGB_E_NOTCONV", -6: "OGB_E_BREAKDOWN", -7: "OGB_E_ZERODIAG", -8: "OGB_E_MESH",
+          -9: "OGB_E_LIMIT"}
+PREC_FP64 = 0
+PREC_MIXED = 1
+# solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
+SOLVER_STATUS = (0, -5, -6, -7)
+
+# Every entry point of include/oofem_gb300.h: name -> (restype, argtypes)
+_vp = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_i64 = C.c_int64
+_pi64 = C.POINTER(C.c_int64)
+_pi = C.POINTER(C.c_int)
+_pd = C.POINTER(C.c_double)
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("achieved", C.c_double),
+                ("status", C.c_int)]
+
+
+SIGNATURES = {
+    "ogb_last_error": (C.c_char_p, []),
+    "ogb_version": (_i, []),
+    "ogb_ctx_create": (_i, [_i, C.POINTER(_vp)]),
+    "ogb_ctx_destroy": (_i, [_vp]),
+    "ogb_ctx_stream": (_vp, [_vp]),
+    "ogb_ctx_synchronize": (_i, [_vp]),
+    "ogb_ctx_kernel_launches": (_i64, [_vp]),
+    "ogb_ctx_profile_enable": (_i, [_vp, _i]),
+    "ogb_ctx_profile_read": (_i, [_vp, _pd, _pi64, _pd]),
+    "ogb_mtrx_create": (_i, [_vp, C.POINTER(_vp)]),
+    "ogb_mtrx_destroy": (_i, [_vp]),
+    "ogb_mtrx_build_structure": (_i, [_vp, _i, _i, _vp, _vp]),
+    "ogb_mtrx_neq": (_i, [_vp, _pi]),
+    "ogb_mtrx_nnz": (_i, [_vp, _pi64]),
+    "ogb_mtrx_pattern": (_i, [_vp, _vp, _vp]),
+    "ogb_mtrx_values": (_i, [_vp, _vp]),
+    "ogb_mtrx_zero": (_i, [_vp]),
+    "ogb_mtrx_assemble_begin": (_i, [_vp]),
+    "ogb_mtrx_assemble": (_i, [_vp, _i, _vp, _vp]),
+    "ogb_mtrx_assemble_end": (_i, [_vp]),
+    "ogb_mtrx_times": (_i, [_vp, _vp, _vp]),
+    "ogb_mtrx_times_dev": (_i, [_vp, _vp, _vp]),
+    "ogb_mtrx_at": (_i, [_vp, _i, _i, _pd]),
+    "ogb_mtrx_set_at": (_i, [_vp, _i, _i, _d]),
+    "ogb_mtrx_version": (_i, [_vp, _pi64]),
+    "ogb_pcg_solve": (_i, [_vp, _vp, _vp, _d, _i, _i, C.POINTER(SolveInfo)]),
+    "ogb_pcg_solve_dev": (_i, [_vp, _vp, _vp, _d, _i, _i, C.POINTER(SolveInfo)]),
+    "ogb_model_create": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _d, _vp, C.POINTER(_vp)]),
+    "ogb_model_destroy": (_i, [_vp]),
+    "ogb_model_neq": (_i, [_vp, _pi, _pi]),
+    "ogb_model_equations": (_i, [_vp, _vp]),
+    "ogb_model_build_matrix": (_i, [_vp, _vp]),
+    "ogb_model_assemble_stiffness": (_i, [_vp, _vp]),
+    "ogb_model_internal_forces": (_i, [_vp, _vp, _vp]),
+    "ogb_model_internal_forces_dev": (_i, [_vp, _vp, _vp]),
+    "ogb_model_gp_stress": (_i, [_vp, _vp, _vp]),
+    "ogb_model_commit_state": (_i, [_vp]),
+    "ogb_model_gp_state": (_i, [_vp, _vp]),
+    "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
+    "ogb_linear_static_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
+}
+
+_lib = None
+
+
+class OgbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load the CUDA library (fails loudly when it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is missing; run __graft_entry__.build() (no CPU fallback)")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(code: int):
+    if code != OGB_OK:
+        raise OgbError(code, load().ogb_last_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _dptr(t) -> C.c_void_p:
+    """Device pointer of a torch tensor."""
+    return C.c_void_p(t.data_ptr())
+
+
+class Context:
+    """Device + stream (ogb_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        _check(self.lib.ogb_ctx_create(device, C.byref(h)))
+        self.h = h
+
+    @property
+    def stream(self) -> int:
+        return self.lib.ogb_ctx_stream(self.h)
+
+    def synchronize(self):
+        _check(self.lib.ogb_ctx_synchronize(self.h))
+
+    def kernel_launches(self) -> int:
+        return self.lib.ogb_ctx_kernel_launches(self.h)
+
+    def profile(self, enable: bool):
+        _check(self.lib.ogb_ctx_profile_enable(self.h, int(enable)))
+
+    def profile_read(self):
+        ms, n, by = C.c_double(), C.c_int64(), C.c_double()
+        _check(self.lib.ogb_ctx_profile_read(self.h, C.byref(ms), C.byref(n), C.byref(by)))
+        return ms.value, n.value, by.value
+
+    def close(self):
+        if self.h:
+            self.lib.ogb_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuCsrMtrx:
+    """SparseMtrx on the GPU: full-pattern CSR (== CompCol colptr/rowind)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        _check(self.lib.ogb_mtrx_create(ctx.h, C.byref(h)))
+        self.h = h
+
+    # SparseMtrx::buildInternalStructure from element location arrays
+    def build_internal_structure(self, neq: int, locs) -> None:
+        if isinstance(locs, np.ndarray) and locs.ndim == 2:
+            loc = np.ascontiguousarray(locs, dtype=np.int32).ravel()
+            ptr = np.arange(locs.shape[0] + 1, dtype=np.int64) * locs.shape[1]
+            ne = locs.shape[0]
+        else:
+            arrs = [np.asarray(l, dtype=np.int32) for l in locs]
+            ptr = np.zeros(len(arrs) + 1, np.int64)
+            ptr[1:] = np.cumsum([a.size for a in arrs])
+            loc = np.concatenate(arrs) if arrs else np.zeros(0, np.int32)
+            ne = len(arrs)
+        _check(self.lib.ogb_mtrx_build_structure(self.h, neq, ne, _ptr(ptr), _ptr(loc)))
+
+    @property
+    def neq(self) -> int:
+        v = C.c_int()
+        _check(self.lib.ogb_mtrx_neq(self.h, C.byref(v)))
+        return v.value
+
+    @property
+    def nnz(self) -> int:
+        v = C.c_int64()
+        _check(self.lib.ogb_mtrx_nnz(self.h, C.byref(v)))
+        return v.value
+
+    def pattern(self):
+        n, nz = self.neq, self.nnz
+        rp = np.zeros(n + 1, np.int64)
+        ci = np.zeros(max(nz, 1), np.int32)
+        _check(self.lib.ogb_mtrx_pattern(self.h, _ptr(rp), _ptr(ci)))
+        return rp, ci[:nz]
+
+    def values(self) -> np.ndarray:
+        v = np.zeros(max(self.nnz, 1))
+        _check(self.lib.ogb_mtrx_values(self.h, _ptr(v)))
+        return v[:self.nnz]
+
+    def zero(self):
+        _check(self.lib.ogb_mtrx_zero(self.h))
+
+    def assemble_begin(self):
+        _check(self.lib.ogb_mtrx_assemble_begin(self.h))
+
+    def assemble(self, loc, mat: np.ndarray) -> int:
+        """SparseMtrx::assemble(loc, mat); mat is the element matrix (any
+        layout in numpy, passed column-major like FloatMatrix)."""
+        loc = np.ascontiguousarray(loc, dtype=np.int32)
+        km = np.asfortranarray(mat, dtype=np.float64)
+        _check(self.lib.ogb_mtrx_assemble(self.h, loc.size, _ptr(loc),
+                                          km.ctypes.data_as(C.c_void_p)))
+        return 1
+
+    def assemble_end(self):
+        _check(self.lib.ogb_mtrx_assemble_end(self.h))
+
+    def times(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.neq)
+        _check(self.lib.ogb_mtrx_times(self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def at(self, i: int, j: int) -> float:
+        v = C.c_double()
+        _check(self.lib.ogb_mtrx_at(self.h, i, j, C.byref(v)))
+        return v.value
+
+    def set_at(self, i: int, j: int, value: float):
+        _check(self.lib.ogb_mtrx_set_at(self.h, i, j, float(value)))
+
+    @property
+    def version(self) -> int:
+        v = C.c_int64()
+        _check(self.lib.ogb_mtrx_version(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            self.lib.ogb_mtrx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuPcgSolver:
+    """SparseLinearSystemNM::solve with IML CG + Jacobi semantics
+    (lstol / lsiter as in IMLSolver::initializeFrom, imlsolver.C:66-98)."""
+
+    def __init__(self, lstol: float = 1e-5, lsiter: int = 200, precision: int = PREC_FP64):
+        self.tol = lstol
+        self.maxit = lsiter
+        self.precision = precision
+        self.last = SolveInfo()
+
+    def solve(self, A: GpuCsrMtrx, b: np.ndarray, x: np.ndarray) -> int:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        info = SolveInfo()
+        code = A.lib.ogb_pcg_solve(A.h, _ptr(b), _ptr(x), self.tol, self.maxit, self.precision,
+                                   C.byref(info))
+        self.last = info
+        if code not in SOLVER_STATUS:
+            _check(code)
+        return code
+
+
+class GpuModel:
+    """Element backend for one mesh (one element type)."""
+
+    def __init__(self, ctx: Context, mesh):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.mesh = mesh
+        self._coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+        self._conn = np.ascontiguousarray(mesh.conn, dtype=np.int32)
+        self._emat = np.ascontiguousarray(mesh.elem_mat, dtype=np.int32)
+        self._mats = np.ascontiguousarray(mesh.material_table(), dtype=np.float64)
+        self._bcm = np.ascontiguousarray(mesh.bc_mask, dtype=np.uint8)
+        h = C.c_void_p()
+        _check(self.lib.ogb_model_create(ctx.h, mesh.elem_type, mesh.nnodes, _ptr(self._coords),
+                                         mesh.nelem, _ptr(self._conn), _ptr(self._emat),
+                                         self._mats.shape[0], _ptr(self._mats), float(mesh.thickness),
+                                         _ptr(self._bcm), C.byref(h)))
+        self.h = h
+
+    def neq(self):
+        a, b = C.c_int(), C.c_int()
+        _check(self.lib.ogb_model_neq(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def equations(self) -> np.ndarray:
+        eq = np.zeros((self.mesh.nnodes, self.mesh.ndofpn), np.int32)
+        _check(self.lib.ogb_model_equations(self.h, _ptr(eq)))
+        return eq
+
+    def build_matrix(self, A: GpuCsrMtrx):
+        _check(self.lib.ogb_model_build_matrix(self.h, A.h))
+
+    def assemble_stiffness(self, A: GpuCsrMtrx):
+        _check(self.lib.ogb_model_assemble_stiffness(self.h, A.h))
+
+    def internal_forces(self, u_node: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u_node, dtype=np.float64)
+        f = np.zeros_like(u)
+        _check(self.lib.ogb_model_internal_forces(self.h, _ptr(u), _ptr(f)))
+        return f
+
+    def gp_stress(self):
+        m = self.mesh
+        ngp = {1: 8, 2: 4, 3: 1}[m.elem_type]
+        ns = 3 if m.elem_type == 2 else 6
+        s = np.zeros((m.nelem, ngp, ns))
+        e = np.zeros_like(s)
+        _check(self.lib.ogb_model_gp_stress(self.h, _ptr(s), _ptr(e)))
+        return s, e
+
+    def gp_state(self):
+        m = self.mesh
+        ngp = {1: 8, 2: 4, 3: 1}[m.elem_type]
+        s = np.zeros((m.nelem, ngp, 4))
+        _check(self.lib.ogb_model_gp_state(self.h, _ptr(s)))
+        return s
+
+    def commit_state(self):
+        _check(self.lib.ogb_model_commit_state(self.h))
+
+    def linear_static(self, A: GpuCsrMtrx, bc_value=None, nodal_load=None, rtol=1e-12,
+                      maxit=100000, precision=PREC_FP64, want_reactions=True):
+        m = self.mesh
+        bcv = np.ascontiguousarray(m.bc_value if bc_value is None else bc_value, dtype=np.float64)
+        ld = np.ascontiguousarray(m.nodal_load if nodal_load is None else nodal_load, dtype=np.float64)
+        u = np.zeros_like(bcv)
+        reac = np.zeros_like(bcv) if want_reactions else None
+        info = SolveInfo()
+        code = self.lib.ogb_linear_static(self.h, A.h, _ptr(bcv), _ptr(ld), rtol, maxit, precision,
+                                          _ptr(u), _ptr(reac) if reac is not None else None,
+                                          C.byref(info))
+        if code not in SOLVER_STATUS:
+            _check(code)
+        return u, reac, info
+
+    def close(self):
+        if self.h:
+            self.lib.ogb_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

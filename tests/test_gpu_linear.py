@@ -1,0 +1,203 @@
+"""GPU parity of the linear path through the C ABI against the reference's own
+golden vectors (tests/golden) and the C oracle.
+
+Bars: CSR pattern and equation numbers bit-exact; assembled values within
+1e-12 relative; displacements / reactions / GP stresses within 1e-9 relative
+of the reference's direct solve when PCG runs to ||r||/||b|| <= 1e-14 (the
+solve tolerance bounds the displacement error, not the kernels); mixed
+precision + FP64 refinement to 1e-8 relative residual within 1e-6 of the
+reference displacements."""
+import numpy as np
+import pytest
+
+from conftest import LINEAR_CASES, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    s = np.abs(b).max()
+    return np.abs(a - b).max() / (s if s > 0 else 1.0)
+
+
+def mesh_from_golden(g):
+    from oofem_gb300 import meshgen as mg
+    mats = [mg.Material(int(r[0]), r[1], r[2], r[3], r[4], r[5], r[6]) for r in g["mats"]]
+    return mg.Mesh(int(g["etype"]), g["coords"], g["conn"].astype(np.int32), g["elem_mat"].astype(np.int32),
+                   mats, g["bc_mask"].astype(np.uint8), g["bc_value"], g["nodal_load"],
+                   thickness=float(g["thickness"]))
+
+
+@pytest.fixture(scope="module")
+def ctx(native_lib):
+    return native_lib.Context(0)
+
+
+@pytest.mark.parametrize("case", LINEAR_CASES)
+def test_model_path_matches_reference(case, ctx, native_lib):
+    g = load_golden(case)
+    mesh = mesh_from_golden(g)
+    model = native_lib.GpuModel(ctx, mesh)
+    eq = model.equations()
+    assert np.array_equal(np.where(eq > 0, eq, 0), g["s1_eq"])
+    A = native_lib.GpuCsrMtrx(ctx)
+    u, reac, info = model.linear_static(A, rtol=1e-14, maxit=100000)
+    assert info.status == 0
+    rp, ci = A.pattern()
+    assert np.array_equal(rp, g["K_colptr"]) and np.array_equal(ci, g["K_rowind"])
+    assert rel(A.values(), g["K_val"]) < 1e-12
+    assert rel(u, g["s1_u"]) < 1e-9
+    assert rel(reac, g["s1_reac"]) < 1e-9
+    # GP stresses of the final state: internal forces at u
+    model.internal_forces(u)
+    s, e = model.gp_stress()
+    assert rel(s, g["s1_stress"]) < 1e-9
+    assert rel(e, g["s1_strain"]) < 1e-9
+
+
+@pytest.mark.parametrize("case", LINEAR_CASES)
+def test_dropin_sparse_matrix_path(case, ctx, native_lib, oracle):
+    """SparseMtrx drop-in: buildInternalStructure from location arrays,
+    assemble(loc, Ke) per element from the host, assembleEnd, times, at, solve."""
+    g = load_golden(case)
+    et = int(g["etype"])
+    neq, _, eq = oracle.number_equations(g["bc_mask"])
+    loc = oracle.location_arrays(g["conn"], eq)
+    A = native_lib.GpuCsrMtrx(ctx)
+    A.build_internal_structure(neq, loc)
+    rp, ci = A.pattern()
+    assert np.array_equal(rp, g["K_colptr"]) and np.array_equal(ci, g["K_rowind"])
+    A.assemble_begin()
+    for e in range(g["conn"].shape[0]):
+        m = g["mats"][g["elem_mat"][e]]
+        ke = oracle.elem_stiffness(et, g["coords"][g["conn"][e]], oracle.isole_d(et, m[1], m[2]),
+                                   float(g["thickness"]))
+        A.assemble(loc[e], ke)
+    A.assemble_end()
+    val = A.values()
+    ref = oracle.assemble_tangent(g, loc, neq, rp, ci)
+    assert np.array_equal(val, ref), "staged assembly must add in the reference order"
+    assert rel(val, g["K_val"]) < 1e-13
+    x = np.random.default_rng(0).standard_normal(neq)
+    assert rel(A.times(x), oracle.spmv(rp, ci, ref, x)) < 1e-14
+    assert A.at(1, 1) == ref[rp[0] + np.searchsorted(ci[rp[0]:rp[1]], 0)]
+    solver = native_lib.GpuPcgSolver(lstol=1e-12, lsiter=100000)
+    b = np.random.default_rng(1).standard_normal(neq)
+    xg = np.zeros(neq)
+    assert solver.solve(A, b, xg) == 0
+    xo, st, it, ach = oracle.pcg(rp, ci, ref, b, rtol=1e-12)
+    assert abs(solver.last.iterations - it) <= 2
+    assert rel(xg, xo) < 1e-9
+
+
+def test_version_bumps_and_set_at(ctx, native_lib, oracle):
+    g = load_golden("hex_cantilever_6x3x3_jit")
+    neq, _, eq = oracle.number_equations(g["bc_mask"])
+    loc = oracle.location_arrays(g["conn"], eq)
+    A = native_lib.GpuCsrMtrx(ctx)
+    A.build_internal_structure(neq, loc)
+    v0 = A.version
+    A.set_at(3, 3, 2.5)
+    assert A.at(3, 3) == 2.5 and A.version > v0
+    A.zero()
+    assert A.at(3, 3) == 0.0
+    assert A.at(1, neq) == 0.0   # structural zero reads 0
+
+
+def test_assembly_is_deterministic(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(12, 5, 5, jitter=0.2, seed=5)
+    vals = []
+    for _ in range(2):
+        model = native_lib.GpuModel(ctx, mesh)
+        A = native_lib.GpuCsrMtrx(ctx)
+        model.build_matrix(A)
+        model.assemble_stiffness(A)
+        vals.append(A.values())
+    assert np.array_equal(vals[0], vals[1])
+
+
+@pytest.mark.parametrize("case", ["hex_cantilever_20x4x4", "tet_cube_3_jit", "quad_rve_8_s3_lc2"])
+def test_mixed_precision_refinement(case, ctx, native_lib):
+    g = load_golden(case)
+    mesh = mesh_from_golden(g)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    u, reac, info = model.linear_static(A, rtol=1e-8, maxit=100000, precision=native_lib.PREC_MIXED)
+    assert info.status == 0 and info.achieved <= 1e-8
+    assert rel(u, g["s1_u"]) < 1e-5
+
+
+def test_larger_mesh_pattern_and_residual(ctx, native_lib, oracle):
+    """40x8x8 jittered cantilever: pattern bit-exact vs the oracle, values, and
+    the FP64 solution's true residual."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(40, 8, 8, jitter=0.2, seed=9)
+    md = oracle.mesh_dict(mesh)
+    neq, _, eq = oracle.number_equations(mesh.bc_mask)
+    loc = oracle.location_arrays(mesh.conn, eq)
+    rp, ci = oracle.build_pattern(neq, loc)
+    val = oracle.assemble_tangent(md, loc, neq, rp, ci)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    u, reac, info = model.linear_static(A, rtol=1e-10, maxit=100000)
+    grp, gci = A.pattern()
+    assert np.array_equal(grp, rp) and np.array_equal(gci, ci)
+    assert rel(A.values(), val) < 1e-12
+    x = u[eq > 0]
+    order = np.argsort(eq[eq > 0])
+    x = x[order]
+    b = mesh.nodal_load[eq > 0][order]
+    r = b - oracle.spmv(rp, ci, val, x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-9
+
+
+def test_failure_status_not_converged(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(10, 3, 3)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    u, reac, info = model.linear_static(A, rtol=1e-14, maxit=3)
+    assert info.status == -5 and info.iterations <= 3 + 16
+
+
+def test_failure_nan_rhs_is_breakdown(ctx, native_lib, oracle):
+    g = load_golden("quad_rve_8_s3_lc0")
+    neq, _, eq = oracle.number_equations(g["bc_mask"])
+    loc = oracle.location_arrays(g["conn"], eq)
+    A = native_lib.GpuCsrMtrx(ctx)
+    A.build_internal_structure(neq, loc)
+    A.assemble_begin()
+    for e in range(g["conn"].shape[0]):
+        m = g["mats"][g["elem_mat"][e]]
+        A.assemble(loc[e], oracle.elem_stiffness(2, g["coords"][g["conn"][e]], oracle.isole_d(2, m[1], m[2])))
+    A.assemble_end()
+    b = np.ones(neq)
+    b[3] = np.nan
+    x = np.zeros(neq)
+    code = A.lib.ogb_pcg_solve(A.h, b.ctypes.data_as(__import__("ctypes").c_void_p),
+                               x.ctypes.data_as(__import__("ctypes").c_void_p), 1e-10, 1000, 0, None)
+    assert code == -6
+
+
+def test_zero_diagonal_detected(ctx, native_lib):
+    A = native_lib.GpuCsrMtrx(ctx)
+    A.build_internal_structure(4, np.array([[1, 2], [3, 4]], np.int32))
+    A.assemble_begin()
+    A.assemble([1, 2], np.array([[2.0, -1.0], [-1.0, 2.0]]))
+    A.assemble_end()
+    solver = native_lib.GpuPcgSolver(lstol=1e-10, lsiter=100)
+    x = np.zeros(4)
+    assert solver.solve(A, np.ones(4), x) == -7
+
+
+def test_negative_tet_volume_rejected(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.tet_cube_linear(2)
+    mesh.conn[0] = mesh.conn[0][[0, 2, 1, 3]]
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    with pytest.raises(native_lib.OgbError) as ei:
+        model.assemble_stiffness(A)
+    assert ei.value.code == -8

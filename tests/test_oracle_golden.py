@@ -1,0 +1,87 @@
+"""The C oracle against golden vectors written by the reference executable
+(tests/golden/*.npz via oracle/ref_harness.C) and against the golden values
+embedded in the reference's own LTRSpace patch deck (tests/sm/patch300.in)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, LINEAR_CASES, load_golden
+
+
+def rel(a, b):
+    s = np.abs(b).max()
+    return np.abs(a - b).max() / (s if s > 0 else 1.0)
+
+
+@pytest.mark.parametrize("case", LINEAR_CASES)
+def test_numbering_pattern_values(case, oracle):
+    g = load_golden(case)
+    neq, npeq, eq = oracle.number_equations(g["bc_mask"])
+    assert np.array_equal(np.where(eq > 0, eq, 0), g["s1_eq"])
+    assert neq == int(g["neq"])
+    loc = oracle.location_arrays(g["conn"], eq)
+    rp, ci = oracle.build_pattern(neq, loc)
+    # CompCol colptr/rowind of the full symmetric pattern == CSR rowptr/colind
+    assert np.array_equal(rp, g["K_colptr"])
+    assert np.array_equal(ci, g["K_rowind"])
+    val = oracle.assemble_tangent(g, loc, neq, rp, ci)
+    assert rel(val, g["K_val"]) < 1e-13
+
+
+@pytest.mark.parametrize("case", LINEAR_CASES)
+def test_element_stiffness(case, oracle):
+    g = load_golden(case)
+    et = int(g["etype"])
+    for e in range(1, 5):
+        key = f"ke{e}"
+        if key not in g:
+            continue
+        xe = g["coords"][g["conn"][e - 1]]
+        m = g["mats"][g["elem_mat"][e - 1]]
+        ke = oracle.elem_stiffness(et, xe, oracle.isole_d(et, m[1], m[2]), float(g["thickness"]))
+        assert rel(ke, g[key]) < 1e-14
+
+
+@pytest.mark.parametrize("case", LINEAR_CASES)
+def test_linear_static(case, oracle):
+    g = load_golden(case)
+    r = oracle.linear_static(g, rtol=1e-15, maxit=100000)
+    assert r["status"] == 0
+    assert rel(r["u"], g["s1_u"]) < 1e-10
+    assert rel(r["reac"], g["s1_reac"]) < 1e-10
+    assert rel(r["stress"], g["s1_stress"]) < 1e-10
+    assert rel(r["strain"], g["s1_strain"]) < 1e-10
+
+
+def test_patch300_reference_deck(oracle):
+    """LTRSpace compression patch test, exact solution from tests/sm/patch300.in."""
+    rules = json.load(open(os.path.join(GOLDEN, "patch300.json")))
+    coords = np.array([[0, 0, 0], [3, 0, 0], [0, 3, 0], [0, 0, 6], [3, 0, 6], [0, 3, 6]], float)
+    conn = np.array([[1, 2, 3, 4], [4, 5, 2, 3], [4, 6, 5, 3]], np.int32) - 1
+    bc = np.zeros((6, 3), np.uint8)
+    bc[0:3, :] = 1
+    bc[3:6, 0:2] = 1
+    load = np.zeros((6, 3))
+    load[3:6, 2] = -1.5
+    m = dict(etype=3, coords=coords, conn=conn, elem_mat=np.zeros(3, np.int32),
+             mats=np.array([[1, 15.0, 0.25, 0, 0, 0, 0, 0]]), bc_mask=bc, bc_value=np.zeros((6, 3)),
+             nodal_load=load, thickness=1.0)
+    r = oracle.linear_static(m, rtol=1e-14)
+    tol = rules["tolerance"]
+    for node, dof, v in rules["nodes"]:
+        assert abs(r["u"][node - 1, dof - 1] - v) <= tol
+    for node, dof, v in rules["reactions"]:
+        assert abs(r["reac"][node - 1, dof - 1] - v) <= tol
+
+
+def test_pcg_matches_reference_iteration_count(oracle):
+    """cfg1 with IML Jacobi-CG at lstol 1e-12: the survey's reference run logged
+    'nite 111, achieved tol 9.19e-13' (imlsolver.C:131)."""
+    g = load_golden("hex_cantilever_20x4x4")
+    r = oracle.linear_static(g, rtol=1e-12)
+    assert abs(r["iters"] - 111) <= 1
+    assert r["achieved"] <= 1e-12
+    tip = r["u"][20, 2]
+    assert abs(tip - (-1.16468948e-03)) < 5e-11
