@@ -79,6 +79,18 @@ OGB_API void *ogb_ctx_stream(ogb_ctx *ctx);                 /* cudaStream_t */
 OGB_API int ogb_ctx_synchronize(ogb_ctx *ctx);
 /* Number of kernels this library launched on the context since creation. */
 OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
+/* Tuning options of a context (no reference counterpart):
+ *   OGB_OPT_MIXED_VEC32 (0/1): mixed solves keep the CG vectors in FP32 instead
+ *   of FP64 (default 0). */
+#define OGB_OPT_MIXED_VEC32 1
+/*   OGB_OPT_MIXED_DIFF (0/1): FP32 operator stored in difference form (default 1).
+ *   OGB_OPT_MIXED_ORTH (0/1): restore r.p = 0 after an FP64 residual replacement.
+ *   OGB_OPT_MIXED_DROP_PPM: residual drop factor between replacements, in 1e-6
+ *   units (default 100000 = 0.1). */
+#define OGB_OPT_MIXED_DIFF 2
+#define OGB_OPT_MIXED_ORTH 3
+#define OGB_OPT_MIXED_DROP_PPM 4
+OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, every SpMV launch (the dominant kernel of the
  * solve) is bracketed by CUDA events on the context stream; ogb_ctx_profile_read
  * returns the summed device time (ms), the launch count and the algorithmic

@@ -326,6 +326,21 @@ int ogb_ctx_synchronize(ogb_ctx *ctx)
 
 int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
+{
+    if (!ctx) return fail(OGB_E_ARG, "null context");
+    switch (option) {
+    case OGB_OPT_MIXED_VEC32: ctx->mixed_vec32 = value != 0; return OGB_OK;
+    case OGB_OPT_MIXED_DIFF: ctx->mixed_diff = value != 0; return OGB_OK;
+    case OGB_OPT_MIXED_ORTH: ctx->mixed_orth = value != 0; return OGB_OK;
+    case OGB_OPT_MIXED_DROP_PPM:
+        if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
+        ctx->mixed_drop = value * 1e-6;
+        return OGB_OK;
+    }
+    return fail(OGB_E_ARG, "unknown option");
+}
+
 int ogb_ctx_profile_enable(ogb_ctx *ctx, int enable)
 {
     if (!ctx) return fail(OGB_E_ARG, "null context");
@@ -688,6 +703,7 @@ int ogb_model_build_matrix(ogb_model *md, ogb_mtrx *m)
     if (md->ctx != m->ctx) return fail(OGB_E_ARG, "model and matrix on different contexts");
     OGB_CUDA(cudaSetDevice(md->ctx->device));
     OGB_CHECK(build_model_pattern(md, m));
+    OGB_CHECK(build_sell(md, m));
     m->spmv_tpr = pick_tpr(m);
     md->bound = m;
     return OGB_OK;

@@ -107,8 +107,35 @@ struct PcgScal {
     double pq;        // p.q
     double rnorm2;    // ||r||^2
     double alpha, beta;
-    int done;         // 1 converged, 2 breakdown, 3 zero diagonal
+    double rmax2;     // ||r||^2 at the last FP64 residual replacement (mixed)
+    double tol2;      // (rtol ||b||)^2 (mixed)
+    double drop2;     // replacement threshold: ||r||^2 <= drop2 * rmax2 (mixed)
+    double zcoef;     // p = zcoef z + beta p (1 except right after a replacement)
+    int done;         // 1 converged, 2 breakdown, 3 zero diagonal, 4 max iterations
     int iters;
+    int reliable;     // mixed: an FP64 residual replacement is due
+    int pad_;
+};
+
+// Node-block SELL-32 storage: rows = active nodes (>= 1 free DOF) in node
+// order, ND x ND blocks, 32 rows per slice, blocks of a slice stored k-major so
+// that lane r of a warp reads row r's k-th block with coalesced loads.
+//   slot(s, k, r)   = sl_ptr[s] + 32 k + r                (column index array)
+//   value(slot, e)  = (slot - r) * ND*ND + 32 e + r        (e = i*ND + j)
+struct SellMat {
+    int nd = 0;
+    int nact = 0;           // active node rows
+    int nslices = 0;        // padded to a multiple of 32 slices
+    int64_t nslots = 0;
+    DBuf<int64_t> sl_ptr;   // nslices+1
+    DBuf<int> sl_width;     // blocks per row of each slice
+    DBuf<int> col;          // nslots
+    DBuf<int64_t> diag;     // slot of the diagonal block of each row (nslices*32)
+    DBuf<double> v64;       // nslots * ND*ND
+    DBuf<float> v32;
+    int64_t v32_version = -1;
+    DBuf<int> ns_of_eq;     // node-space index of equation e (0-based)
+    int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
 
 }  // namespace ogb
@@ -126,6 +153,10 @@ struct ogb_ctx {
     std::vector<cudaEvent_t> ev_pending;   // start/stop pairs
     double prof_ms = 0.0, prof_bytes = 0.0, pending_bytes = 0.0;
     int64_t prof_count = 0;
+    bool mixed_vec32 = false;   // mixed solve with FP32 Krylov vectors (see solver.cu)
+    bool mixed_diff = true;     // FP32 operator in difference form (see solver.cu)
+    bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
+    double mixed_drop = 0.1;    // residual drop between FP64 replacements
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;
 };
@@ -155,6 +186,11 @@ struct ogb_mtrx {
     ogb::HBuf<ogb::PcgScal> h_scal;
     ogb::DBuf<unsigned int> w_count;
     int spmv_tpr = 8;    // threads per row of the CSR SpMV (autotuned)
+    // node-block copy used by the solver when the matrix was built from a model
+    bool has_sell = false;
+    ogb::SellMat sell;
+    ogb::DBuf<double> n_b, n_x, n_r64, n_q64;   // node-space FP64 vectors
+    ogb::DBuf<float> n_d32;                      // mixed: solution increment since the last replacement
 };
 
 struct ogb_model {
@@ -178,6 +214,8 @@ struct ogb_model {
     ogb::DBuf<uint32_t> cb;
     ogb::DBuf<int64_t> node_rowbase;   // CSR position of the first row of each node
     ogb::DBuf<int> node_rowlen;
+    ogb::DBuf<int> act;                // active-node index per node (-1: all DOFs prescribed)
+    ogb::DBuf<int64_t> blk_slot;       // SELL slot per node block (-1: none)
     // element buffers
     ogb::DBuf<double> ke;       // nelem x nnpe x nnpe x ndofpn x ndofpn
     ogb::DBuf<double> fe;       // nelem x nnpe x ndofpn
@@ -204,6 +242,7 @@ int build_model_pattern(ogb_model *md, ogb_mtrx *m);
 int build_loc_pattern(ogb_mtrx *m, int neq, int nelem, const int64_t *loc_ptr_h, const int *loc_h);
 int staged_assemble(ogb_mtrx *m);
 int pad_matrix_rows(ogb_mtrx *m);
+int build_sell(ogb_model *md, ogb_mtrx *m);
 
 // element.cu
 int launch_elem_stiffness(ogb_model *md);

@@ -549,3 +549,168 @@ int staged_assemble(ogb_mtrx *m)
 }
 
 }  // namespace ogb
+
+// ---------------------------------------------------------------------------
+// Node-block SELL-32 copy of a model-built matrix (solver storage).
+namespace ogb {
+namespace {
+
+__global__ void k_act_flags(int nnodes, int ndofpn, const int *eq, int64_t *flag)
+{
+    int A = blockIdx.x * blockDim.x + threadIdx.x;
+    if (A > nnodes) return;
+    flag[A] = A < nnodes ? (nfree_of(eq, ndofpn, A) > 0) : 0;
+}
+
+__global__ void k_act_index(int nnodes, int ndofpn, const int *eq, const int64_t *scan, int *act, int *rownode)
+{
+    int A = blockIdx.x * blockDim.x + threadIdx.x;
+    if (A >= nnodes) return;
+    if (nfree_of(eq, ndofpn, A) > 0) {
+        int a = (int)scan[A];
+        act[A] = a;
+        rownode[a] = A;
+    } else {
+        act[A] = -1;
+    }
+}
+
+// Width (active neighbours) of every row; padding rows get one (identity) block.
+__global__ void k_row_width(int nrows_pad, int nact, const int *rownode, const int64_t *nb_ptr, const int *nb_col,
+                            const int *act, int *width)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nrows_pad) return;
+    if (a >= nact) {
+        width[a] = 1;
+        return;
+    }
+    int A = rownode[a], w = 0;
+    for (int64_t k = nb_ptr[A]; k < nb_ptr[A + 1]; ++k) w += act[nb_col[k]] >= 0;
+    width[a] = w;
+}
+
+__global__ void k_slice_width(int nslices, const int *width, int *sl_width, int64_t *slots)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > nslices) return;
+    if (s == nslices) {
+        slots[s] = 0;
+        return;
+    }
+    int w = 0;
+    for (int r = 0; r < 32; ++r) w = max(w, width[s * 32 + r]);
+    sl_width[s] = w;
+    slots[s] = (int64_t)w * 32;
+}
+
+template <int ND>
+__global__ void k_fill_sell(int nrows_pad, int nact, const int *rownode, const int64_t *nb_ptr, const int *nb_col,
+                            const int *act, const int64_t *sl_ptr, const int *sl_width, int *col, int64_t *diag,
+                            int64_t *blk_slot, double *v64, float *v32)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nrows_pad) return;
+    int s = a >> 5, r = a & 31;
+    int64_t base = sl_ptr[s];
+    int w = sl_width[s];
+    int kk = 0;
+    if (a < nact) {
+        int A = rownode[a];
+        for (int64_t k = nb_ptr[A]; k < nb_ptr[A + 1]; ++k) {
+            int B = nb_col[k];
+            int b = act[B];
+            if (b < 0) {
+                blk_slot[k] = -1;
+                continue;
+            }
+            int64_t slot = base + (int64_t)kk * 32 + r;
+            col[slot] = b;
+            blk_slot[k] = slot;
+            if (B == A) diag[a] = slot;
+            ++kk;
+        }
+    } else {
+        int64_t slot = base + r;   // identity block
+        col[slot] = a;
+        diag[a] = slot;
+        for (int e = 0; e < ND * ND; ++e) {
+            double v = (e % (ND + 1) == 0) ? 1.0 : 0.0;
+            v64[(slot - r) * ND * ND + 32 * e + r] = v;
+            v32[(slot - r) * ND * ND + 32 * e + r] = (float)v;
+        }
+        kk = 1;
+    }
+    for (; kk < w; ++kk) col[base + (int64_t)kk * 32 + r] = a < nact ? a : a;   // zero-valued padding slots
+}
+
+__global__ void k_ns_of_eq(int nnodes, int ndofpn, const int *eq, const int *act, int *ns_of_eq)
+{
+    int A = blockIdx.x * blockDim.x + threadIdx.x;
+    if (A >= nnodes || act[A] < 0) return;
+    for (int d = 0; d < ndofpn; ++d) {
+        int q = eq[(size_t)A * ndofpn + d];
+        if (q > 0) ns_of_eq[q - 1] = act[A] * ndofpn + d;
+    }
+}
+
+}  // namespace
+
+int build_sell(ogb_model *md, ogb_mtrx *m)
+{
+    ogb_ctx *ctx = md->ctx;
+    cudaStream_t st = ctx->stream;
+    const int nn = md->nnodes, nd = md->ndofpn;
+    SellMat &S = m->sell;
+    S.nd = nd;
+    DBuf<int64_t> flag;
+    OGB_CHECK(flag.alloc(nn + 1));
+    k_act_flags<<<nblk(nn + 1), NTHREADS, 0, st>>>(nn, nd, md->eq.p, flag.p);
+    count_launch(ctx);
+    int64_t nact = 0;
+    OGB_CHECK(exclusive_scan_i64(ctx, flag.p, flag.p, nn + 1, &nact));
+    S.nact = (int)nact;
+    int nslices = (int)ceil_div(nact > 0 ? nact : 1, 32);
+    nslices = (int)(ceil_div(nslices, 32) * 32);   // node-space length a multiple of CHUNK
+    S.nslices = nslices;
+    const int nrows_pad = nslices * 32;
+    DBuf<int> rownode, width;
+    OGB_CHECK(md->act.alloc(nn));
+    OGB_CHECK(rownode.alloc(nrows_pad));
+    OGB_CHECK(width.alloc(nrows_pad));
+    k_act_index<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, flag.p, md->act.p, rownode.p);
+    k_row_width<<<nblk(nrows_pad), NTHREADS, 0, st>>>(nrows_pad, S.nact, rownode.p, md->nb_ptr.p, md->nb_col.p,
+                                                      md->act.p, width.p);
+    OGB_CHECK(S.sl_ptr.alloc(nslices + 1));
+    OGB_CHECK(S.sl_width.alloc(nslices));
+    k_slice_width<<<nblk(nslices + 1), NTHREADS, 0, st>>>(nslices, width.p, S.sl_width.p, S.sl_ptr.p);
+    count_launch(ctx, 3);
+    int64_t nslots = 0;
+    OGB_CHECK(exclusive_scan_i64(ctx, S.sl_ptr.p, S.sl_ptr.p, nslices + 1, &nslots));
+    S.nslots = nslots;
+    OGB_CHECK(S.col.alloc(nslots));
+    OGB_CHECK(S.diag.alloc(nrows_pad));
+    OGB_CHECK(S.v64.alloc((size_t)nslots * nd * nd));
+    OGB_CHECK(S.v32.alloc((size_t)nslots * nd * nd));
+    OGB_CHECK(md->blk_slot.alloc(md->nblocks > 0 ? md->nblocks : 1));
+    OGB_CUDA(cudaMemsetAsync(S.v64.p, 0, (size_t)nslots * nd * nd * sizeof(double), st));
+    OGB_CUDA(cudaMemsetAsync(S.v32.p, 0, (size_t)nslots * nd * nd * sizeof(float), st));
+    if (nd == 3)
+        k_fill_sell<3><<<nblk(nrows_pad), NTHREADS, 0, st>>>(nrows_pad, S.nact, rownode.p, md->nb_ptr.p, md->nb_col.p,
+                                                             md->act.p, S.sl_ptr.p, S.sl_width.p, S.col.p, S.diag.p,
+                                                             md->blk_slot.p, S.v64.p, S.v32.p);
+    else
+        k_fill_sell<2><<<nblk(nrows_pad), NTHREADS, 0, st>>>(nrows_pad, S.nact, rownode.p, md->nb_ptr.p, md->nb_col.p,
+                                                             md->act.p, S.sl_ptr.p, S.sl_width.p, S.col.p, S.diag.p,
+                                                             md->blk_slot.p, S.v64.p, S.v32.p);
+    OGB_CHECK(S.ns_of_eq.alloc(md->neq > 0 ? md->neq : 1));
+    k_ns_of_eq<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, md->act.p, S.ns_of_eq.p);
+    count_launch(ctx, 2);
+    OGB_CUDA(cudaGetLastError());
+    OGB_CUDA(cudaStreamSynchronize(st));
+    S.v32_version = -1;
+    m->has_sell = true;
+    return OGB_OK;
+}
+
+}  // namespace ogb

@@ -1,5 +1,5 @@
 // Sparse matrix-vector product (K6), Jacobi-preconditioned CG (K7) and the
-// mixed-precision iterative-refinement loop (K8).
+// mixed-precision loop with FP64 residual replacement (K8).
 //
 // PCG restates IML++ CG (iml/cg.h:22-71) with DiagPreconditioner
 // (src/core/iml/diagpre.C:40-67): x0 = incoming x, r = b - A x, stop when
@@ -9,10 +9,25 @@
 //   update   : x += alpha p, r -= alpha q, z = D^-1 r, r.r, r.z -> convergence, beta
 //   p_update : p = z + beta p
 // Reductions: each block reduces its rows in a fixed order, the last block to
-// finish sums the per-block partials in index order, so every scalar is
-// bitwise reproducible. The scalars live on the device; kernels return at
-// once when the system is marked done, so the host checks convergence only
-// every few iterations and launches are never waited on per iteration.
+// finish sums the per-block partials in a fixed order, so every scalar is
+// bitwise reproducible. The scalars live on the device; kernels return at once
+// when the system is marked done, so the host looks at them only every few
+// iterations and never waits on a single launch.
+//
+// The operator is either the CSR matrix (drop-in SparseMtrx storage, any
+// pattern) or, for matrices assembled from a mesh, the node-block SELL-32 copy
+// (one column index per ND x ND block, coalesced k-major block loads), on
+// node-space vectors (ND slots per active node, prescribed slots are identity
+// rows with zero right-hand side).
+//
+// Mixed precision (OGB_PREC_MIXED): CG applies the FP32 matrix with FP32
+// multiply-adds; whenever the recursive residual has dropped by a factor 10
+// (or reached the tolerance) it is replaced by the true FP64 residual
+// r = b - A64 x64, keeping the search direction (reliable updates), so the
+// FP64 solution converges to the FP64 system. Convergence is decided on that
+// FP64 residual. The Krylov vectors are FP64 by default (FP32 vectors lose
+// orthogonality on these ill-conditioned systems and need several times more
+// iterations); an all-FP32 vector variant is selectable per context.
 #include <math.h>
 
 #include "internal.cuh"
@@ -22,6 +37,7 @@ namespace ogb {
 namespace {
 
 constexpr int GRID_MULT = 8;   // blocks per SM for the vector kernels
+constexpr double RELIABLE_DROP = 0.1;
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T v)
@@ -55,45 +71,63 @@ __device__ __forceinline__ void block_sum(double (&v)[NV])
     __syncthreads();
 }
 
-// Publish this block's partials; returns true only in thread 0 of the last
-// block, which alone runs the epilogue (reads and writes of the scalars).
+// Publish this block's partials and report (to every thread of the block)
+// whether it was the last block of the grid to do so.
 template <int NV>
 __device__ __forceinline__ bool publish_partials(const double (&v)[NV], double *part, unsigned int *count)
 {
-    if (threadIdx.x != 0) return false;
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) part[(size_t)k * gridDim.x + blockIdx.x] = v[k];
-    __threadfence();
-    unsigned int t = atomicAdd(count, 1u);
-    return t == gridDim.x - 1;
+        for (int k = 0; k < NV; ++k) part[(size_t)k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned int t = atomicAdd(count, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
 }
 
+// Run by every thread of the last block: thread t sums partials t, t+256, ...,
+// then the fixed-order block reduction; the result does not depend on which
+// block finished last. Valid in thread 0; only thread 0 writes the scalars.
 template <int NV>
 __device__ __forceinline__ void final_sums(const double *part, double (&out)[NV])
 {
-    // executed by thread 0 of the last block: fixed index order
     __threadfence();
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         double s = 0;
         const volatile double *pp = part + (size_t)k * gridDim.x;
-        for (unsigned b = 0; b < gridDim.x; ++b) s += pp[b];
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += NTHREADS) s += pp[b];
         out[k] = s;
     }
+    block_sum<NV>(out);
 }
 
-// ---------------------------------------------------------------- SpMV
+__device__ __forceinline__ bool halted(const PcgScal *sc) { return sc->done || sc->reliable; }
+
+// Epilogue of the p.q reduction: alpha = rho / p.q (thread 0 of the last block).
+__device__ __forceinline__ void finish_pq(double pq, unsigned int *count, PcgScal *sc)
+{
+    *count = 0;
+    sc->pq = pq;
+    if (!(pq > 0.0) || !isfinite(pq)) sc->done = 2;
+    else sc->alpha = sc->rho / pq;
+}
+
+// ---------------------------------------------------------------- CSR SpMV
 // TPR threads per row; a block walks CHUNK rows of a chunk in passes of
-// NTHREADS/TPR rows. Row r's entries are read by its TPR lanes in consecutive
-// order (coalesced), the partial sums are combined by shuffles.
-template <int TPR, class V, class X, bool DOT>
+// NTHREADS/TPR rows; the lanes of a row read its entries in order (coalesced)
+// and combine partial sums with shuffles.
+template <int TPR, class V, class X, class ACC, bool DOT>
 __global__ void __launch_bounds__(NTHREADS) k_spmv(int nchunks, const int64_t *__restrict__ rowptr,
                                                    const int *__restrict__ colind, const V *__restrict__ val,
                                                    const X *__restrict__ x, X *__restrict__ y, double *part,
                                                    unsigned int *count, PcgScal *sc)
 {
-    if (DOT && sc->done) return;
-    constexpr int RPP = NTHREADS / TPR;   // rows per pass
+    if (DOT && halted(sc)) return;
+    constexpr int RPP = NTHREADS / TPR;
     const int sub = threadIdx.x / TPR, lane = threadIdx.x % TPR;
     double acc[1] = {0.0};
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -102,12 +136,12 @@ __global__ void __launch_bounds__(NTHREADS) k_spmv(int nchunks, const int64_t *_
         for (int rb = 0; rb < CHUNK; rb += RPP) {
             const int row = r0 + rb + sub;
             const int64_t kb = rowptr[row], ke = rowptr[row + 1];
-            X s = 0;
-            for (int64_t k = kb + lane; k < ke; k += TPR) s += (X)val[k] * __ldg(x + colind[k]);
+            ACC s = 0;
+            for (int64_t k = kb + lane; k < ke; k += TPR) s += (ACC)val[k] * (ACC)__ldg(x + colind[k]);
 #pragma unroll
             for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
             if (lane == 0) {
-                y[row] = s;
+                y[row] = (X)s;
                 if (DOT) acc[0] += (double)x[row] * (double)s;
             }
         }
@@ -115,33 +149,90 @@ __global__ void __launch_bounds__(NTHREADS) k_spmv(int nchunks, const int64_t *_
     if (!DOT) return;
     block_sum<1>(acc);
     if (publish_partials<1>(acc, part, count)) {
-        double tot[1];
-        final_sums<1>(part, tot);
-        *count = 0;
-        double pq = tot[0];
-        sc->pq = pq;
-        if (!(pq > 0.0) || !isfinite(pq)) {
-            sc->done = 2;   // breakdown
-        } else {
-            sc->alpha = sc->rho / pq;
-        }
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], count, sc);
     }
 }
 
-// r = b - Ax (Ax already in q), z = D^-1 r, p = z; ||b||^2, ||r||^2, r.z.
+// ---------------------------------------------------------------- SELL SpMV
+// One warp per slice of 32 node rows, lane r owns row r: for every block k of
+// the row it reads the block column and the ND*ND values (each a 128-byte
+// coalesced warp load), gathers ND entries of x and accumulates ND outputs.
+// DIFF: the values hold the difference form of the operator -- off-diagonal
+// blocks K_AB and, in the diagonal slot, the block row sum S_A = sum_B K_AB --
+// and the product is (K x)_A = sum_{B != A} K_AB (x_B - x_A) + S_A x_A, which is
+// K x exactly but keeps the products small for smooth fields, so FP32 storage
+// loses far less on the near-rigid modes that decide CG convergence.
+template <int ND, class V, class X, class ACC, bool DOT, bool DIFF = false>
+__global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64_t *__restrict__ sl_ptr,
+                                                        const int *__restrict__ sl_width, const int *__restrict__ col,
+                                                        const V *__restrict__ val, const X *__restrict__ x,
+                                                        X *__restrict__ y, double *part, unsigned int *count,
+                                                        PcgScal *sc)
+{
+    if (DOT && halted(sc)) return;
+    const int s = blockIdx.x * (NTHREADS / 32) + (threadIdx.x >> 5);
+    const int r = threadIdx.x & 31;
+    double acc[1] = {0.0};
+    if (s < nslices) {
+        const int64_t base = sl_ptr[s];
+        const int w = sl_width[s];
+        const int arow = s * 32 + r;
+        ACC yy[ND], xa[ND];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            yy[i] = 0;
+            xa[i] = DIFF ? (ACC)x[(int64_t)arow * ND + i] : (ACC)0;
+        }
+        const V *vp = val + base * (ND * ND) + r;
+        const int *cp = col + base + r;
+#pragma unroll 4
+        for (int k = 0; k < w; ++k) {
+            const int c = __ldg(cp + 32 * k);
+            ACC xb[ND];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+                xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
+                if (DIFF && c != arow) xb[j] -= xa[j];
+            }
+            const V *vk = vp + (int64_t)k * (32 * ND * ND);
+#pragma unroll
+            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldg(vk + 32 * (i * ND + j)) * xb[j];
+        }
+        const int64_t a = (int64_t)s * 32 + r;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            y[a * ND + i] = (X)yy[i];
+            if (DOT) acc[0] += (double)x[a * ND + i] * (double)yy[i];
+        }
+    }
+    if (!DOT) return;
+    block_sum<1>(acc);
+    if (publish_partials<1>(acc, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], count, sc);
+    }
+}
+
+// ---------------------------------------------------------------- vector kernels
+// r = b - Ax (Ax in q), z = D^-1 r, p = z; ||b||^2, ||r||^2, r.z.
 template <class X>
 __global__ void __launch_bounds__(NTHREADS) k_pcg_init(int nchunks, const double *__restrict__ b,
                                                        const X *__restrict__ q, const X *__restrict__ dinv,
                                                        X *__restrict__ r, X *__restrict__ z, X *__restrict__ p,
-                                                       double *part, unsigned int *count, PcgScal *sc, double rtol,
-                                                       const double *bscale)
+                                                       double *part, unsigned int *count, PcgScal *sc, double rtol)
 {
     double v[3] = {0, 0, 0};
-    const double bs = bscale ? *bscale : 1.0;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
         for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
             int row = c * CHUNK + i;
-            double bb = b[row] * bs;
+            double bb = b[row];
             X rr = (X)bb - q[row];
             X zz = rr * dinv[row];
             r[row] = rr;
@@ -155,11 +246,13 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_init(int nchunks, const double
     if (publish_partials<3>(v, part, count)) {
         double t[3];
         final_sums<3>(part, t);
+        if (threadIdx.x != 0) return;
         *count = 0;
         sc->bnorm2 = t[0];
         sc->rnorm2 = t[1];
         sc->rho = t[2];
         sc->iters = 0;
+        sc->zcoef = 1.0;
         double normb = sqrt(t[0]);
         if (normb == 0.0) normb = 1.0;
         if (sc->done == 0) {
@@ -169,6 +262,7 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_init(int nchunks, const double
     }
 }
 
+// FP64 drop-in update (x += alpha p etc.) with the IML convergence test.
 template <class X>
 __global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restrict__ x, X *__restrict__ r,
                                                          X *__restrict__ z, const X *__restrict__ p,
@@ -176,7 +270,7 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restr
                                                          double *part, unsigned int *count, PcgScal *sc, double rtol,
                                                          int maxit)
 {
-    if (sc->done) return;
+    if (halted(sc)) return;
     const X alpha = (X)sc->alpha;
     double v[2] = {0, 0};
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
@@ -194,13 +288,13 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restr
     if (publish_partials<2>(v, part, count)) {
         double t[2];
         final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
         *count = 0;
         sc->rnorm2 = t[0];
         sc->iters += 1;
         double normb = sqrt(sc->bnorm2);
         if (normb == 0.0) normb = 1.0;
-        double resid = sqrt(t[0]) / normb;
-        if (resid <= rtol) {
+        if (sqrt(t[0]) / normb <= rtol) {
             sc->done = 1;
         } else if (!isfinite(t[1]) || !(t[1] > 0.0)) {
             sc->done = 2;
@@ -210,7 +304,96 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restr
             sc->beta = t[1] / sc->rho;
             sc->rho_old = sc->rho;
             sc->rho = t[1];
+            sc->zcoef = 1.0;
         }
+    }
+}
+
+// Mixed update: d += alpha p (FP32 increment), r -= alpha q, z = D^-1 r. Asks
+// for an FP64 residual replacement once ||r|| fell by RELIABLE_DROP since the
+// last one or below the tolerance; then rho is left for the replacement.
+template <class X>
+__global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__restrict__ d, X *__restrict__ r,
+                                                           X *__restrict__ z, const X *__restrict__ p,
+                                                           const X *__restrict__ q, const X *__restrict__ dinv,
+                                                           double *part, unsigned int *count, PcgScal *sc, int maxit)
+{
+    if (halted(sc)) return;
+    const X alpha = (X)sc->alpha;
+    double v[2] = {0, 0};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
+        for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
+            int row = c * CHUNK + i;
+            d[row] += alpha * p[row];
+            X rr = r[row] - alpha * q[row];
+            X zz = rr * dinv[row];
+            r[row] = rr;
+            z[row] = zz;
+            v[0] += (double)rr * (double)rr;
+            v[1] += (double)rr * (double)zz;
+        }
+    block_sum<2>(v);
+    if (publish_partials<2>(v, part, count)) {
+        double t[2];
+        final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        if (!isfinite(t[0]) || !isfinite(t[1])) {
+            sc->done = 2;
+        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 ||
+                   !(t[1] > 0.0) || sc->iters >= maxit) {
+            sc->reliable = 1;
+        } else {
+            sc->beta = t[1] / sc->rho;
+            sc->rho_old = sc->rho;
+            sc->rho = t[1];
+            sc->zcoef = 1.0;
+        }
+    }
+}
+
+// Residual replacement: r32 = r64, z = D^-1 r32, beta = r.z / rho (0 at the start).
+template <class X>
+__global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const double *__restrict__ r64,
+                                                            X *__restrict__ r, X *__restrict__ z,
+                                                            const X *__restrict__ p, const X *__restrict__ dinv,
+                                                            double *part, unsigned int *count, PcgScal *sc, int first,
+                                                            int orth)
+{
+    double v[3] = {0, 0, 0};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
+        for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
+            int row = c * CHUNK + i;
+            double r6 = r64[row];
+            X rr = (X)r6;
+            X zz = rr * dinv[row];
+            r[row] = rr;
+            z[row] = zz;
+            v[0] += r6 * r6;
+            v[1] += (double)rr * (double)zz;
+            v[2] += (double)rr * (double)p[row];
+        }
+    block_sum<3>(v);
+    if (publish_partials<3>(v, part, count)) {
+        double t[3];
+        final_sums<3>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rmax2 = t[0];
+        sc->rnorm2 = t[0];
+        if (!isfinite(t[1]) || !(t[1] > 0.0)) {
+            sc->done = 2;
+        } else {
+            sc->beta = first ? 0.0 : t[1] / sc->rho;
+            // restore r.p = 0 lost by the replacement: p <- p - (r.p / r.z) z before
+            // p = z + beta p, i.e. p = (1 - beta*gamma) z + beta p
+            double gamma = (orth && !first) ? t[2] / t[1] : 0.0;
+            sc->zcoef = 1.0 - sc->beta * gamma;
+            sc->rho = t[1];
+        }
+        sc->reliable = 0;
     }
 }
 
@@ -218,36 +401,14 @@ template <class X>
 __global__ void __launch_bounds__(NTHREADS) k_pcg_pupdate(int n, const X *__restrict__ z, X *__restrict__ p,
                                                           const PcgScal *sc)
 {
-    if (sc->done) return;
+    if (halted(sc)) return;
     const X beta = (X)sc->beta;
+    const X zc = (X)sc->zcoef;
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x)
-        p[row] = z[row] + beta * p[row];
+        p[row] = zc * z[row] + beta * p[row];
 }
 
-// D^-1 from the diagonal (DiagPreconditioner::init, diagpre.C:40-56).
-template <class X, class V>
-__global__ void k_diag_inv(int npad, const int64_t *__restrict__ diagpos, const V *__restrict__ val, X *dinv,
-                           PcgScal *sc)
-{
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= npad) return;
-    int64_t p = diagpos[r];
-    double d = p >= 0 ? (double)val[p] : 0.0;
-    if (d == 0.0) {
-        sc->done = 3;
-        dinv[r] = 0;
-    } else {
-        dinv[r] = (X)(1.0 / d);
-    }
-}
-
-__global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__restrict__ b)
-{
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        b[i] = (float)a[i];
-}
-
-// r = b - A x in FP64 (x FP64), residual norm partials; used by the refinement loop.
+// r = b - Ax in FP64, ||r||^2 and ||b||^2 into out2.
 __global__ void __launch_bounds__(NTHREADS) k_residual64(int nchunks, const double *__restrict__ b,
                                                          const double *__restrict__ ax, double *__restrict__ r,
                                                          double *part, unsigned int *count, double *out2)
@@ -265,77 +426,197 @@ __global__ void __launch_bounds__(NTHREADS) k_residual64(int nchunks, const doub
     if (publish_partials<2>(v, part, count)) {
         double t[2];
         final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
         *count = 0;
         out2[0] = t[0];
         out2[1] = t[1];
     }
 }
 
-// x64 += d32 (solution update in FP64), clears d.
-__global__ void k_axpy_update(int n, double *__restrict__ x, float *__restrict__ d, double scale)
+// x64 += d (FP64 solution update), d = 0.
+__global__ void k_fold_increment(int n, double *__restrict__ x, float *__restrict__ d)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += (double)d[i] * scale;
+        x[i] += (double)d[i];
         d[i] = 0.0f;
     }
 }
 
-inline int vec_grid(int nchunks) { return nchunks < NUM_SMS * GRID_MULT ? nchunks : NUM_SMS * GRID_MULT; }
-
-template <class V, class X, bool DOT>
-int launch_spmv_tpr(ogb_ctx *ctx, int tpr, int nchunks, int64_t nzt, const int64_t *rowptr, const int *colind,
-                    const V *val, const X *x, X *y, double *part, unsigned int *count, PcgScal *sc)
+// D^-1 from the diagonal (DiagPreconditioner::init, diagpre.C:40-56).
+template <class X, class V>
+__global__ void k_diag_inv_csr(int n, const int64_t *__restrict__ diagpos, const V *__restrict__ val, X *dinv,
+                               PcgScal *sc)
 {
-    int g = vec_grid(nchunks);
-    cudaStream_t s = ctx->stream;
-    prof_begin(ctx);
-    switch (tpr) {
-    case 2: k_spmv<2, V, X, DOT><<<g, NTHREADS, 0, s>>>(nchunks, rowptr, colind, val, x, y, part, count, sc); break;
-    case 4: k_spmv<4, V, X, DOT><<<g, NTHREADS, 0, s>>>(nchunks, rowptr, colind, val, x, y, part, count, sc); break;
-    case 8: k_spmv<8, V, X, DOT><<<g, NTHREADS, 0, s>>>(nchunks, rowptr, colind, val, x, y, part, count, sc); break;
-    case 16: k_spmv<16, V, X, DOT><<<g, NTHREADS, 0, s>>>(nchunks, rowptr, colind, val, x, y, part, count, sc); break;
-    default: k_spmv<32, V, X, DOT><<<g, NTHREADS, 0, s>>>(nchunks, rowptr, colind, val, x, y, part, count, sc); break;
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int64_t p = diagpos[r];
+    double d = p >= 0 ? (double)val[p] : 0.0;
+    if (d == 0.0) {
+        sc->done = 3;
+        dinv[r] = 0;
+    } else {
+        dinv[r] = (X)(1.0 / d);
     }
-    if (ctx->prof) {
-        // algorithmic bytes: values + column indices + row pointers + x (once) + y
-        int64_t n = (int64_t)nchunks * CHUNK;
-        prof_end(ctx, (double)nzt * (sizeof(V) + sizeof(int)) + (double)(n + 1) * sizeof(int64_t) +
-                          (double)n * sizeof(X) * 2);
+}
+
+template <int ND, class X, class V>
+__global__ void k_diag_inv_sell(int nrows, const int64_t *__restrict__ diag, const V *__restrict__ val, X *dinv,
+                                PcgScal *sc)
+{
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nrows) return;
+    int64_t slot = diag[a];
+    int r = (int)(slot & 31);
+    const V *vb = val + (slot - r) * (ND * ND) + r;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+        double v = (double)vb[32 * (d * ND + d)];
+        if (v == 0.0) {
+            sc->done = 3;
+            dinv[(int64_t)a * ND + d] = 0;
+        } else {
+            dinv[(int64_t)a * ND + d] = (X)(1.0 / v);
+        }
+    }
+}
+
+__global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__restrict__ b)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+__global__ void k_eq_to_ns(int neq, const int *__restrict__ ns_of_eq, const double *__restrict__ xe,
+                           double *__restrict__ xn)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < neq) xn[ns_of_eq[e]] = xe[e];
+}
+
+__global__ void k_ns_to_eq(int neq, const int *__restrict__ ns_of_eq, const double *__restrict__ xn,
+                           double *__restrict__ xe)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < neq) xe[e] = xn[ns_of_eq[e]];
+}
+
+inline int vec_grid(int nchunks) { return nchunks < NUM_SMS * GRID_MULT ? nchunks : NUM_SMS * GRID_MULT; }
+inline unsigned nb(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
+
+// ---------------------------------------------------------------- operator
+struct Op {
+    bool sell = false;
+    int64_t n = 0;            // vector length (multiple of CHUNK)
+    // CSR
+    const int64_t *rowptr = nullptr;
+    const int *colind = nullptr;
+    const int64_t *diagpos = nullptr;
+    int tpr = 8;
+    int64_t nzt = 0;
+    // SELL
+    const SellMat *S = nullptr;
+    int nchunks() const { return (int)(n / CHUNK); }
+    int spmv_grid() const { return sell ? (int)ceil_div(S->nslices, NTHREADS / 32) : vec_grid(nchunks()); }
+};
+
+Op make_op(ogb_mtrx *m, bool use_sell)
+{
+    Op op;
+    if (use_sell) {
+        op.sell = true;
+        op.S = &m->sell;
+        op.n = m->sell.nns();
+    } else {
+        op.n = m->npad;
+        op.rowptr = m->rowptr.p;
+        op.colind = m->colind.p;
+        op.diagpos = m->diagpos.p;
+        op.tpr = m->spmv_tpr;
+        op.nzt = m->nnz + (m->npad - m->neq);
+    }
+    return op;
+}
+
+template <class V, class X, bool DOT, class ACC = V, bool DIFF = false>
+int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double *part, unsigned int *count,
+             PcgScal *sc)
+{
+    cudaStream_t s = ctx->stream;
+    const int g = op.spmv_grid();
+    double bytes;
+    prof_begin(ctx);
+    if (op.sell) {
+        const SellMat &S = *op.S;
+        if (S.nd == 3)
+            k_sell_spmv<3, V, X, ACC, DOT, DIFF><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y,
+                                                              part, count, sc);
+        else
+            k_sell_spmv<2, V, X, ACC, DOT, DIFF><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y,
+                                                              part, count, sc);
+        bytes = (double)S.nslots * (S.nd * S.nd * sizeof(V) + sizeof(int)) + (double)S.nslices * 12 +
+                (double)op.n * sizeof(X) * 2;
+    } else {
+        const int nch = op.nchunks();
+        switch (op.tpr) {
+        case 2: k_spmv<2, V, X, ACC, DOT><<<g, NTHREADS, 0, s>>>(nch, op.rowptr, op.colind, val, x, y, part, count, sc); break;
+        case 4: k_spmv<4, V, X, ACC, DOT><<<g, NTHREADS, 0, s>>>(nch, op.rowptr, op.colind, val, x, y, part, count, sc); break;
+        case 8: k_spmv<8, V, X, ACC, DOT><<<g, NTHREADS, 0, s>>>(nch, op.rowptr, op.colind, val, x, y, part, count, sc); break;
+        case 16: k_spmv<16, V, X, ACC, DOT><<<g, NTHREADS, 0, s>>>(nch, op.rowptr, op.colind, val, x, y, part, count, sc); break;
+        default: k_spmv<32, V, X, ACC, DOT><<<g, NTHREADS, 0, s>>>(nch, op.rowptr, op.colind, val, x, y, part, count, sc); break;
+        }
+        bytes = (double)op.nzt * (sizeof(V) + sizeof(int)) + (double)(op.n + 1) * sizeof(int64_t) +
+                (double)op.n * sizeof(X) * 2;
+    }
+    prof_end(ctx, bytes);
+    count_launch(ctx);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+template <class X, class V>
+int launch_diag_inv(ogb_ctx *ctx, const Op &op, const V *val, X *dinv, PcgScal *sc)
+{
+    cudaStream_t s = ctx->stream;
+    if (op.sell) {
+        int nrows = op.S->nslices * 32;
+        if (op.S->nd == 3) k_diag_inv_sell<3, X, V><<<nb(nrows), NTHREADS, 0, s>>>(nrows, op.S->diag.p, val, dinv, sc);
+        else k_diag_inv_sell<2, X, V><<<nb(nrows), NTHREADS, 0, s>>>(nrows, op.S->diag.p, val, dinv, sc);
+    } else {
+        k_diag_inv_csr<X, V><<<nb(op.n), NTHREADS, 0, s>>>((int)op.n, op.diagpos, val, dinv, sc);
     }
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
     return OGB_OK;
 }
 
-int ensure_workspace(ogb_mtrx *m, bool mixed)
+int ensure_workspace(ogb_mtrx *m, const Op &op, bool mixed)
 {
-    int np = m->npad;
-    int nch = np / CHUNK;
-    OGB_CHECK(m->w_x.alloc(np));
-    OGB_CHECK(m->w_b.alloc(np));
-    OGB_CHECK(m->w_part.alloc((size_t)4 * vec_grid(nch)));
+    const int64_t n = op.n;
+    int gmax = op.spmv_grid() > vec_grid(op.nchunks()) ? op.spmv_grid() : vec_grid(op.nchunks());
+    OGB_CHECK(m->w_part.alloc((size_t)4 * gmax));
     OGB_CHECK(m->w_scal.alloc(2));
     OGB_CHECK(m->h_scal.alloc(2));
+    OGB_CHECK(m->w_d.alloc(4));
     if (!m->w_count.p) {
         OGB_CHECK(m->w_count.alloc(1));
         OGB_CUDA(cudaMemsetAsync(m->w_count.p, 0, sizeof(unsigned int), m->ctx->stream));
     }
-    if (!mixed) {
-        OGB_CHECK(m->w_r.alloc(np));
-        OGB_CHECK(m->w_z.alloc(np));
-        OGB_CHECK(m->w_p.alloc(np));
-        OGB_CHECK(m->w_q.alloc(np));
-        OGB_CHECK(m->w_dinv.alloc(np));
-    } else {
-        OGB_CHECK(m->w_r.alloc(np));
-        OGB_CHECK(m->w_q.alloc(np));
-        OGB_CHECK(m->w_d.alloc(4));
-        OGB_CHECK(m->w_r32.alloc(np));
-        OGB_CHECK(m->w_z32.alloc(np));
-        OGB_CHECK(m->w_p32.alloc(np));
-        OGB_CHECK(m->w_q32.alloc(np));
-        OGB_CHECK(m->w_dinv32.alloc(np));
-        OGB_CHECK(m->w_x32.alloc(np));
+    if (!mixed || !m->ctx->mixed_vec32) {
+        OGB_CHECK(m->w_r.alloc(n));
+        OGB_CHECK(m->w_z.alloc(n));
+        OGB_CHECK(m->w_p.alloc(n));
+        OGB_CHECK(m->w_q.alloc(n));
+        OGB_CHECK(m->w_dinv.alloc(n));
+    }
+    if (mixed) {
+        OGB_CHECK(m->n_r64.alloc(n));
+        OGB_CHECK(m->n_q64.alloc(n));
+        OGB_CHECK(m->w_r32.alloc(n));
+        OGB_CHECK(m->w_z32.alloc(n));
+        OGB_CHECK(m->w_p32.alloc(n));
+        OGB_CHECK(m->w_q32.alloc(n));
+        OGB_CHECK(m->w_dinv32.alloc(n));
+        OGB_CHECK(m->n_d32.alloc(n));
     }
     return OGB_OK;
 }
@@ -349,45 +630,135 @@ int read_scal(ogb_mtrx *m, PcgScal &out)
     return OGB_OK;
 }
 
-// Generic PCG on (V matrix values, X vectors). b64 is the FP64 right-hand side
-// (scaled by *bscale when given), the solution accumulates in x (type X).
-template <class V, class X>
-int pcg_core(ogb_mtrx *m, const V *val, const double *b64, const double *bscale, X *x, X *r, X *z, X *p, X *q,
-             X *dinv, double rtol, int maxit, PcgScal &res)
+constexpr int BATCH = 16;
+
+// FP64 PCG (drop-in semantics) on op-space vectors b (read), x (initial guess, updated).
+int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, double *x, double rtol, int maxit,
+               PcgScal &res)
 {
     ogb_ctx *ctx = m->ctx;
     cudaStream_t s = ctx->stream;
-    const int np = m->npad, nch = np / CHUNK;
-    const int g = vec_grid(nch);
+    const int nch = op.nchunks(), g = vec_grid(nch);
     PcgScal *sc = m->w_scal.p;
+    double *r = m->w_r.p, *z = m->w_z.p, *p = m->w_p.p, *q = m->w_q.p, *dinv = m->w_dinv.p;
     OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
-    k_diag_inv<X, V><<<(unsigned)ceil_div(np, NTHREADS), NTHREADS, 0, s>>>(np, m->diagpos.p, val, dinv, sc);
-    count_launch(ctx);
-    // q = A x0
-    OGB_CHECK((launch_spmv_tpr<V, X, false>(ctx, m->spmv_tpr, nch, m->nnz + (m->npad - m->neq), m->rowptr.p, m->colind.p, val, x, q, nullptr,
-                                             nullptr, nullptr)));
-    k_pcg_init<X><<<g, NTHREADS, 0, s>>>(nch, b64, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol, bscale);
+    OGB_CHECK((launch_diag_inv<double, double>(ctx, op, val, dinv, sc)));
+    OGB_CHECK((apply_op<double, double, false>(ctx, op, val, x, q, nullptr, nullptr, nullptr)));
+    k_pcg_init<double><<<g, NTHREADS, 0, s>>>(nch, b, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol);
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
-    const int batch = 16;
     int it = 0;
     for (;;) {
         OGB_CHECK(read_scal(m, res));
-        if (res.done) break;
-        if (it >= maxit) break;
-        for (int k = 0; k < batch; ++k) {
-            OGB_CHECK((launch_spmv_tpr<V, X, true>(ctx, m->spmv_tpr, nch, m->nnz + (m->npad - m->neq), m->rowptr.p, m->colind.p, val, p, q,
-                                                    m->w_part.p, m->w_count.p, sc)));
-            k_pcg_update<X><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc, rtol,
-                                                   maxit);
-            k_pcg_pupdate<X><<<g, NTHREADS, 0, s>>>(np, z, p, sc);
+        if (res.done || it >= maxit) break;
+        for (int k = 0; k < BATCH; ++k) {
+            OGB_CHECK((apply_op<double, double, true>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc)));
+            k_pcg_update<double><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
+                                                        rtol, maxit);
+            k_pcg_pupdate<double><<<g, NTHREADS, 0, s>>>((int)op.n, z, p, sc);
             count_launch(ctx, 2);
         }
         OGB_CUDA(cudaGetLastError());
-        it += batch;
+        it += BATCH;
     }
     return OGB_OK;
 }
+
+// Mixed precision with FP64 residual replacement (see file header). X is the
+// type of the Krylov vectors: float keeps everything but the residual and the
+// solution in FP32 (the solution increment d is folded into x64 at every
+// replacement); double keeps r, z, p, q and x in FP64 while the matrix stays
+// FP32 and the SpMV multiplies and accumulates in FP32.
+template <class X>
+int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v32, const double *b, double *x,
+                   double rtol, int maxit, ogb_solve_info *info)
+{
+    ogb_ctx *ctx = m->ctx;
+    cudaStream_t s = ctx->stream;
+    const int nch = op.nchunks(), g = vec_grid(nch);
+    const int n = (int)op.n;
+    constexpr bool F32 = sizeof(X) == 4;
+    PcgScal *sc = m->w_scal.p;
+    X *r, *z, *p, *q, *dinv, *d;
+    if constexpr (F32) {
+        r = m->w_r32.p; z = m->w_z32.p; p = m->w_p32.p; q = m->w_q32.p; dinv = m->w_dinv32.p; d = m->n_d32.p;
+    } else {
+        r = m->w_r.p; z = m->w_z.p; p = m->w_p.p; q = m->w_q.p; dinv = m->w_dinv.p; d = x;
+    }
+    double *r64 = m->n_r64.p, *q64 = m->n_q64.p;
+    OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
+    if constexpr (F32) OGB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(X), s));
+    OGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(X), s));
+    // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
+    OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
+    const bool diff = op.sell && ctx->mixed_diff;
+    int iters = 0, replacements = 0, status = OGB_E_NOTCONV;
+    double achieved = 0.0;
+    bool first = true;
+    PcgScal res{};
+    for (;;) {
+        // FP64 residual of the current x64
+        OGB_CHECK((apply_op<double, double, false>(ctx, op, v64, x, q64, nullptr, nullptr, nullptr)));
+        k_residual64<<<g, NTHREADS, 0, s>>>(nch, b, q64, r64, m->w_part.p, m->w_count.p, m->w_d.p);
+        count_launch(ctx);
+        double h2[2];
+        OGB_CUDA(cudaMemcpyAsync(h2, m->w_d.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        OGB_CUDA(cudaStreamSynchronize(s));
+        double normb = sqrt(h2[1]);
+        if (normb == 0.0) normb = 1.0;
+        achieved = sqrt(h2[0]) / normb;
+        if (achieved <= rtol) { status = OGB_OK; break; }
+        if (!isfinite(achieved)) { status = OGB_E_BREAKDOWN; break; }
+        if (iters >= maxit) break;
+        if (first) {
+            // the recursive residual below half the target asks for an FP64 check
+            double th[2] = {0.25 * rtol * rtol * normb * normb, ctx->mixed_drop * ctx->mixed_drop};
+            OGB_CUDA(cudaMemcpyAsync(&sc->tol2, th, 2 * sizeof(double), cudaMemcpyHostToDevice, s));
+            OGB_CUDA(cudaStreamSynchronize(s));
+        }
+        // replacement: r = r64, z = D^-1 r, beta; then p = z + beta p
+        k_mixed_replace<X><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
+                                                  first ? 1 : 0, ctx->mixed_orth ? 1 : 0);
+        k_pcg_pupdate<X><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+        count_launch(ctx, 2);
+        first = false;
+        ++replacements;
+        // iterations on the FP32 operator until the next replacement is due
+        for (;;) {
+            OGB_CHECK(read_scal(m, res));
+            if (res.done || res.reliable) break;
+            for (int k = 0; k < BATCH; ++k) {
+                if (diff)
+                    OGB_CHECK((apply_op<float, X, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+                else
+                    OGB_CHECK((apply_op<float, X, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+                k_mixed_update<X><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
+                                                         maxit);
+                k_pcg_pupdate<X><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+                count_launch(ctx, 2);
+            }
+            OGB_CUDA(cudaGetLastError());
+        }
+        iters = res.iters;
+        if (res.done == 3) { status = OGB_E_ZERODIAG; break; }
+        if (res.done == 2) { status = OGB_E_BREAKDOWN; break; }
+        if constexpr (F32) {
+            // fold the FP32 increment into the FP64 solution
+            k_fold_increment<<<NUM_SMS * 8, NTHREADS, 0, s>>>(n, x, d);
+            count_launch(ctx);
+        }
+        if (replacements > 400) break;
+    }
+    if (info) {
+        info->iterations = iters;
+        info->outer = replacements;
+        info->achieved = achieved;
+        info->status = status;
+    }
+    return OGB_OK;
+}
+
+bool sell_current(const ogb_mtrx *m) { return m->has_sell && m->sell.v32_version == m->version; }
 
 }  // namespace
 
@@ -404,97 +775,104 @@ int pick_tpr(const ogb_mtrx *m)
 
 int spmv64(ogb_mtrx *m, const double *x, double *y)
 {
-    return launch_spmv_tpr<double, double, false>(m->ctx, m->spmv_tpr, m->npad / CHUNK, m->nnz + (m->npad - m->neq),
-                                                  m->rowptr.p, m->colind.p,
-                                                  m->val.p, x, y, nullptr, nullptr, nullptr);
+    Op op = make_op(m, false);
+    return apply_op<double, double, false>(m->ctx, op, m->val.p, x, y, nullptr, nullptr, nullptr);
 }
 
-static int map_status(const PcgScal &s, ogb_solve_info *info)
+static int map_status(int done)
 {
-    int st;
-    switch (s.done) {
-    case 1: st = OGB_OK; break;
-    case 2: st = OGB_E_BREAKDOWN; break;
-    case 3: st = OGB_E_ZERODIAG; break;
-    default: st = OGB_E_NOTCONV; break;
+    switch (done) {
+    case 1: return OGB_OK;
+    case 2: return OGB_E_BREAKDOWN;
+    case 3: return OGB_E_ZERODIAG;
+    default: return OGB_E_NOTCONV;
     }
-    if (info) info->status = st;
-    return st;
 }
 
-// FP64 drop-in solve on padded device vectors (b, x of length npad; padding zero).
+// Operator-space copies of b and x: node space for the SELL operator, the
+// padded equation space (b, x themselves) for CSR.
+static int to_op_space(ogb_mtrx *m, const Op &op, const double *b, double *x, const double **bo, double **xo)
+{
+    if (!op.sell) {
+        *bo = b;
+        *xo = x;
+        return OGB_OK;
+    }
+    cudaStream_t s = m->ctx->stream;
+    OGB_CHECK(m->n_b.alloc(op.n));
+    OGB_CHECK(m->n_x.alloc(op.n));
+    OGB_CUDA(cudaMemsetAsync(m->n_b.p, 0, op.n * sizeof(double), s));
+    OGB_CUDA(cudaMemsetAsync(m->n_x.p, 0, op.n * sizeof(double), s));
+    k_eq_to_ns<<<nb(m->neq), NTHREADS, 0, s>>>(m->neq, m->sell.ns_of_eq.p, b, m->n_b.p);
+    k_eq_to_ns<<<nb(m->neq), NTHREADS, 0, s>>>(m->neq, m->sell.ns_of_eq.p, x, m->n_x.p);
+    count_launch(m->ctx, 2);
+    *bo = m->n_b.p;
+    *xo = m->n_x.p;
+    return OGB_OK;
+}
+
+static int from_op_space(ogb_mtrx *m, const Op &op, double *x)
+{
+    if (!op.sell) return OGB_OK;
+    k_ns_to_eq<<<nb(m->neq), NTHREADS, 0, m->ctx->stream>>>(m->neq, m->sell.ns_of_eq.p, m->n_x.p, x);
+    count_launch(m->ctx);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+// FP64 drop-in solve on padded equation-space device vectors (padding zero).
 int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
-    OGB_CHECK(ensure_workspace(m, false));
+    const bool use_sell = sell_current(m);
+    Op op = make_op(m, use_sell);
+    OGB_CHECK(ensure_workspace(m, op, false));
+    const double *bo;
+    double *xo;
+    OGB_CHECK(to_op_space(m, op, b, x, &bo, &xo));
     PcgScal res{};
-    OGB_CHECK((pcg_core<double, double>(m, m->val.p, b, nullptr, x, m->w_r.p, m->w_z.p, m->w_p.p, m->w_q.p,
-                                        m->w_dinv.p, rtol, maxit, res)));
+    OGB_CHECK(pcg64_core(m, op, use_sell ? m->sell.v64.p : m->val.p, bo, xo, rtol, maxit, res));
+    OGB_CHECK(from_op_space(m, op, x));
     double normb = sqrt(res.bnorm2);
     if (normb == 0.0) normb = 1.0;
     if (info) {
         info->iterations = res.iters;
         info->outer = 0;
         info->achieved = sqrt(res.rnorm2) / normb;
+        info->status = map_status(res.done);
     }
-    map_status(res, info);
     return OGB_OK;
 }
 
-// Mixed precision: FP32 matrix + FP32 Jacobi-PCG inner solves inside an FP64
-// iterative-refinement loop; the residual f - K u and the update u += d are FP64.
 int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
     ogb_ctx *ctx = m->ctx;
-    cudaStream_t s = ctx->stream;
-    OGB_CHECK(ensure_workspace(m, true));
-    const int np = m->npad, nch = np / CHUNK;
-    const int64_t ntot = m->nnz + (np - m->neq);
-    if (m->val32_version != m->version) {
-        OGB_CHECK(m->val32.alloc(ntot));
-        k_to_float<<<NUM_SMS * 8, NTHREADS, 0, s>>>(ntot, m->val.p, m->val32.p);
-        count_launch(ctx);
-        m->val32_version = m->version;
+    const bool use_sell = sell_current(m);
+    Op op = make_op(m, use_sell);
+    OGB_CHECK(ensure_workspace(m, op, true));
+    const double *v64;
+    const float *v32;
+    if (use_sell) {
+        v64 = m->sell.v64.p;
+        v32 = m->sell.v32.p;
+    } else {
+        const int64_t ntot = m->nnz + (m->npad - m->neq);
+        if (m->val32_version != m->version) {
+            OGB_CHECK(m->val32.alloc(ntot));
+            k_to_float<<<NUM_SMS * 8, NTHREADS, 0, ctx->stream>>>(ntot, m->val.p, m->val32.p);
+            count_launch(ctx);
+            m->val32_version = m->version;
+        }
+        v64 = m->val.p;
+        v32 = m->val32.p;
     }
-    const double inner_tol = 1e-4;
-    int total_inner = 0, outer = 0;
-    double achieved = 0.0;
-    int status = OGB_E_NOTCONV;
-    OGB_CUDA(cudaMemsetAsync(m->w_x32.p, 0, np * sizeof(float), s));
-    for (outer = 0; outer < 30; ++outer) {
-        // r = b - A x in FP64
-        OGB_CHECK(spmv64(m, x, m->w_q.p));
-        k_residual64<<<vec_grid(nch), NTHREADS, 0, s>>>(nch, b, m->w_q.p, m->w_r.p, m->w_part.p, m->w_count.p,
-                                                         m->w_d.p);
-        count_launch(ctx);
-        double h2[2];
-        OGB_CUDA(cudaMemcpyAsync(h2, m->w_d.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-        OGB_CUDA(cudaStreamSynchronize(s));
-        double normb = sqrt(h2[1]);
-        if (normb == 0.0) normb = 1.0;
-        achieved = sqrt(h2[0]) / normb;
-        if (achieved <= rtol) { status = OGB_OK; break; }
-        if (!isfinite(achieved)) { status = OGB_E_BREAKDOWN; break; }
-        if (total_inner >= maxit) break;
-        // inner FP32 solve A d = r, d0 = 0, scaled by 1/||r|| to stay in FP32 range
-        double inv = 1.0 / sqrt(h2[0]);
-        OGB_CUDA(cudaMemcpyAsync(m->w_d.p + 2, &inv, sizeof(double), cudaMemcpyHostToDevice, s));
-        PcgScal res{};
-        double tol_in = inner_tol;
-        if (tol_in < rtol / achieved * 0.5) tol_in = rtol / achieved * 0.5;
-        OGB_CHECK((pcg_core<float, float>(m, m->val32.p, m->w_r.p, m->w_d.p + 2, m->w_x32.p, m->w_r32.p,
-                                          m->w_z32.p, m->w_p32.p, m->w_q32.p, m->w_dinv32.p, tol_in,
-                                          maxit - total_inner, res)));
-        total_inner += res.iters;
-        if (res.done == 3) { status = OGB_E_ZERODIAG; break; }
-        k_axpy_update<<<NUM_SMS * 8, NTHREADS, 0, s>>>(np, x, m->w_x32.p, sqrt(h2[0]));
-        count_launch(ctx);
-    }
-    if (info) {
-        info->iterations = total_inner;
-        info->outer = outer;
-        info->achieved = achieved;
-        info->status = status;
-    }
+    const double *bo;
+    double *xo;
+    OGB_CHECK(to_op_space(m, op, b, x, &bo, &xo));
+    if (m->ctx->mixed_vec32)
+        OGB_CHECK(pcg_mixed_core<float>(m, op, v64, v32, bo, xo, rtol, maxit, info));
+    else
+        OGB_CHECK(pcg_mixed_core<double>(m, op, v64, v32, bo, xo, rtol, maxit, info));
+    OGB_CHECK(from_op_space(m, op, x));
     return OGB_OK;
 }
 

@@ -26,6 +26,10 @@ ERRORS = {-1: "OGB_E_ARG", -2: "OGB_E_CUDA", -3: "OGB_E_STATE", -4: "OGB_E_PATTE
           -9: "OGB_E_LIMIT"}
 PREC_FP64 = 0
 PREC_MIXED = 1
+OPT_MIXED_VEC32 = 1
+OPT_MIXED_DIFF = 2
+OPT_MIXED_ORTH = 3
+OPT_MIXED_DROP_PPM = 4
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
@@ -52,6 +56,7 @@ SIGNATURES = {
     "ogb_ctx_stream": (_vp, [_vp]),
     "ogb_ctx_synchronize": (_i, [_vp]),
     "ogb_ctx_kernel_launches": (_i64, [_vp]),
+    "ogb_ctx_set_option": (_i, [_vp, _i, _i64]),
     "ogb_ctx_profile_enable": (_i, [_vp, _i]),
     "ogb_ctx_profile_read": (_i, [_vp, _pd, _pi64, _pd]),
     "ogb_mtrx_create": (_i, [_vp, C.POINTER(_vp)]),
@@ -143,6 +148,9 @@ class Context:
 
     def kernel_launches(self) -> int:
         return self.lib.ogb_ctx_kernel_launches(self.h)
+
+    def set_option(self, option: int, value: int):
+        _check(self.lib.ogb_ctx_set_option(self.h, option, value))
 
     def profile(self, enable: bool):
         _check(self.lib.ogb_ctx_profile_enable(self.h, int(enable)))

@@ -201,3 +201,43 @@ def test_negative_tet_volume_rejected(ctx, native_lib):
     with pytest.raises(native_lib.OgbError) as ei:
         model.assemble_stiffness(A)
     assert ei.value.code == -8
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-6)])
+def test_partially_constrained_nodes(precision, tol, ctx, native_lib, oracle):
+    """x=L face with only u_x prescribed: active nodes with prescribed slots
+    (identity rows in the node-block solver storage)."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_block_pull(10, 4, 3, jitter=0.2, seed=4, material=mg.Material(1, 210e9, 0.3),
+                             end_disp=1e-3)
+    ref = oracle.linear_static(oracle.mesh_dict(mesh), rtol=1e-14)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    u, reac, info = model.linear_static(A, rtol=1e-12 if precision == 0 else 1e-10, maxit=100000,
+                                        precision=precision)
+    assert info.status == 0
+    assert rel(u, ref["u"]) < tol
+    assert rel(reac, ref["reac"]) < tol
+
+
+def test_sell_and_csr_operators_agree(ctx, native_lib, oracle):
+    """The node-block solver storage and the CSR storage give the same solve."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(16, 4, 4, jitter=0.2, seed=2)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    model.assemble_stiffness(A)
+    neq, _ = model.neq()
+    eq = model.equations()
+    b = np.zeros(neq)
+    b[eq[eq > 0] - 1] = mesh.nodal_load[eq > 0]
+    s = native_lib.GpuPcgSolver(lstol=1e-12, lsiter=100000)
+    x1 = np.zeros(neq)
+    assert s.solve(A, b, x1) == 0
+    it1 = s.last.iterations
+    A.set_at(1, 1, A.at(1, 1))   # any CSR-side mutation makes the solver use the CSR storage
+    x2 = np.zeros(neq)
+    assert s.solve(A, b, x2) == 0
+    assert abs(s.last.iterations - it1) <= 2
+    assert rel(x1, x2) < 1e-9
