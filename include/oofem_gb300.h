@@ -81,7 +81,7 @@ OGB_API int ogb_ctx_synchronize(ogb_ctx *ctx);
 OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 /* Tuning options of a context (no reference counterpart):
  *   OGB_OPT_MIXED_VEC32 (0/1): mixed solves keep the CG vectors in FP32 instead
- *   of FP64 (default 0). */
+ *   of FP64 (default 1). */
 #define OGB_OPT_MIXED_VEC32 1
 /*   OGB_OPT_MIXED_DIFF (0/1): FP32 operator stored in difference form (default 1).
  *   OGB_OPT_MIXED_ORTH (0/1): restore r.p = 0 after an FP64 residual replacement.
@@ -90,6 +90,11 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 #define OGB_OPT_MIXED_DIFF 2
 #define OGB_OPT_MIXED_ORTH 3
 #define OGB_OPT_MIXED_DROP_PPM 4
+/*   OGB_OPT_MIXED_P32 (0/1): mixed solves keep p and q = K p in FP32 only. */
+#define OGB_OPT_MIXED_P32 5
+/*   OGB_OPT_MIXED_X64 (0/1): with FP32 vectors, accumulate the solution in FP64
+ *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
+#define OGB_OPT_MIXED_X64 6
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, every SpMV launch (the dominant kernel of the
  * solve) is bracketed by CUDA events on the context stream; ogb_ctx_profile_read

@@ -333,6 +333,8 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
     case OGB_OPT_MIXED_VEC32: ctx->mixed_vec32 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_DIFF: ctx->mixed_diff = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_ORTH: ctx->mixed_orth = value != 0; return OGB_OK;
+    case OGB_OPT_MIXED_P32: ctx->mixed_p32 = value != 0; return OGB_OK;
+    case OGB_OPT_MIXED_X64: ctx->mixed_x64 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
         ctx->mixed_drop = value * 1e-6;

@@ -153,9 +153,11 @@ struct ogb_ctx {
     std::vector<cudaEvent_t> ev_pending;   // start/stop pairs
     double prof_ms = 0.0, prof_bytes = 0.0, pending_bytes = 0.0;
     int64_t prof_count = 0;
-    bool mixed_vec32 = false;   // mixed solve with FP32 Krylov vectors (see solver.cu)
+    bool mixed_vec32 = true;    // mixed solve with FP32 Krylov vectors (see solver.cu)
     bool mixed_diff = true;     // FP32 operator in difference form (see solver.cu)
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
+    bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)
+    bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;

@@ -21,13 +21,15 @@
 // rows with zero right-hand side).
 //
 // Mixed precision (OGB_PREC_MIXED): CG applies the FP32 matrix with FP32
-// multiply-adds; whenever the recursive residual has dropped by a factor 10
-// (or reached the tolerance) it is replaced by the true FP64 residual
-// r = b - A64 x64, keeping the search direction (reliable updates), so the
-// FP64 solution converges to the FP64 system. Convergence is decided on that
-// FP64 residual. The Krylov vectors are FP64 by default (FP32 vectors lose
-// orthogonality on these ill-conditioned systems and need several times more
-// iterations); an all-FP32 vector variant is selectable per context.
+// multiply-adds on FP32 vectors r, z, p, q; only the solution x is FP64
+// (x += alpha p, the one FP64 operation per row). Whenever the recursive
+// residual has dropped by a factor 10 (or reached the tolerance) it is replaced
+// by the true FP64 residual r = b - A64 x64, keeping the search direction
+// (reliable updates), so x converges to the solution of the FP64 system;
+// convergence is decided on that FP64 residual. Accumulating x itself in FP32
+// between replacements (OGB_OPT_MIXED_X64 0) or an FP32 operator not in
+// difference form (OGB_OPT_MIXED_DIFF 0) triples the iteration count on the
+// ill-conditioned cantilever; both stay selectable for study.
 #include <math.h>
 
 #include "internal.cuh"
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
         const int *cp = col + base + r;
 #pragma unroll 4
         for (int k = 0; k < w; ++k) {
-            const int c = __ldg(cp + 32 * k);
+            const int c = __ldcs(cp + 32 * k);   // values and columns are streamed once: evict first
             ACC xb[ND];
 #pragma unroll
             for (int j = 0; j < ND; ++j) {
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 #pragma unroll
             for (int i = 0; i < ND; ++i)
 #pragma unroll
-                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldg(vk + 32 * (i * ND + j)) * xb[j];
+                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
         }
         const int64_t a = (int64_t)s * 32 + r;
 #pragma unroll
@@ -312,10 +314,10 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restr
 // Mixed update: d += alpha p (FP32 increment), r -= alpha q, z = D^-1 r. Asks
 // for an FP64 residual replacement once ||r|| fell by RELIABLE_DROP since the
 // last one or below the tolerance; then rho is left for the replacement.
-template <class X>
+template <class X, class P>
 __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__restrict__ d, X *__restrict__ r,
-                                                           X *__restrict__ z, const X *__restrict__ p,
-                                                           const X *__restrict__ q, const X *__restrict__ dinv,
+                                                           X *__restrict__ z, const P *__restrict__ p,
+                                                           const P *__restrict__ q, const X *__restrict__ dinv,
                                                            double *part, unsigned int *count, PcgScal *sc, int maxit)
 {
     if (halted(sc)) return;
@@ -324,8 +326,8 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__res
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
         for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
             int row = c * CHUNK + i;
-            d[row] += alpha * p[row];
-            X rr = r[row] - alpha * q[row];
+            d[row] += alpha * (X)p[row];
+            X rr = r[row] - alpha * (X)q[row];
             X zz = rr * dinv[row];
             r[row] = rr;
             z[row] = zz;
@@ -355,10 +357,10 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__res
 }
 
 // Residual replacement: r32 = r64, z = D^-1 r32, beta = r.z / rho (0 at the start).
-template <class X>
+template <class X, class P>
 __global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const double *__restrict__ r64,
                                                             X *__restrict__ r, X *__restrict__ z,
-                                                            const X *__restrict__ p, const X *__restrict__ dinv,
+                                                            const P *__restrict__ p, const X *__restrict__ dinv,
                                                             double *part, unsigned int *count, PcgScal *sc, int first,
                                                             int orth)
 {
@@ -397,15 +399,188 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const d
     }
 }
 
-template <class X>
-__global__ void __launch_bounds__(NTHREADS) k_pcg_pupdate(int n, const X *__restrict__ z, X *__restrict__ p,
+template <class X, class P = X>
+__global__ void __launch_bounds__(NTHREADS) k_pcg_pupdate(int n, const X *__restrict__ z, P *__restrict__ p,
                                                           const PcgScal *sc)
 {
     if (halted(sc)) return;
     const X beta = (X)sc->beta;
     const X zc = (X)sc->zcoef;
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x)
-        p[row] = zc * z[row] + beta * p[row];
+        p[row] = (P)(zc * z[row] + beta * (X)p[row]);
+}
+
+// ---- unrolled variants: each thread owns rows t, t+256, t+512, t+768 of a
+// chunk (CHUNK = 4 * NTHREADS); all loads of the four rows are issued before
+// any arithmetic, so a warp keeps 4 coalesced requests per vector in flight.
+// FP64 x, r, z, dinv; p, q of type P. MIXED: the mixed-precision test (ask for a
+// residual replacement); otherwise the IML convergence test.
+template <bool MIXED, class P>
+__global__ void __launch_bounds__(NTHREADS) k_update4(int nchunks, double *__restrict__ x, double *__restrict__ r,
+                                                      double *__restrict__ z, const P *__restrict__ p,
+                                                      const P *__restrict__ q, const double *__restrict__ dinv,
+                                                      double *part, unsigned int *count, PcgScal *sc, double rtol,
+                                                      int maxit)
+{
+    if (halted(sc)) return;
+    const double alpha = sc->alpha;
+    double v[2] = {0, 0};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t row0 = (int64_t)c * CHUNK + threadIdx.x;
+        double xx[4], rr[4], dd[4];
+        P pp[4], qq[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t row = row0 + k * NTHREADS;
+            xx[k] = x[row];
+            rr[k] = r[row];
+            dd[k] = dinv[row];
+            pp[k] = p[row];
+            qq[k] = q[row];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t row = row0 + k * NTHREADS;
+            xx[k] += alpha * (double)pp[k];
+            rr[k] -= alpha * (double)qq[k];
+            const double zz = rr[k] * dd[k];
+            x[row] = xx[k];
+            r[row] = rr[k];
+            z[row] = zz;
+            v[0] += rr[k] * rr[k];
+            v[1] += rr[k] * zz;
+        }
+    }
+    block_sum<2>(v);
+    if (publish_partials<2>(v, part, count)) {
+        double t[2];
+        final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        if (MIXED) {
+            if (!isfinite(t[0]) || !isfinite(t[1])) {
+                sc->done = 2;
+            } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit) {
+                sc->reliable = 1;
+                return;
+            }
+        } else {
+            double normb = sqrt(sc->bnorm2);
+            if (normb == 0.0) normb = 1.0;
+            if (sqrt(t[0]) / normb <= rtol) { sc->done = 1; return; }
+            if (!isfinite(t[1]) || !(t[1] > 0.0)) { sc->done = 2; return; }
+            if (sc->iters >= maxit) { sc->done = 4; return; }
+        }
+        if (sc->done) return;
+        sc->beta = t[1] / sc->rho;
+        sc->rho_old = sc->rho;
+        sc->rho = t[1];
+        sc->zcoef = 1.0;
+    }
+}
+
+// p = zcoef z + beta p, same row mapping.
+template <class P>
+__global__ void __launch_bounds__(NTHREADS) k_pupdate4(int nchunks, const double *__restrict__ z, P *__restrict__ p,
+                                                       const PcgScal *sc)
+{
+    if (halted(sc)) return;
+    const double beta = sc->beta, zc = sc->zcoef;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t row0 = (int64_t)c * CHUNK + threadIdx.x;
+        double zz[4];
+        P pp[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            zz[k] = z[row0 + k * NTHREADS];
+            pp[k] = p[row0 + k * NTHREADS];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[row0 + k * NTHREADS] = (P)(zc * zz[k] + beta * (double)pp[k]);
+    }
+}
+
+// Mixed update with FP32 r, z, dinv, p, q and the FP64 solution x: the only
+// FP64 arithmetic per row is x += alpha p; dot products are formed from FP32
+// products, summed in FP32 over the thread's 4 rows of a chunk and in FP64 above.
+__global__ void __launch_bounds__(NTHREADS) k_update_rz32(int nchunks, double *__restrict__ x, float *__restrict__ r,
+                                                          float *__restrict__ z, const float *__restrict__ p,
+                                                          const float *__restrict__ q, const float *__restrict__ dinv,
+                                                          double *part, unsigned int *count, PcgScal *sc, int maxit)
+{
+    if (halted(sc)) return;
+    const double alpha = sc->alpha;
+    const float af = (float)alpha;
+    double v[2] = {0, 0};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t row0 = (int64_t)c * CHUNK + threadIdx.x;
+        double xx[4];
+        float rr[4], dd[4], pp[4], qq[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t row = row0 + k * NTHREADS;
+            xx[k] = x[row];
+            rr[k] = r[row];
+            dd[k] = dinv[row];
+            pp[k] = p[row];
+            qq[k] = q[row];
+        }
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t row = row0 + k * NTHREADS;
+            xx[k] += alpha * (double)pp[k];
+            rr[k] = fmaf(-af, qq[k], rr[k]);
+            const float zz = rr[k] * dd[k];
+            x[row] = xx[k];
+            r[row] = rr[k];
+            z[row] = zz;
+            s0 = fmaf(rr[k], rr[k], s0);
+            s1 = fmaf(rr[k], zz, s1);
+        }
+        v[0] += (double)s0;
+        v[1] += (double)s1;
+    }
+    block_sum<2>(v);
+    if (publish_partials<2>(v, part, count)) {
+        double t[2];
+        final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        if (!isfinite(t[0]) || !isfinite(t[1])) {
+            sc->done = 2;
+        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit) {
+            sc->reliable = 1;
+        } else {
+            sc->beta = t[1] / sc->rho;
+            sc->rho_old = sc->rho;
+            sc->rho = t[1];
+            sc->zcoef = 1.0;
+        }
+    }
+}
+
+// p = zcoef z + beta p in FP32.
+__global__ void __launch_bounds__(NTHREADS) k_pupdate_f32(int nchunks, const float *__restrict__ z,
+                                                          float *__restrict__ p, const PcgScal *sc)
+{
+    if (halted(sc)) return;
+    const float beta = (float)sc->beta, zc = (float)sc->zcoef;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t row0 = (int64_t)c * CHUNK + threadIdx.x;
+        float zz[4], pp[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            zz[k] = z[row0 + k * NTHREADS];
+            pp[k] = p[row0 + k * NTHREADS];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[row0 + k * NTHREADS] = fmaf(zc, zz[k], beta * pp[k]);
+    }
 }
 
 // r = b - Ax in FP64, ||r||^2 and ||b||^2 into out2.
@@ -601,7 +776,7 @@ int ensure_workspace(ogb_mtrx *m, const Op &op, bool mixed)
         OGB_CHECK(m->w_count.alloc(1));
         OGB_CUDA(cudaMemsetAsync(m->w_count.p, 0, sizeof(unsigned int), m->ctx->stream));
     }
-    if (!mixed || !m->ctx->mixed_vec32) {
+    if (true) {
         OGB_CHECK(m->w_r.alloc(n));
         OGB_CHECK(m->w_z.alloc(n));
         OGB_CHECK(m->w_p.alloc(n));
@@ -653,9 +828,9 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
         if (res.done || it >= maxit) break;
         for (int k = 0; k < BATCH; ++k) {
             OGB_CHECK((apply_op<double, double, true>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc)));
-            k_pcg_update<double><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
-                                                        rtol, maxit);
-            k_pcg_pupdate<double><<<g, NTHREADS, 0, s>>>((int)op.n, z, p, sc);
+            k_update4<false, double><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
+                                                            sc, rtol, maxit);
+            k_pupdate4<double><<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
             count_launch(ctx, 2);
         }
         OGB_CUDA(cudaGetLastError());
@@ -669,7 +844,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
 // solution in FP32 (the solution increment d is folded into x64 at every
 // replacement); double keeps r, z, p, q and x in FP64 while the matrix stays
 // FP32 and the SpMV multiplies and accumulates in FP32.
-template <class X>
+template <class X, class P>
 int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v32, const double *b, double *x,
                    double rtol, int maxit, ogb_solve_info *info)
 {
@@ -679,16 +854,22 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     const int n = (int)op.n;
     constexpr bool F32 = sizeof(X) == 4;
     PcgScal *sc = m->w_scal.p;
-    X *r, *z, *p, *q, *dinv, *d;
+    X *r, *z, *dinv, *d;
+    P *p, *q;
     if constexpr (F32) {
-        r = m->w_r32.p; z = m->w_z32.p; p = m->w_p32.p; q = m->w_q32.p; dinv = m->w_dinv32.p; d = m->n_d32.p;
+        r = m->w_r32.p; z = m->w_z32.p; dinv = m->w_dinv32.p; d = m->n_d32.p;
     } else {
-        r = m->w_r.p; z = m->w_z.p; p = m->w_p.p; q = m->w_q.p; dinv = m->w_dinv.p; d = x;
+        r = m->w_r.p; z = m->w_z.p; dinv = m->w_dinv.p; d = x;
+    }
+    if constexpr (sizeof(P) == 4) {
+        p = m->w_p32.p; q = m->w_q32.p;
+    } else {
+        p = m->w_p.p; q = m->w_q.p;
     }
     double *r64 = m->n_r64.p, *q64 = m->n_q64.p;
     OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
     if constexpr (F32) OGB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(X), s));
-    OGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(X), s));
+    OGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(P), s));
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
     OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
     const bool diff = op.sell && ctx->mixed_diff;
@@ -717,9 +898,9 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             OGB_CUDA(cudaStreamSynchronize(s));
         }
         // replacement: r = r64, z = D^-1 r, beta; then p = z + beta p
-        k_mixed_replace<X><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
-                                                  first ? 1 : 0, ctx->mixed_orth ? 1 : 0);
-        k_pcg_pupdate<X><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+        k_mixed_replace<X, P><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
+                                                     first ? 1 : 0, ctx->mixed_orth ? 1 : 0);
+        k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
         count_launch(ctx, 2);
         first = false;
         ++replacements;
@@ -729,12 +910,24 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             if (res.done || res.reliable) break;
             for (int k = 0; k < BATCH; ++k) {
                 if (diff)
-                    OGB_CHECK((apply_op<float, X, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+                    OGB_CHECK((apply_op<float, P, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
                 else
-                    OGB_CHECK((apply_op<float, X, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
-                k_mixed_update<X><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
-                                                         maxit);
-                k_pcg_pupdate<X><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+                    OGB_CHECK((apply_op<float, P, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+                if constexpr (F32) {
+                    if (ctx->mixed_x64) {
+                        k_update_rz32<<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
+                                                              maxit);
+                        k_pupdate_f32<<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
+                    } else {
+                        k_mixed_update<X, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p,
+                                                                    m->w_count.p, sc, maxit);
+                        k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+                    }
+                } else {
+                    k_update4<true, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
+                                                              sc, rtol, maxit);
+                    k_pupdate4<P><<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
+                }
                 count_launch(ctx, 2);
             }
             OGB_CUDA(cudaGetLastError());
@@ -869,9 +1062,11 @@ int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, o
     double *xo;
     OGB_CHECK(to_op_space(m, op, b, x, &bo, &xo));
     if (m->ctx->mixed_vec32)
-        OGB_CHECK(pcg_mixed_core<float>(m, op, v64, v32, bo, xo, rtol, maxit, info));
+        OGB_CHECK((pcg_mixed_core<float, float>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
+    else if (m->ctx->mixed_p32)
+        OGB_CHECK((pcg_mixed_core<double, float>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
     else
-        OGB_CHECK(pcg_mixed_core<double>(m, op, v64, v32, bo, xo, rtol, maxit, info));
+        OGB_CHECK((pcg_mixed_core<double, double>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
     OGB_CHECK(from_op_space(m, op, x));
     return OGB_OK;
 }

@@ -30,6 +30,8 @@ OPT_MIXED_VEC32 = 1
 OPT_MIXED_DIFF = 2
 OPT_MIXED_ORTH = 3
 OPT_MIXED_DROP_PPM = 4
+OPT_MIXED_P32 = 5
+OPT_MIXED_X64 = 6
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
