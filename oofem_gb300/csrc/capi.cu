@@ -67,6 +67,13 @@ static cudaEvent_t take_event(ogb_ctx *ctx)
 void prof_begin(ogb_ctx *ctx)
 {
     if (!ctx->prof) return;
+    if (ctx->capture_events) {   // inside a graph capture: the graph owns its events
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, ctx->stream);
+        ctx->capture_events->push_back(e);
+        return;
+    }
     cudaEvent_t e = take_event(ctx);
     if (!e) return;
     cudaEventRecord(e, ctx->stream);
@@ -75,7 +82,16 @@ void prof_begin(ogb_ctx *ctx)
 
 void prof_end(ogb_ctx *ctx, double bytes)
 {
-    if (!ctx->prof || ctx->ev_pending.size() % 2 == 0) return;
+    if (!ctx->prof) return;
+    if (ctx->capture_events) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, ctx->stream);
+        ctx->capture_events->push_back(e);
+        ctx->capture_bytes += bytes;
+        return;
+    }
+    if (ctx->ev_pending.size() % 2 == 0) return;
     cudaEvent_t e = take_event(ctx);
     if (!e) {
         ctx->ev_pool.push_back(ctx->ev_pending.back());

@@ -154,6 +154,9 @@ struct ogb_ctx {
     double prof_ms = 0.0, prof_bytes = 0.0, pending_bytes = 0.0;
     int64_t prof_count = 0;
     bool mixed_vec32 = true;    // mixed solve with FP32 Krylov vectors (see solver.cu)
+    bool use_graphs = true;     // replay PCG iteration batches as CUDA graphs
+    std::vector<cudaEvent_t> *capture_events = nullptr;   // profiling events recorded into a graph
+    double capture_bytes = 0.0;
     bool mixed_diff = true;     // FP32 operator in difference form (see solver.cu)
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)

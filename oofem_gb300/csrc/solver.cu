@@ -807,6 +807,62 @@ int read_scal(ogb_mtrx *m, PcgScal &out)
 
 constexpr int BATCH = 16;
 
+// One batch of PCG iterations recorded as a CUDA graph and replayed until the
+// device-side scalars say the system is done. With profiling on, the SpMV
+// launches of the batch are bracketed by event nodes owned by the graph; their
+// times are added after every replay (the host waits for each batch anyway).
+struct IterGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> ev;
+    double bytes = 0.0;
+    ~IterGraph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+    template <class F>
+    int capture(ogb_ctx *ctx, F &&launch_batch)
+    {
+        cudaGraph_t g = nullptr;
+        ctx->capture_events = &ev;
+        ctx->capture_bytes = 0.0;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            ctx->capture_events = nullptr;
+            return cuda_fail(e, "cudaStreamBeginCapture");
+        }
+        int r = launch_batch();
+        cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+        ctx->capture_events = nullptr;
+        bytes = ctx->capture_bytes;
+        if (r != OGB_OK) {
+            if (g) cudaGraphDestroy(g);
+            return r;
+        }
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        return OGB_OK;
+    }
+    int launch(ogb_ctx *ctx)
+    {
+        OGB_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        return OGB_OK;
+    }
+    // after the stream is synchronized
+    void harvest(ogb_ctx *ctx)
+    {
+        if (!ctx->prof) return;
+        for (size_t k = 0; k + 1 < ev.size(); k += 2) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) ctx->prof_ms += ms;
+            ctx->prof_count++;
+        }
+        ctx->prof_bytes += bytes;
+    }
+};
+
 // FP64 PCG (drop-in semantics) on op-space vectors b (read), x (initial guess, updated).
 int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, double *x, double rtol, int maxit,
                PcgScal &res)
@@ -822,10 +878,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
     k_pcg_init<double><<<g, NTHREADS, 0, s>>>(nch, b, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol);
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
-    int it = 0;
-    for (;;) {
-        OGB_CHECK(read_scal(m, res));
-        if (res.done || it >= maxit) break;
+    auto batch = [&]() -> int {
         for (int k = 0; k < BATCH; ++k) {
             OGB_CHECK((apply_op<double, double, true>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc)));
             k_update4<false, double><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
@@ -834,6 +887,21 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
             count_launch(ctx, 2);
         }
         OGB_CUDA(cudaGetLastError());
+        return OGB_OK;
+    };
+    IterGraph graph;
+    if (ctx->use_graphs) OGB_CHECK(graph.capture(ctx, batch));
+    int it = 0;
+    for (;;) {
+        OGB_CHECK(read_scal(m, res));
+        if (ctx->use_graphs && it > 0) graph.harvest(ctx);
+        if (res.done || it >= maxit) break;
+        if (ctx->use_graphs) {
+            OGB_CHECK(graph.launch(ctx));
+            count_launch(ctx, 3 * BATCH);
+        } else {
+            OGB_CHECK(batch());
+        }
         it += BATCH;
     }
     return OGB_OK;
@@ -877,6 +945,34 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     double achieved = 0.0;
     bool first = true;
     PcgScal res{};
+    auto batch = [&]() -> int {
+        for (int k = 0; k < BATCH; ++k) {
+            if (diff)
+                OGB_CHECK((apply_op<float, P, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+            else
+                OGB_CHECK((apply_op<float, P, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+            if constexpr (F32) {
+                if (ctx->mixed_x64) {
+                    k_update_rz32<<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
+                                                          maxit);
+                    k_pupdate_f32<<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
+                } else {
+                    k_mixed_update<X, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
+                                                                sc, maxit);
+                    k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
+                }
+            } else {
+                k_update4<true, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
+                                                          rtol, maxit);
+                k_pupdate4<P><<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
+            }
+            count_launch(ctx, 2);
+        }
+        OGB_CUDA(cudaGetLastError());
+        return OGB_OK;
+    };
+    IterGraph graph;
+    if (ctx->use_graphs) OGB_CHECK(graph.capture(ctx, batch));
     for (;;) {
         // FP64 residual of the current x64
         OGB_CHECK((apply_op<double, double, false>(ctx, op, v64, x, q64, nullptr, nullptr, nullptr)));
@@ -905,40 +1001,26 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
         first = false;
         ++replacements;
         // iterations on the FP32 operator until the next replacement is due
-        for (;;) {
+        for (int nb = 0;; ++nb) {
             OGB_CHECK(read_scal(m, res));
+            if (ctx->use_graphs && nb > 0) graph.harvest(ctx);
             if (res.done || res.reliable) break;
-            for (int k = 0; k < BATCH; ++k) {
-                if (diff)
-                    OGB_CHECK((apply_op<float, P, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
-                else
-                    OGB_CHECK((apply_op<float, P, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
-                if constexpr (F32) {
-                    if (ctx->mixed_x64) {
-                        k_update_rz32<<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
-                                                              maxit);
-                        k_pupdate_f32<<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
-                    } else {
-                        k_mixed_update<X, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p,
-                                                                    m->w_count.p, sc, maxit);
-                        k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
-                    }
-                } else {
-                    k_update4<true, P><<<g, NTHREADS, 0, s>>>(nch, d, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
-                                                              sc, rtol, maxit);
-                    k_pupdate4<P><<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
-                }
-                count_launch(ctx, 2);
+            if (ctx->use_graphs) {
+                OGB_CHECK(graph.launch(ctx));
+                count_launch(ctx, 3 * BATCH);
+            } else {
+                OGB_CHECK(batch());
             }
-            OGB_CUDA(cudaGetLastError());
         }
         iters = res.iters;
         if (res.done == 3) { status = OGB_E_ZERODIAG; break; }
         if (res.done == 2) { status = OGB_E_BREAKDOWN; break; }
         if constexpr (F32) {
-            // fold the FP32 increment into the FP64 solution
-            k_fold_increment<<<NUM_SMS * 8, NTHREADS, 0, s>>>(n, x, d);
-            count_launch(ctx);
+            if (!ctx->mixed_x64) {
+                // fold the FP32 increment into the FP64 solution
+                k_fold_increment<<<NUM_SMS * 8, NTHREADS, 0, s>>>(n, x, d);
+                count_launch(ctx);
+            }
         }
         if (replacements > 400) break;
     }
