@@ -158,6 +158,25 @@ OGB_API int ogb_pcg_solve(ogb_mtrx *m, const double *b, double *x, double rtol, 
 OGB_API int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b_dev, double *x_dev, double rtol,
                       int maxit, int precision, ogb_solve_info *info);
 
+/* Allocation-free Jacobi-PCG. No counterpart in the reference: it exists for
+ * callers that must not allocate device memory while they run (an application
+ * that reserves the GPU's memory for its own pool at start-up, or a time-step
+ * loop in which cudaMalloc/cudaFree -- cudaFree synchronizes the device -- would
+ * stall every stream). The caller passes the CSR matrix (n+1 row pointers,
+ * sorted 0-based column indices, values), b and the initial guess x, all in
+ * device memory, and the stream to run on (cudaStream_t, 0 = default stream).
+ * Same semantics and status codes as ogb_pcg_solve with OGB_PREC_FP64.
+ * Limit: n <= 131072 equations (OGB_E_LIMIT beyond). The work vectors live in
+ * one file-scope device array of about 5.2 MB that every GPU which loads the
+ * library holds until the process exits; the first call on a device looks up
+ * that array's device address (do it before any stream capture). All calls
+ * share the array: each call clears the parts that must start at zero, and
+ * calls that overlap on the GPU race on it. It calls no cudaMalloc, cudaFree
+ * or allocating library routine. */
+OGB_API int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr_dev, const int *colind_dev, const double *val_dev,
+                                  const double *b_dev, double *x_dev, double rtol, int maxit, void *stream,
+                                  ogb_solve_info *info);
+
 /* ---- element backend: LSpace / PlaneStress2d / LTRSpace element loops
  *      (NLStructuralElement::computeStiffnessMatrix nlstructuralelement.C:332-446,
  *      ::giveInternalForcesVector :151-240; EngngModel::assemble engngm.C:889-1037,

@@ -1156,3 +1156,255 @@ int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, o
 int extract_diag(ogb_mtrx *m) { (void)m; return OGB_OK; }
 
 }  // namespace ogb
+
+// ---------------------------------------------------------------------------
+// Allocation-free Jacobi-PCG (ogb_pcg_solve_noalloc).
+//
+// For callers that must not allocate device memory once they are running --
+// for example an application that reserves the GPU's memory for its own pool
+// at start-up, or a time-stepping loop in which a cudaMalloc/cudaFree (cudaFree
+// synchronizes the whole device) would stall every stream. The caller passes
+// the CSR matrix, b and x in device memory; the solver's work vectors live in
+// the file-scope array below, which every GPU that loads this library holds
+// until the process exits. All calls share it: a call clears what must start at
+// zero, and two calls that overlap on the GPU (different streams or threads)
+// race on it.
+namespace ogb {
+namespace {
+
+constexpr int NOALLOC_MAX_ROWS = 1 << 17;           // 131,072 equations
+constexpr int NOALLOC_GRID = NUM_SMS * 2;           // fixed grid: deterministic reductions
+constexpr size_t NOALLOC_DOUBLES = (size_t)5 * NOALLOC_MAX_ROWS + 4 * NOALLOC_GRID + 16;
+
+// r, z, p, q, dinv (NOALLOC_MAX_ROWS each), reduction partials, the PcgScal
+// record and the last-block counter: about 5.2 MB.
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
+
+struct NoallocView {
+    double *r, *z, *p, *q, *dinv, *part;
+    PcgScal *sc;
+    unsigned int *count;
+};
+
+__host__ __device__ inline NoallocView noalloc_view(double *base)
+{
+    NoallocView v;
+    v.r = base;
+    v.z = base + NOALLOC_MAX_ROWS;
+    v.p = base + 2 * (size_t)NOALLOC_MAX_ROWS;
+    v.q = base + 3 * (size_t)NOALLOC_MAX_ROWS;
+    v.dinv = base + 4 * (size_t)NOALLOC_MAX_ROWS;
+    v.part = base + 5 * (size_t)NOALLOC_MAX_ROWS;
+    v.sc = reinterpret_cast<PcgScal *>(v.part + 4 * NOALLOC_GRID);
+    v.count = reinterpret_cast<unsigned int *>(v.sc + 1);
+    return v;
+}
+
+// D^-1 by a binary search for the diagonal of each (sorted) row.
+__global__ void k_na_diag(int n, const int64_t *__restrict__ rowptr, const int *__restrict__ colind,
+                          const double *__restrict__ val, double *scratch)
+{
+    NoallocView w = noalloc_view(scratch);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int64_t lo = rowptr[i], hi = rowptr[i + 1] - 1;
+        double d = 0.0;
+        while (lo <= hi) {
+            int64_t mid = (lo + hi) >> 1;
+            int c = colind[mid];
+            if (c < i) lo = mid + 1;
+            else if (c > i) hi = mid - 1;
+            else { d = val[mid]; break; }
+        }
+        if (d == 0.0) {
+            w.sc->done = 3;
+            w.dinv[i] = 0.0;
+        } else {
+            w.dinv[i] = 1.0 / d;
+        }
+    }
+}
+
+// y = A x (8 lanes per row); with DOT also x.y -> alpha = rho / p.q.
+template <bool DOT>
+__global__ void __launch_bounds__(NTHREADS) k_na_spmv(int n, const int64_t *__restrict__ rowptr,
+                                                      const int *__restrict__ colind, const double *__restrict__ val,
+                                                      const double *x, double *y, double *scratch)
+{
+    NoallocView w = noalloc_view(scratch);
+    if (DOT && w.sc->done) return;
+    const int sub = threadIdx.x >> 3, lane = threadIdx.x & 7;
+    double acc[1] = {0.0};
+    for (int64_t rb = (int64_t)blockIdx.x * (NTHREADS / 8); rb < n; rb += (int64_t)gridDim.x * (NTHREADS / 8)) {
+        const int64_t row = rb + sub;
+        double s = 0.0;
+        if (row < n)
+            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += 8) s += val[k] * x[colind[k]];
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, 8);
+        if (lane == 0 && row < n) {
+            y[row] = s;
+            if (DOT) acc[0] += x[row] * s;
+        }
+    }
+    if (!DOT) return;
+    block_sum<1>(acc);
+    if (publish_partials<1>(acc, w.part, w.count)) {
+        double t[1];
+        final_sums<1>(w.part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], w.count, w.sc);
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_na_init(int n, const double *__restrict__ b, double *scratch,
+                                                      double rtol)
+{
+    NoallocView w = noalloc_view(scratch);
+    double v[3] = {0, 0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double rr = b[i] - w.q[i];
+        double zz = rr * w.dinv[i];
+        w.r[i] = rr;
+        w.z[i] = zz;
+        w.p[i] = zz;
+        v[0] += b[i] * b[i];
+        v[1] += rr * rr;
+        v[2] += rr * zz;
+    }
+    block_sum<3>(v);
+    if (publish_partials<3>(v, w.part, w.count)) {
+        double t[3];
+        final_sums<3>(w.part, t);
+        if (threadIdx.x != 0) return;
+        *w.count = 0;
+        PcgScal *sc = w.sc;
+        sc->bnorm2 = t[0];
+        sc->rnorm2 = t[1];
+        sc->rho = t[2];
+        double normb = sqrt(t[0]);
+        if (normb == 0.0) normb = 1.0;
+        if (sc->done == 0) {
+            if (sqrt(t[1]) / normb <= rtol) sc->done = 1;
+            else if (!isfinite(t[2]) || !(t[2] > 0.0)) sc->done = 2;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_na_update(int n, double *__restrict__ x, double *scratch, double rtol,
+                                                        int maxit)
+{
+    NoallocView w = noalloc_view(scratch);
+    PcgScal *sc = w.sc;
+    if (sc->done) return;
+    const double alpha = sc->alpha;
+    double v[2] = {0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += alpha * w.p[i];
+        double rr = w.r[i] - alpha * w.q[i];
+        double zz = rr * w.dinv[i];
+        w.r[i] = rr;
+        w.z[i] = zz;
+        v[0] += rr * rr;
+        v[1] += rr * zz;
+    }
+    block_sum<2>(v);
+    if (publish_partials<2>(v, w.part, w.count)) {
+        double t[2];
+        final_sums<2>(w.part, t);
+        if (threadIdx.x != 0) return;
+        *w.count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        double normb = sqrt(sc->bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        if (sqrt(t[0]) / normb <= rtol) sc->done = 1;
+        else if (!isfinite(t[1]) || !(t[1] > 0.0)) sc->done = 2;
+        else if (sc->iters >= maxit) sc->done = 4;
+        else {
+            sc->beta = t[1] / sc->rho;
+            sc->rho = t[1];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_na_pupdate(int n, double *scratch)
+{
+    NoallocView w = noalloc_view(scratch);
+    if (w.sc->done) return;
+    const double beta = w.sc->beta;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        w.p[i] = w.z[i] + beta * w.p[i];
+}
+
+// Device address of g_noalloc_scratch, looked up once per device (with that
+// device current) because in host code the symbol's name is only a host-side
+// stand-in, not a device address.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+int noalloc_scratch(double **out)
+{
+    int dev = 0;
+    OGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(OGB_E_LIMIT, "device index beyond the supported range");
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return OGB_OK;
+}
+
+}  // namespace
+}  // namespace ogb
+
+extern "C" int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr, const int *colind, const double *val,
+                                     const double *b, double *x, double rtol, int maxit, void *stream,
+                                     ogb_solve_info *info)
+{
+    using namespace ogb;
+    if (n < 0 || (n > 0 && (!rowptr || !colind || !val || !b || !x)))
+        return fail(OGB_E_ARG, "ogb_pcg_solve_noalloc: null device pointer or negative size");
+    if (n > NOALLOC_MAX_ROWS)
+        return fail(OGB_E_LIMIT, "ogb_pcg_solve_noalloc: " + std::to_string(n) + " equations exceed its fixed maximum of " +
+                                     std::to_string(NOALLOC_MAX_ROWS) + "; use ogb_pcg_solve");
+    double *base = nullptr;
+    OGB_CHECK(noalloc_scratch(&base));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    NoallocView w = noalloc_view(base);
+    // the scalars and the last-block counter must start at zero
+    OGB_CUDA(cudaMemsetAsync(w.sc, 0, sizeof(PcgScal) + sizeof(double), s));
+    const int gv = NOALLOC_GRID;
+    k_na_diag<<<gv, NTHREADS, 0, s>>>(n, rowptr, colind, val, base);
+    k_na_spmv<false><<<gv, NTHREADS, 0, s>>>(n, rowptr, colind, val, x, w.q, base);
+    k_na_init<<<gv, NTHREADS, 0, s>>>(n, b, base, rtol);
+    OGB_CUDA(cudaGetLastError());
+    PcgScal h{};
+    for (int it = 0;; it += BATCH) {
+        OGB_CUDA(cudaMemcpyAsync(&h, w.sc, sizeof(PcgScal), cudaMemcpyDeviceToHost, s));
+        OGB_CUDA(cudaStreamSynchronize(s));
+        if (h.done || it >= maxit) break;
+        for (int k = 0; k < BATCH; ++k) {
+            k_na_spmv<true><<<gv, NTHREADS, 0, s>>>(n, rowptr, colind, val, w.p, w.q, base);
+            k_na_update<<<gv, NTHREADS, 0, s>>>(n, x, base, rtol, maxit);
+            k_na_pupdate<<<gv, NTHREADS, 0, s>>>(n, base);
+        }
+        OGB_CUDA(cudaGetLastError());
+    }
+    double normb = sqrt(h.bnorm2);
+    if (normb == 0.0) normb = 1.0;
+    int st = map_status(h.done);
+    if (info) {
+        info->iterations = h.iters;
+        info->outer = 0;
+        info->achieved = sqrt(h.rnorm2) / normb;
+        info->status = st;
+    }
+    if (st != OGB_OK)
+        set_error(st == OGB_E_ZERODIAG ? "zero diagonal detected"
+                  : st == OGB_E_BREAKDOWN ? "PCG breakdown (rho or p'q not positive/finite)"
+                                          : "PCG did not converge within maxit");
+    return st;
+}

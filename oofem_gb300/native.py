@@ -79,6 +79,7 @@ SIGNATURES = {
     "ogb_mtrx_version": (_i, [_vp, _pi64]),
     "ogb_pcg_solve": (_i, [_vp, _vp, _vp, _d, _i, _i, C.POINTER(SolveInfo)]),
     "ogb_pcg_solve_dev": (_i, [_vp, _vp, _vp, _d, _i, _i, C.POINTER(SolveInfo)]),
+    "ogb_pcg_solve_noalloc": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _i, _vp, C.POINTER(SolveInfo)]),
     "ogb_model_create": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _d, _vp, C.POINTER(_vp)]),
     "ogb_model_destroy": (_i, [_vp]),
     "ogb_model_neq": (_i, [_vp, _pi, _pi]),
