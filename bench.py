@@ -319,13 +319,14 @@ def run_gpu(args):
         "config": {"workload": "hex_cantilever_%dx%dx%d_jitter0.2_seed0" % (WORKLOAD["nx"], WORKLOAD["ny"], WORKLOAD["nz"]),
                    "free_dofs": nfree,
                    "elements": mesh.nelem, "nnz": nnz, "rtol": RTOL, "precision": "mixed FP32 PCG + FP64 IR",
-                   "l2": "inputs larger than L2 (matrix %.2f GB)" % (nnz * 12 / 1e9),
+                   "l2": "inputs larger than L2 (FP32 node-block matrix %.2f GB, FP64 %.2f GB)" % (
+                       nnz * 4.44 / 1e9, nnz * 8.44 / 1e9),
                    "parallelism": f"replicas x{ws}"},
         "solve": {"inner_iterations": info.iterations, "outer": info.outer, "achieved": info.achieved},
         "fp64": {"value": nfree / (ms64 * 1e-3), "ms_per_step": ms64, "iterations": infos64[-1].iterations,
                  "achieved": infos64[-1].achieved},
         "mixed_over_fp64": ms64 / ms,
-        "roofline": {"bound": "hbm", "kernel": "k_spmv (CSR, FP32 values, fused p.q)",
+        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv (node-block SELL-32, FP32 values, difference form, fused p.q)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind,

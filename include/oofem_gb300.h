@@ -96,8 +96,9 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
 #define OGB_OPT_MIXED_X64 6
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
-/* Kernel timing: when enabled, every SpMV launch (the dominant kernel of the
- * solve) is bracketed by CUDA events on the context stream; ogb_ctx_profile_read
+/* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
+ * are bracketed by CUDA events on the context stream -- every launch outside CUDA
+ * graphs, the first of each replayed 16-iteration batch inside them; ogb_ctx_profile_read
  * returns the summed device time (ms), the launch count and the algorithmic
  * bytes of those launches (values + column indices + row pointers + x + y),
  * and resets the counters. No reference counterpart (instrumentation). */

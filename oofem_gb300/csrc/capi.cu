@@ -66,11 +66,12 @@ static cudaEvent_t take_event(ogb_ctx *ctx)
 
 void prof_begin(ogb_ctx *ctx)
 {
-    if (!ctx->prof) return;
+    if (!ctx->prof || !ctx->prof_sample) return;
     if (ctx->capture_events) {   // inside a graph capture: the graph owns its events
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) return;
-        cudaEventRecord(e, ctx->stream);
+        // inside a capture only an external record becomes a timestamp node
+        cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal);
         ctx->capture_events->push_back(e);
         return;
     }
@@ -82,11 +83,11 @@ void prof_begin(ogb_ctx *ctx)
 
 void prof_end(ogb_ctx *ctx, double bytes)
 {
-    if (!ctx->prof) return;
+    if (!ctx->prof || !ctx->prof_sample) return;
     if (ctx->capture_events) {
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) return;
-        cudaEventRecord(e, ctx->stream);
+        cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal);
         ctx->capture_events->push_back(e);
         ctx->capture_bytes += bytes;
         return;
@@ -111,6 +112,7 @@ void prof_harvest(ogb_ctx *ctx)
     for (size_t k = 0; k < n; k += 2) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, ctx->ev_pending[k], ctx->ev_pending[k + 1]) == cudaSuccess) ctx->prof_ms += ms;
+        else cudaGetLastError();   // a failed query must not leak into the next error check
         ctx->ev_pool.push_back(ctx->ev_pending[k]);
         ctx->ev_pool.push_back(ctx->ev_pending[k + 1]);
     }

@@ -157,6 +157,7 @@ struct ogb_ctx {
     bool use_graphs = true;     // replay PCG iteration batches as CUDA graphs
     std::vector<cudaEvent_t> *capture_events = nullptr;   // profiling events recorded into a graph
     double capture_bytes = 0.0;
+    bool prof_sample = true;    // inside a captured batch only the first SpMV is bracketed
     bool mixed_diff = true;     // FP32 operator in difference form (see solver.cu)
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)

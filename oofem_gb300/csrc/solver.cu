@@ -701,6 +701,7 @@ Op make_op(ogb_mtrx *m, bool use_sell)
         op.sell = true;
         op.S = &m->sell;
         op.n = m->sell.nns();
+        op.nzt = m->nnz;
     } else {
         op.n = m->npad;
         op.rowptr = m->rowptr.p;
@@ -728,7 +729,9 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
         else
             k_sell_spmv<2, V, X, ACC, DOT, DIFF><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y,
                                                               part, count, sc);
-        bytes = (double)S.nslots * (S.nd * S.nd * sizeof(V) + sizeof(int)) + (double)S.nslices * 12 +
+        // algorithmic bytes: every stored value and block column once (the SELL
+        // padding slots are not counted), x once and y once
+        bytes = (double)op.nzt * sizeof(V) + (double)op.nzt / (S.nd * S.nd) * sizeof(int) +
                 (double)op.n * sizeof(X) * 2;
     } else {
         const int nch = op.nchunks();
@@ -856,8 +859,12 @@ struct IterGraph {
         if (!ctx->prof) return;
         for (size_t k = 0; k + 1 < ev.size(); k += 2) {
             float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) ctx->prof_ms += ms;
-            ctx->prof_count++;
+            if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) {
+                ctx->prof_ms += ms;
+                ctx->prof_count++;
+            } else {
+                cudaGetLastError();   // a failed query must not leak into the next error check
+            }
         }
         ctx->prof_bytes += bytes;
     }
@@ -880,7 +887,9 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
     OGB_CUDA(cudaGetLastError());
     auto batch = [&]() -> int {
         for (int k = 0; k < BATCH; ++k) {
+            ctx->prof_sample = k == 0 || !ctx->capture_events;   // time one SpMV per replayed batch
             OGB_CHECK((apply_op<double, double, true>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc)));
+            ctx->prof_sample = true;
             k_update4<false, double><<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p,
                                                             sc, rtol, maxit);
             k_pupdate4<double><<<g, NTHREADS, 0, s>>>(nch, z, p, sc);
@@ -947,10 +956,12 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     PcgScal res{};
     auto batch = [&]() -> int {
         for (int k = 0; k < BATCH; ++k) {
+            ctx->prof_sample = k == 0 || !ctx->capture_events;   // time one SpMV per replayed batch
             if (diff)
                 OGB_CHECK((apply_op<float, P, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
             else
                 OGB_CHECK((apply_op<float, P, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+            ctx->prof_sample = true;
             if constexpr (F32) {
                 if (ctx->mixed_x64) {
                     k_update_rz32<<<g, NTHREADS, 0, s>>>(nch, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
