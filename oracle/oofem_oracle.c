@@ -757,16 +757,19 @@ void oro_commit_state(int etype, const double *mat, double *st)
 }
 
 /* a9/a15: internal forces over all elements (EngngModel::assembleVectorFromElements,
- * engngm.C:1351-1533, with InternalForceAssembler), node-indexed output. */
+ * engngm.C:1351-1533, with InternalForceAssembler), node-indexed output; enorm
+ * (optional, ndofpn) receives the per-DOF-id sums of squared element force
+ * entries that NRSolver uses as internalForcesEBENorm. */
 void oro_internal_forces(int etype, int ndim, int nnodes, const double *coords, int nelem,
                          const int *conn, const int *elem_mat, const double *mats,
                          double thickness, const double *u_node, double *state,
-                         double *f_node, double *gp_stress, double *gp_strain)
+                         double *f_node, double *gp_stress, double *gp_strain, double *enorm)
 {
     int nn = oro_nnpe(etype), ndof = oro_ndofpn(etype), ng = oro_ngp(etype);
     int ns = oro_nstress(etype), nl = nn * ndof;
     double xe[24], ue[24], eps[8 * 6], sig[8 * 6], fe[24];
     memset(f_node, 0, (size_t)nnodes * ndof * sizeof(double));
+    if (enorm) memset(enorm, 0, (size_t)ndof * sizeof(double));
     for (int e = 0; e < nelem; ++e) {
         oro_gather_element(etype, ndim, coords, conn, e, xe);
         for (int a = 0; a < nn; ++a)
@@ -783,8 +786,11 @@ void oro_internal_forces(int etype, int ndim, int nnodes, const double *coords, 
         if (gp_strain) memcpy(gp_strain + (size_t)e * ng * ns, eps, (size_t)ng * ns * sizeof(double));
         oro_elem_internal_force(etype, xe, sig, thickness, fe);
         for (int a = 0; a < nn; ++a)
-            for (int d = 0; d < ndof; ++d)
+            for (int d = 0; d < ndof; ++d) {
                 f_node[(size_t)conn[(size_t)e * nn + a] * ndof + d] += fe[a * ndof + d];
+                /* FloatArray::assembleSquared by DOF id (engngm.C:1398-1401) */
+                if (enorm) enorm[d] += fe[a * ndof + d] * fe[a * ndof + d];
+            }
     }
     (void)nl;
 }

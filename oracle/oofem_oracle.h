@@ -84,7 +84,7 @@ void oro_commit_state(int etype, const double *mat, double *state);
 void oro_internal_forces(int etype, int ndim, int nnodes, const double *coords, int nelem,
                          const int *conn, const int *elem_mat, const double *mats,
                          double thickness, const double *u_node, double *state,
-                         double *f_node, double *gp_stress, double *gp_strain);
+                         double *f_node, double *gp_stress, double *gp_strain, double *enorm);
 
 void oro_assemble_tangent(int etype, int ndim, int nnodes, const double *coords, int nelem,
                           const int *conn, const int *elem_mat, const double *mats,

@@ -119,9 +119,10 @@ def assemble_tangent(m: dict, loc, neq, rowptr, colind, state=None):
     return val
 
 
-def internal_forces(m: dict, u_node: np.ndarray, state=None):
+def internal_forces(m: dict, u_node: np.ndarray, state=None, want_enorm=False):
     """Node-indexed internal forces for the total displacement field; updates
-    the temp part of ``state`` in place. Returns (f_node, gp_stress, gp_strain)."""
+    the temp part of ``state`` in place. Returns (f_node, gp_stress, gp_strain)
+    and, with want_enorm, the per-DOF-id element force norms as a 4th item."""
     et = int(m["etype"])
     coords = np.ascontiguousarray(m["coords"], dtype=np.float64)
     conn = np.ascontiguousarray(m["conn"], dtype=np.int32)
@@ -133,9 +134,12 @@ def internal_forces(m: dict, u_node: np.ndarray, state=None):
     eps = np.zeros_like(sig)
     u = np.ascontiguousarray(u_node, dtype=np.float64)
     st = None if state is None else _p(state)
+    en = np.zeros(ndofpn(et))
     lib().oro_internal_forces(et, coords.shape[1], nn, _p(coords), ne, _p(conn), _p(emat),
                               _p(mats), C.c_double(float(m["thickness"])), _p(u), st, _p(f),
-                              _p(sig), _p(eps))
+                              _p(sig), _p(eps), _p(en))
+    if want_enorm:
+        return f, sig, eps, en
     return f, sig, eps
 
 
@@ -200,3 +204,75 @@ def linear_static(m: dict, rtol=1e-12, maxit=100000, load_factor=1.0, bc_factor=
     return dict(neq=neq, eq=eq, loc=loc, rowptr=rowptr, colind=colind, val=val, b=b, x=x,
                 u=u_node, reac=reac, stress=sig, strain=eps, status=status, iters=iters,
                 achieved=ach)
+
+
+def check_convergence(rhs_node, RT_node, eq, enorm, rtolf, nite):
+    """NRSolver::checkConvergence with DOF grouping (nrsolver.C:593-790):
+    per DOF id, forceErr = sqrt(sum rhs^2 / (sum RT^2 + eNorm)) over free DOFs
+    (absolute when the denominator is below 1e-6); converged when every group is
+    <= rtolf, and never at iteration 0 with a non-zero error."""
+    ok = True
+    errs = []
+    for d in range(eq.shape[1]):
+        free = eq[:, d] > 0
+        if not free.any():
+            continue
+        fe = float((rhs_node[free, d] ** 2).sum())
+        den = float((RT_node[free, d] ** 2).sum()) + float(enorm[d])
+        err = np.sqrt(fe / den) if den >= 1e-6 else np.sqrt(fe)
+        errs.append(err)
+        if not np.isfinite(err) or err > rtolf * 1e20:
+            raise RuntimeError("NRSolver divergence")
+        if err > rtolf:
+            ok = False
+        if err > 0.0 and nite == 0:
+            ok = False
+    return ok, errs
+
+
+def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: int):
+    """NonLinearStatic (controlmode 1, no initial guess, tangent stiffness) with
+    NRSolver in full Newton mode (manrmsteps 1: tangent re-assembled every
+    iteration after the first, nrsolver.C:204-402). Prescribed values and loads
+    follow PiecewiseLinFunction t:[0, ramp_steps] -> f:[0, 1]. The linear systems
+    are solved directly (the reference decks use the default Skyline LDL^T).
+    Returns a list of per-step dicts (u, reactions, stresses, state, iterations)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    et = int(m["etype"])
+    bc_mask = np.asarray(m["bc_mask"])
+    neq, npeq, eq = number_equations(bc_mask)
+    loc = location_arrays(np.asarray(m["conn"]), eq)
+    rowptr, colind = build_pattern(neq, loc)
+    ne = np.asarray(m["conn"]).shape[0]
+    state = np.zeros((ne * ngp(et), NSTATE))
+    free = eq > 0
+    X = np.zeros(neq)
+    out = []
+    for t in times:
+        fac = float(t) / float(ramp_steps)
+        u_presc = np.where(bc_mask == 1, np.asarray(m["bc_value"]) * fac, 0.0)
+        RT_node = np.where(free, np.asarray(m["nodal_load"]) * fac, 0.0)
+        val = assemble_tangent(m, loc, neq, rowptr, colind, state)
+        nite = 0
+        while True:
+            u_node = u_presc.copy()
+            u_node[free] = X[eq[free] - 1]
+            F, sig, eps, en = internal_forces(m, u_node, state, want_enorm=True)
+            rhs = np.where(free, RT_node - F, 0.0)
+            conv, errs = check_convergence(rhs, RT_node, eq, en, rtolf, nite)
+            if conv:
+                break
+            if nite >= maxiter:
+                raise RuntimeError("NRSolver: maximum number of iterations reached")
+            if nite > 0:
+                val = assemble_tangent(m, loc, neq, rowptr, colind, state)
+            K = sp.csr_matrix((val, colind, rowptr), shape=(neq, neq))
+            b = np.zeros(neq)
+            b[eq[free] - 1] = rhs[free]
+            X += spla.spsolve(K.tocsc(), b)
+            nite += 1
+        commit_state(m, state)
+        reac = np.where(bc_mask == 1, F - np.asarray(m["nodal_load"]) * fac, 0.0)
+        out.append(dict(u=u_node, reac=reac, stress=sig, strain=eps, nite=nite, state=state.copy()))
+    return out

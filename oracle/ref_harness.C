@@ -3,7 +3,7 @@
 // Links against a build of the reference (liboofem) and runs an unchanged OOFEM
 // input deck, adding one export module, "refdump", that writes full-precision
 // (%.17g) per-step data the .out file only carries to 8 digits:
-//   step <n> <target time>
+//   step <n> <target time> <Newton iterations of the step>
 //   u <node> <dof> <eq> <value>             (eq: default numbering; 0 = prescribed)
 //   gp <elem> <gp> s <stress...> e <strain...> k <kappa> w <omega> le <Le>
 //   reac <node> <dof> <value>
@@ -58,7 +58,7 @@ public:
         }
         Domain *d = emodel->giveDomain(1);
         EModelDefaultEquationNumbering num;
-        fprintf(g_out, "step %d %.17g\n", tStep->giveNumber(), tStep->giveTargetTime());
+        fprintf(g_out, "step %d %.17g %d\n", tStep->giveNumber(), tStep->giveTargetTime(), tStep->numberOfIterations);
         for ( auto &node : d->giveDofManagers() ) {
             for ( Dof *dof : *node ) {
                 fprintf(g_out, "u %d %d %d %.17g\n", node->giveNumber(), ( int ) dof->giveDofID(),

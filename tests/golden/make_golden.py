@@ -49,7 +49,8 @@ def parse_dump(path):
             continue
         t = ln.split()
         if t[0] == "step":
-            cur = {"step": int(t[1]), "time": float(t[2]), "u": [], "gp": [], "reac": []}
+            cur = {"step": int(t[1]), "time": float(t[2]), "nite": int(t[3]) if len(t) > 3 else 0,
+                   "u": [], "gp": [], "reac": []}
             steps.append(cur)
         elif t[0] == "u":
             cur["u"].append((int(t[1]), int(t[2]), int(t[3]), float(t[4])))
@@ -109,10 +110,11 @@ def step_arrays(mesh: mg.Mesh, step: dict, prefix: str) -> dict:
         reac[node - 1, dof - 1] = v
     return {f"{prefix}u": u, f"{prefix}eq": eq, f"{prefix}stress": sig, f"{prefix}strain": eps,
             f"{prefix}kappa": kap, f"{prefix}omega": om, f"{prefix}le": le,
-            f"{prefix}reac": reac, f"{prefix}time": np.float64(step["time"])}
+            f"{prefix}reac": reac, f"{prefix}time": np.float64(step["time"]),
+            f"{prefix}nite": np.int32(step["nite"])}
 
 
-def run_case(name, mesh, work, analysis="LinearStatic nsteps 1", dumpK=True, **deck_kw):
+def run_case(name, mesh, work, analysis="LinearStatic nsteps 1", dumpK=True, extra=None, **deck_kw):
     deck = os.path.join(work, name + ".in")
     dump = os.path.join(work, name + ".dump")
     write_deck(mesh, deck, analysis, **deck_kw)
@@ -125,6 +127,8 @@ def run_case(name, mesh, work, analysis="LinearStatic nsteps 1", dumpK=True, **d
     steps, K, kes = parse_dump(dump)
     out = mesh_arrays(mesh)
     out["nsteps"] = np.int32(len(steps))
+    for k, v in (extra or {}).items():
+        out[k] = v
     for k, st in enumerate(steps):
         out.update(step_arrays(mesh, st, f"s{k + 1}_"))
     if K is not None:
@@ -169,6 +173,15 @@ def main():
     args = ap.parse_args()
     os.makedirs(args.work, exist_ok=True)
     patch300(args.ref_src)
+    def nonlinear(name, mesh, nsteps, rtolf=1e-8, maxiter=100):
+        analysis = (f"NonLinearStatic nsteps {nsteps} controlmode 1 rtolf {rtolf!r} maxiter {maxiter} "
+                    f"manrmsteps 1 stiffmode 0")
+        ramp = f"PiecewiseLinFunction 2 nPoints 2 t 2 0.0 {float(nsteps)!r} f(t) 2 0.0 1.0"
+        run_case(name, mesh, args.work, analysis=analysis, dumpK=False, bc_ltf=2, load_ltf=2,
+                 extra_funcs=(ramp,), extra=dict(rtolf=np.float64(rtolf), ramp_steps=np.int32(nsteps),
+                                                 maxiter=np.int32(maxiter)))
+
+    ey = 250e6 / 210e9
     cases = {
         "hex_cantilever_20x4x4": lambda: run_case(
             "hex_cantilever_20x4x4", mg.hex_cantilever(20, 4, 4), args.work),
@@ -178,6 +191,18 @@ def main():
             f"quad_rve_8_s3_lc{lc}", mg.quad_rve(8, seed=3, load_case=lc), args.work) for lc in range(3)],
         "tet_cube_3_jit": lambda: run_case(
             "tet_cube_3_jit", mg.tet_cube_linear(3, jitter=0.15, seed=5), args.work),
+        "mises_hex_4x2x2": lambda: nonlinear(
+            "mises_hex_4x2x2", mg.hex_block_pull(4, 2, 2, h=0.05, jitter=0.2, seed=3,
+                                                 material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6, H=2e9),
+                                                 end_disp=3 * ey * 0.2), 6),
+        "mises_hex_6x3x3": lambda: nonlinear(
+            "mises_hex_6x3x3", mg.hex_block_pull(6, 3, 3, h=0.05, jitter=0.2, seed=8,
+                                                 material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6, H=2e9),
+                                                 end_disp=4 * ey * 0.3), 8),
+        "idm1_tet_3": lambda: nonlinear(
+            "idm1_tet_3", mg.tet_cube(3, jitter=0.15, seed=5,
+                                      material=mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=1000.0),
+                                      end_disp=3e-4), 6, rtolf=1e-6, maxiter=400),
     }
     for name, fn in cases.items():
         if args.only and args.only not in name:

@@ -85,3 +85,32 @@ def test_pcg_matches_reference_iteration_count(oracle):
     assert r["achieved"] <= 1e-12
     tip = r["u"][20, 2]
     assert abs(tip - (-1.16468948e-03)) < 5e-11
+
+
+NONLINEAR_CASES = ["mises_hex_4x2x2", "mises_hex_6x3x3", "idm1_tet_3"]
+
+
+@pytest.mark.parametrize("case", NONLINEAR_CASES)
+def test_nonlinear_static_newton(case, oracle):
+    """NonLinearStatic + NRSolver (full Newton) with MisesMat (J2 radial return)
+    and IsotropicDamageMaterial1 (Mazars, exponential cohesive crack, crack
+    band) against the reference run step by step: same Newton iteration count,
+    same displacements, reactions, GP stresses, kappa and damage."""
+    g = load_golden(case)
+    ns = int(g["nsteps"])
+    times = [float(g[f"s{k}_time"]) for k in range(1, ns + 1)]
+    res = oracle.nonlinear_static(g, times, float(g["ramp_steps"]), float(g["rtolf"]), int(g["maxiter"]))
+    mises = "mises" in case
+    for k, r in enumerate(res, 1):
+        assert r["nite"] == int(g[f"s{k}_nite"])
+        assert rel(r["u"], g[f"s{k}_u"]) < 1e-9
+        assert rel(r["reac"], g[f"s{k}_reac"]) < 1e-9
+        assert rel(r["stress"], g[f"s{k}_stress"]) < 1e-9
+        kap = r["state"][:, 6] if mises else r["state"][:, 0]
+        assert rel(kap, g[f"s{k}_kappa"].ravel()) < 1e-9
+        if not mises:
+            assert rel(r["state"][:, 1], g[f"s{k}_omega"].ravel()) < 1e-9
+            le = g[f"s{k}_le"].ravel()
+            dam = le > 0
+            if dam.any():
+                assert rel(r["state"][dam, 2], le[dam]) < 1e-9
