@@ -211,6 +211,26 @@ OGB_API int ogb_model_commit_state(ogb_model *md);
 /* Per-GP state (nelem x ngp x 4): kappa, omega, Le, spare (committed). */
 OGB_API int ogb_model_gp_state(ogb_model *md, double *state4);
 
+/* Zero the Newton solution and the material state (a fresh analysis). */
+OGB_API int ogb_model_reset_state(ogb_model *md);
+/* One NonLinearStatic step with NRSolver in full Newton mode
+ * (NonLinearStatic::proceedStep nlinearstatic.C:453-565 with controlmode 1,
+ * stiffmode 0, no initial guess; NRSolver::solve nrsolver.C:204-402 with
+ * manrmsteps 1; NRSolver::checkConvergence nrsolver.C:593-790 with rtolf and DOF
+ * grouping). bc_value / nodal_load: this step's total prescribed values and
+ * nodal loads (nnodes x ndofpn). The model keeps the free-DOF solution between
+ * steps. The linear systems are solved by PCG to lin_rtol in `precision`. On
+ * success the material state is committed (MaterialStatus::updateYourself) and
+ * u_node / reactions (optional) receive the converged fields; *iterations is the
+ * Newton iteration count of the step. OGB_E_NOTCONV after maxiter iterations
+ * (the reference's ConvergenceException), the state then stays uncommitted. */
+OGB_API int ogb_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bc_value, const double *nodal_load,
+                               double rtolf, int maxiter, double lin_rtol, int precision, double *u_node,
+                               double *reactions, int *iterations);
+OGB_API int ogb_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bc_value_dev,
+                                   const double *nodal_load_dev, double rtolf, int maxiter, double lin_rtol,
+                                   int precision, double *u_node_dev, double *reactions_dev, int *iterations);
+
 /* LinearStatic::solveYourselfAt (linearstatic.C:177-253) in one call: build
  * the pattern (once), assemble K, load = f_ext - f_int(prescribed), PCG, node
  * displacements and reactions (structengngmodel.C:183-201). Host arrays:

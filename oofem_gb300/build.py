@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liboofem_gb300.so")
-SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu"]
+SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu", "newton.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]
@@ -36,7 +36,7 @@ def _stale(target: str, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "internal.cuh"),
+    headers = [os.path.join(CSRC, "internal.cuh"), os.path.join(CSRC, "reduce.cuh"),
                os.path.join(os.path.dirname(HERE), "include", "oofem_gb300.h")]
     cc = nvcc()
     jobs = []

@@ -816,6 +816,56 @@ int ogb_model_gp_state(ogb_model *md, double *state4)
     return OGB_OK;
 }
 
+static int nr_assemble(ogb_model *md, ogb_mtrx *m) { return assemble_stiffness_async(md, m); }
+static int nr_forces(ogb_model *md, const double *u, double *f) { return internal_forces_async(md, u, f); }
+static int nr_solve(ogb_mtrx *m, double rtol, int maxit, int precision, ogb_solve_info *info)
+{
+    return solve_padded(m, rtol, maxit, precision, info);
+}
+
+int ogb_model_reset_state(ogb_model *md)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    cudaStream_t s = md->ctx->stream;
+    if (md->nr_X.p) OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, md->nr_X.n * sizeof(double), s));
+    if (md->state.p) OGB_CUDA(cudaMemsetAsync(md->state.p, 0, md->state.n * sizeof(double), s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,
+                           int maxiter, double lin_rtol, int precision, double *u_node, double *reac, int *iterations)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
+    if (!md->inc.p)
+        OGB_CHECK(build_incidence(md->ctx, md->nnodes, md->nelem, md->nnpe, md->conn.p, md->inc_ptr, md->inc));
+    return nonlinear_step(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac, iterations, nullptr,
+                          nr_assemble, nr_forces, nr_solve);
+}
+
+int ogb_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf, int maxiter,
+                       double lin_rtol, int precision, double *u_node, double *reac, int *iterations)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    const size_t n = (size_t)md->nnodes * md->ndofpn;
+    cudaStream_t s = md->ctx->stream;
+    OGB_CHECK(md->v_bcval.alloc(n));
+    OGB_CHECK(md->v_load.alloc(n));
+    OGB_CHECK(md->v_unode.alloc(n));
+    OGB_CHECK(md->v_reac.alloc(n));
+    OGB_CUDA(cudaMemcpyAsync(md->v_bcval.p, bcval, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (load) OGB_CUDA(cudaMemcpyAsync(md->v_load.p, load, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int r = ogb_nonlinear_step_dev(md, m, md->v_bcval.p, load ? md->v_load.p : nullptr, rtolf, maxiter, lin_rtol,
+                                   precision, md->v_unode.p, reac ? md->v_reac.p : nullptr, iterations);
+    if (r != OGB_OK) return r;
+    OGB_CUDA(cudaMemcpyAsync(u_node, md->v_unode.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (reac) OGB_CUDA(cudaMemcpyAsync(reac, md->v_reac.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
 int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtol, int maxit,
                           int precision, double *u_node, double *reac, ogb_solve_info *info)
 {

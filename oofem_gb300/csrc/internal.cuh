@@ -231,6 +231,10 @@ struct ogb_model {
     ogb::DBuf<double> v_unode, v_fnode, v_bcval, v_load, v_b, v_x, v_reac;
     ogb_mtrx *bound = nullptr;
     bool nonlinear = false;
+    // Newton driver
+    ogb::DBuf<double> nr_X, nr_part, nr_out;
+    ogb::DBuf<unsigned int> nr_count;
+    ogb::HBuf<double> h_nr_out;
 };
 
 namespace ogb {
@@ -265,6 +269,13 @@ int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, og
 int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info);
 int extract_diag(ogb_mtrx *m);
 int pick_tpr(const ogb_mtrx *m);
+
+// newton.cu
+int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf, int maxiter,
+                   double lin_rtol, int precision, double *u_node, double *reac, int *iterations,
+                   ogb_solve_info *lin_info, int (*assemble)(ogb_model *, ogb_mtrx *),
+                   int (*forces)(ogb_model *, const double *, double *),
+                   int (*solve)(ogb_mtrx *, double, int, int, ogb_solve_info *));
 
 // helpers in capi.cu
 inline void count_launch(ogb_ctx *ctx, int n = 1) { ctx->launches += n; }

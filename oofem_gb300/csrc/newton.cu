@@ -1,0 +1,216 @@
+// Newton-Raphson step of NonLinearStatic on the GPU.
+//
+// Restates NRSolver::solve (src/core/nrsolver.C:204-402) for the setting
+// NonLinearStatic uses with `controlmode 1 manrmsteps 1` (full Newton, the
+// tangent assembled before the first residual and again in every later
+// iteration, no line search, no initial guess) and NRSolver::checkConvergence
+// with DOF grouping (nrsolver.C:593-790): per DOF id d,
+//   forceErr_d = sqrt( sum_free(d) rhs^2 / (sum_free(d) RT^2 + eNorm_d) ),
+// absolute when the denominator is below 1e-6; converged when every group is
+// <= rtolf, never at iteration 0 with a non-zero error. eNorm_d is the sum of
+// squared element internal-force entries with DOF id d (engngm.C:1398-1401).
+// Everything but the handful of group sums stays on the device; the host reads
+// 3*ndofpn doubles per iteration to take the convergence decision.
+#include <math.h>
+
+#include <vector>
+
+#include "internal.cuh"
+#include "reduce.cuh"
+
+namespace ogb {
+
+namespace {
+
+inline unsigned nblk(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
+constexpr int NR_GRID = NUM_SMS * 4;
+
+__global__ void k_nr_assemble_u(int n, const int *__restrict__ eq, const double *__restrict__ X,
+                                const double *__restrict__ bcval, double *__restrict__ u)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[i] = eq[i] > 0 ? X[eq[i] - 1] : bcval[i];
+}
+
+// rhs = RT - F at free DOFs (written to the equation-space vector b), and the
+// per-DOF-id sums of rhs^2 and RT^2 over free DOFs.
+template <int ND>
+__global__ void __launch_bounds__(NTHREADS) k_nr_rhs(int nnodes, const int *__restrict__ eq,
+                                                     const double *__restrict__ load, const double *__restrict__ fint,
+                                                     double *__restrict__ b, double *part, unsigned int *count,
+                                                     double *out)
+{
+    double v[2 * ND];
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k) v[k] = 0.0;
+    for (int A = blockIdx.x * blockDim.x + threadIdx.x; A < nnodes; A += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const int i = A * ND + d;
+            const int q = eq[i];
+            if (q > 0) {
+                const double rt = load ? load[i] : 0.0;
+                const double r = rt - fint[i];
+                b[q - 1] = r;
+                v[d] += r * r;
+                v[ND + d] += rt * rt;
+            }
+        }
+    }
+    block_sum<2 * ND>(v);
+    if (publish_partials<2 * ND>(v, part, count)) {
+        double t[2 * ND];
+        final_sums<2 * ND>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+#pragma unroll
+        for (int k = 0; k < 2 * ND; ++k) out[k] = t[k];
+    }
+}
+
+// eNorm_d = sum over all element force entries with DOF id d of fe^2.
+template <int ND>
+__global__ void __launch_bounds__(NTHREADS) k_nr_enorm(int64_t nentries, const double *__restrict__ fe, double *part,
+                                                       unsigned int *count, double *out)
+{
+    double v[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) v[d] = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nentries;
+         k += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double f = fe[k * ND + d];
+            v[d] += f * f;
+        }
+    }
+    block_sum<ND>(v);
+    if (publish_partials<ND>(v, part, count)) {
+        double t[ND];
+        final_sums<ND>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+#pragma unroll
+        for (int d = 0; d < ND; ++d) out[d] = t[d];
+    }
+}
+
+__global__ void k_nr_add(int n, double *__restrict__ X, const double *__restrict__ dX)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) X[i] += dX[i];
+}
+
+__global__ void k_nr_reactions(int n, const int *__restrict__ eq, const double *__restrict__ fint,
+                               const double *__restrict__ load, double *__restrict__ reac)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) reac[i] = eq[i] < 0 ? fint[i] - (load ? load[i] : 0.0) : 0.0;
+}
+
+}  // namespace
+
+int nr_ensure(ogb_model *md)
+{
+    if (!md->nr_X.p) {
+        OGB_CHECK(md->nr_X.alloc(md->neq > 0 ? md->neq : 1));
+        OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, (size_t)(md->neq > 0 ? md->neq : 1) * sizeof(double), md->ctx->stream));
+    }
+    OGB_CHECK(md->nr_part.alloc((size_t)8 * NR_GRID));
+    if (!md->nr_count.p) {
+        OGB_CHECK(md->nr_count.alloc(1));
+        OGB_CUDA(cudaMemsetAsync(md->nr_count.p, 0, sizeof(unsigned int), md->ctx->stream));
+    }
+    OGB_CHECK(md->nr_out.alloc(16));
+    OGB_CHECK(md->h_nr_out.alloc(16));
+    return OGB_OK;
+}
+
+// One NonLinearStatic step. bcval/load: this step's total prescribed values and
+// nodal loads (device, nnodes*ndofpn). On success the material state is
+// committed; u_node and reac (device, optional) receive the converged field.
+int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf, int maxiter,
+                   double lin_rtol, int precision, double *u_node, double *reac, int *iterations,
+                   ogb_solve_info *lin_info, int (*assemble)(ogb_model *, ogb_mtrx *),
+                   int (*forces)(ogb_model *, const double *, double *),
+                   int (*solve)(ogb_mtrx *, double, int, int, ogb_solve_info *))
+{
+    ogb_ctx *ctx = md->ctx;
+    cudaStream_t s = ctx->stream;
+    const int nd = md->ndofpn, nn = md->nnodes, n = nn * nd;
+    OGB_CHECK(nr_ensure(md));
+    OGB_CHECK(md->v_fnode.alloc(n));
+    OGB_CHECK(m->w_b.alloc(m->npad));
+    OGB_CHECK(m->w_x.alloc(m->npad));
+    // DOF groups in use (free DOFs per DOF id)
+    std::vector<int> nfree(nd, 0);
+    for (int i = 0; i < n; ++i)
+        if (md->h_eq[i] > 0) nfree[i % nd]++;
+    // tangent at the start of the step (temp state == committed state)
+    OGB_CHECK(assemble(md, m));
+    double *out = md->nr_out.p;
+    int nite = 0;
+    ogb_solve_info last{};
+    for (;;) {
+        k_nr_assemble_u<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->nr_X.p, bcval, u_node);
+        count_launch(ctx);
+        OGB_CHECK(forces(md, u_node, md->v_fnode.p));   // updates the temp material state
+        OGB_CUDA(cudaMemsetAsync(m->w_b.p, 0, (size_t)m->npad * sizeof(double), s));
+        if (nd == 3) {
+            k_nr_rhs<3><<<NR_GRID, NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
+                                                     md->nr_count.p, out);
+            k_nr_enorm<3><<<NR_GRID, NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
+                                                       md->nr_count.p, out + 6);
+        } else {
+            k_nr_rhs<2><<<NR_GRID, NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
+                                                     md->nr_count.p, out);
+            k_nr_enorm<2><<<NR_GRID, NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
+                                                       md->nr_count.p, out + 4);
+        }
+        count_launch(ctx, 2);
+        OGB_CUDA(cudaGetLastError());
+        OGB_CUDA(cudaMemcpyAsync(md->h_nr_out.p, out, 3 * nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+        OGB_CUDA(cudaStreamSynchronize(s));
+        OGB_CHECK(check_device_status(ctx, "nonlinear step"));
+        const double *h = md->h_nr_out.p;
+        bool converged = true;
+        for (int d = 0; d < nd; ++d) {
+            if (!nfree[d]) continue;
+            const double fe2 = h[d], rt2 = h[nd + d], en = h[2 * nd + d];
+            const double den = rt2 + en;
+            const double err = den >= 1e-6 ? sqrt(fe2 / den) : sqrt(fe2);
+            if (!isfinite(err) || err > rtolf * 1e20) {
+                if (iterations) *iterations = nite;
+                return fail(OGB_E_BREAKDOWN, "NRSolver divergence: residual out of range");
+            }
+            if (err > rtolf) converged = false;
+            if (err > 0.0 && nite == 0) converged = false;
+        }
+        if (converged) break;
+        if (nite >= maxiter) {
+            if (iterations) *iterations = nite;
+            return fail(OGB_E_NOTCONV, "NRSolver: maximum number of iterations reached without convergence");
+        }
+        if (nite > 0) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
+        OGB_CUDA(cudaMemsetAsync(m->w_x.p, 0, (size_t)m->npad * sizeof(double), s));
+        int r = solve(m, lin_rtol, 1000000, precision, &last);
+        if (r != OGB_OK) {
+            if (iterations) *iterations = nite;
+            return r;
+        }
+        k_nr_add<<<nblk(md->neq), NTHREADS, 0, s>>>(md->neq, md->nr_X.p, m->w_x.p);
+        count_launch(ctx);
+        ++nite;
+    }
+    OGB_CHECK(ogb_model_commit_state(md));
+    if (reac) {
+        k_nr_reactions<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->v_fnode.p, load, reac);
+        count_launch(ctx);
+    }
+    OGB_CUDA(cudaGetLastError());
+    if (iterations) *iterations = nite;
+    if (lin_info) *lin_info = last;
+    return OGB_OK;
+}
+
+}  // namespace ogb

@@ -33,6 +33,7 @@
 #include <math.h>
 
 #include "internal.cuh"
+#include "reduce.cuh"
 
 namespace ogb {
 
@@ -40,72 +41,6 @@ namespace {
 
 constexpr int GRID_MULT = 8;   // blocks per SM for the vector kernels
 constexpr double RELIABLE_DROP = 0.1;
-
-template <class T>
-__device__ __forceinline__ T warp_sum(T v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Fixed-order block reduction of NV values per thread; result valid in thread 0.
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV])
-{
-    __shared__ double red[NV][NTHREADS / 32];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        double s = warp_sum(v[k]);
-        if (lane == 0) red[k][warp] = s;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double s = 0;
-#pragma unroll
-            for (int w = 0; w < NTHREADS / 32; ++w) s += red[k][w];
-            v[k] = s;
-        }
-    }
-    __syncthreads();
-}
-
-// Publish this block's partials and report (to every thread of the block)
-// whether it was the last block of the grid to do so.
-template <int NV>
-__device__ __forceinline__ bool publish_partials(const double (&v)[NV], double *part, unsigned int *count)
-{
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) part[(size_t)k * gridDim.x + blockIdx.x] = v[k];
-        __threadfence();
-        unsigned int t = atomicAdd(count, 1u);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    return last;
-}
-
-// Run by every thread of the last block: thread t sums partials t, t+256, ...,
-// then the fixed-order block reduction; the result does not depend on which
-// block finished last. Valid in thread 0; only thread 0 writes the scalars.
-template <int NV>
-__device__ __forceinline__ void final_sums(const double *part, double (&out)[NV])
-{
-    __threadfence();
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        double s = 0;
-        const volatile double *pp = part + (size_t)k * gridDim.x;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += NTHREADS) s += pp[b];
-        out[k] = s;
-    }
-    block_sum<NV>(out);
-}
 
 __device__ __forceinline__ bool halted(const PcgScal *sc) { return sc->done || sc->reliable; }
 

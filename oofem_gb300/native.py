@@ -91,6 +91,9 @@ SIGNATURES = {
     "ogb_model_gp_stress": (_i, [_vp, _vp, _vp]),
     "ogb_model_commit_state": (_i, [_vp]),
     "ogb_model_gp_state": (_i, [_vp, _vp]),
+    "ogb_model_reset_state": (_i, [_vp]),
+    "ogb_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
+    "ogb_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_linear_static_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
 }
@@ -369,6 +372,23 @@ class GpuModel:
         if code not in SOLVER_STATUS:
             _check(code)
         return u, reac, info
+
+    def reset_state(self):
+        _check(self.lib.ogb_model_reset_state(self.h))
+
+    def nonlinear_step(self, A: GpuCsrMtrx, bc_value, nodal_load=None, rtolf=1e-8, maxiter=50,
+                       lin_rtol=1e-12, precision=PREC_FP64):
+        """One NonLinearStatic/NRSolver step; returns (u_node, reactions, newton_iterations)."""
+        bcv = np.ascontiguousarray(bc_value, dtype=np.float64)
+        ld = None if nodal_load is None else np.ascontiguousarray(nodal_load, dtype=np.float64)
+        u = np.zeros_like(bcv)
+        reac = np.zeros_like(bcv)
+        it = C.c_int(0)
+        code = self.lib.ogb_nonlinear_step(self.h, A.h, _ptr(bcv), _ptr(ld) if ld is not None else None,
+                                           rtolf, maxiter, lin_rtol, precision, _ptr(u), _ptr(reac),
+                                           C.byref(it))
+        _check(code)
+        return u, reac, it.value
 
     def close(self):
         if self.h:
