@@ -1,0 +1,40 @@
+"""The OOFEM-side binding (oofem_gb300/plugin/oofem_gb300_plugin.C) compiles
+against the reference's headers, links against a reference build, and takes
+over the class factory: the reference executable run on an unchanged deck with
+`smtype 11 lstype 9` constructs GpuCsrMtrx (without a GPU it then stops at
+context creation, which is what this CPU test checks). Skipped where no
+reference source tree and build are available."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+REF_SRC = os.environ.get("OOFEM_REF_SRC", "/root/reference")
+REF_BUILD = os.environ.get("OOFEM_REF_BUILD", "/tmp/oofem_probe")
+
+pytestmark = pytest.mark.skipif(
+    not (os.path.isdir(os.path.join(REF_SRC, "src")) and os.path.exists(os.path.join(REF_BUILD, "liboofem.so"))),
+    reason="needs the reference source tree and a reference build")
+
+
+def test_plugin_registers_through_the_class_factory(tmp_path, native_lib):
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from decks import write_deck
+    from oofem_gb300 import meshgen as mg
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "plugin", f"REF_SRC={REF_SRC}",
+                        f"REF_BUILD={REF_BUILD}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    deck = str(tmp_path / "gpu.in")
+    write_deck(mg.hex_cantilever(4, 2, 2), deck, "LinearStatic nsteps 1 smtype 11 lstype 9 lstol 1e-10 lsiter 1000")
+    text = open(deck).read().replace("nmodules 1", "nmodules 0").replace("refdump tstep_all\n", "")
+    open(deck, "w").write(text)
+    env = dict(os.environ)
+    env["LD_PRELOAD"] = os.path.join(ROOT, "oracle", "_ref", "liboofem_gb300_plugin.so")
+    env["LD_LIBRARY_PATH"] = REF_BUILD + ":" + os.path.join(ROOT, "oofem_gb300")
+    r = subprocess.run([os.path.join(REF_BUILD, "oofem"), "-f", deck], capture_output=True, text=True, env=env,
+                       cwd=str(tmp_path), timeout=120)
+    out = r.stdout + r.stderr
+    assert "GpuCsrMtrx" in out or "liboofem_gb300" in out, out[-2000:]
