@@ -244,6 +244,33 @@ OGB_API int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bc_v
                           int precision, double *u_node_dev, double *reactions_dev,
                           ogb_solve_info *info);
 
+/* ---- batches: independent meshes and load cases solved together ------------ */
+/* Declare the model's mesh to be ninst independent meshes (instances): instance
+ * i owns nodes node_start[i] .. node_start[i+1]-1, node_start[0] = 0,
+ * node_start[ninst] = nnodes, and every element's nodes lie in one instance
+ * (OGB_E_MESH otherwise). Call before the matrix is built; the equation
+ * numbering stays that of the concatenated mesh. No reference counterpart: an
+ * OOFEM run holds one domain, a batch of runs is a loop of separate runs. */
+OGB_API int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_start);
+/* LinearStatic for every instance and nrhs load cases (1..4) in one batched
+ * FP64 Jacobi-PCG: each (instance, load case) pair k = inst * nrhs + c runs its
+ * own CG with its own convergence test and stops when it converges, as a
+ * separate IMLSolver solve would (iml/cg.h:22-71). Replaces the loop of
+ * SparseLinearSystemNM::solve(A, B, X) (sparselinsystemnm.h:91, the column loop
+ * of sparselinsystemnm.C:47-69) and the loop over independent runs.
+ * bc_values / loads / u_nodes / reactions: nrhs consecutive nnodes x ndofpn
+ * vectors (loads and reactions optional). iterations, achieved (relative
+ * residual) and status (OGB_OK / OGB_E_NOTCONV / OGB_E_BREAKDOWN /
+ * OGB_E_ZERODIAG): ninst * nrhs entries, optional. Returns OGB_OK when every
+ * pair converged, else the first failing pair's status. */
+OGB_API int ogb_batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bc_values,
+                                    const double *loads, double rtol, int maxit, double *u_nodes,
+                                    double *reactions, int *iterations, double *achieved, int *status);
+/* Same with device-resident bc_values / loads / u_nodes / reactions. */
+OGB_API int ogb_batch_linear_static_dev(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bc_values_dev,
+                                        const double *loads_dev, double rtol, int maxit, double *u_nodes_dev,
+                                        double *reactions_dev, int *iterations, double *achieved, int *status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,16 +101,17 @@ __global__ void __launch_bounds__(NTHREADS) k_gather_nodes(int nnodes, int nnpe,
     for (int d = 0; d < ND; ++d) f[(size_t)A * ND + d] = s[d];
 }
 
-// Difference form of the FP32 SELL copy: the diagonal slot of every active row
-// receives the FP64 block row sum S_A = sum_B K_AB (see k_sell_spmv DIFF).
+// Difference form of the FP32 SELL copy: the diagonal slot of every row
+// receives the FP64 block row sum S_A = sum_B K_AB (see k_sell_spmv DIFF);
+// padding rows hold one identity block, whose row sum is itself.
 template <int ND>
-__global__ void __launch_bounds__(NTHREADS) k_sell_rowsum(int nact, const int64_t *__restrict__ sl_ptr,
+__global__ void __launch_bounds__(NTHREADS) k_sell_rowsum(int nrows, const int64_t *__restrict__ sl_ptr,
                                                           const int *__restrict__ sl_width,
                                                           const int64_t *__restrict__ diag,
                                                           const double *__restrict__ v64, float *__restrict__ v32)
 {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= nact) return;
+    if (a >= nrows) return;
     int s = a >> 5, r = a & 31;
     const double *vp = v64 + sl_ptr[s] * (ND * ND) + r;
     double S[ND * ND];
@@ -144,12 +145,13 @@ int launch_gather_matrix(ogb_model *md, ogb_mtrx *m)
                                                              md->ke.p, m->rowptr.p, m->val.p, bs, v64, v32);
     if (m->has_sell && ctx->mixed_diff) {
         const SellMat &S = m->sell;
-        unsigned nbr = (unsigned)ceil_div(S.nact > 0 ? S.nact : 1, NTHREADS);
+        const int nrows = S.nslices * 32;   // instances of a batch interleave active and padding rows
+        unsigned nbr = (unsigned)ceil_div(nrows, NTHREADS);
         if (S.nd == 3)
-            k_sell_rowsum<3><<<nbr, NTHREADS, 0, ctx->stream>>>(S.nact, S.sl_ptr.p, S.sl_width.p, S.diag.p, S.v64.p,
+            k_sell_rowsum<3><<<nbr, NTHREADS, 0, ctx->stream>>>(nrows, S.sl_ptr.p, S.sl_width.p, S.diag.p, S.v64.p,
                                                                 S.v32.p);
         else
-            k_sell_rowsum<2><<<nbr, NTHREADS, 0, ctx->stream>>>(S.nact, S.sl_ptr.p, S.sl_width.p, S.diag.p, S.v64.p,
+            k_sell_rowsum<2><<<nbr, NTHREADS, 0, ctx->stream>>>(nrows, S.sl_ptr.p, S.sl_width.p, S.diag.p, S.v64.p,
                                                                 S.v32.p);
         count_launch(ctx);
     }

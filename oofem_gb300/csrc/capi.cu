@@ -648,6 +648,7 @@ int ogb_model_create(ogb_ctx *ctx, int etype, int nnodes, const double *coords, 
     for (size_t k = 0; k < md->h_eq.size(); ++k) md->h_eq[k] = bc_mask[k] ? -(++npeq) : ++neq;
     md->neq = neq;
     md->npeq = npeq;
+    md->inst_start = {0, nnodes};
     std::vector<double> D((size_t)nmat * 36, 0.0);
     for (int i = 0; i < nmat; ++i) isotropic_D(etype, mats[8 * i + 1], mats[8 * i + 2], &D[(size_t)36 * i]);
     cudaStream_t s = ctx->stream;
@@ -864,6 +865,67 @@ int ogb_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const do
     if (reac) OGB_CUDA(cudaMemcpyAsync(reac, md->v_reac.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     OGB_CUDA(cudaStreamSynchronize(s));
     return OGB_OK;
+}
+
+int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_start)
+{
+    if (!md || !node_start || ninst < 1) return fail(OGB_E_ARG, "bad argument");
+    if (md->bound) return fail(OGB_E_STATE, "instances must be declared before the matrix is built");
+    if (node_start[0] != 0 || node_start[ninst] != md->nnodes)
+        return fail(OGB_E_ARG, "node_start must run from 0 to nnodes");
+    for (int i = 0; i < ninst; ++i)
+        if (node_start[i + 1] <= node_start[i]) return fail(OGB_E_ARG, "instances must be non-empty and ordered");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    std::vector<int> conn((size_t)md->nelem * md->nnpe);
+    OGB_CUDA(cudaMemcpy(conn.data(), md->conn.p, conn.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> inst_of(md->nnodes);
+    for (int i = 0; i < ninst; ++i)
+        for (int A = node_start[i]; A < node_start[i + 1]; ++A) inst_of[A] = i;
+    for (int e = 0; e < md->nelem; ++e) {
+        const int i0 = inst_of[conn[(size_t)e * md->nnpe]];
+        for (int a = 1; a < md->nnpe; ++a)
+            if (inst_of[conn[(size_t)e * md->nnpe + a]] != i0)
+                return fail(OGB_E_MESH, "element " + std::to_string(e) + " couples two instances");
+    }
+    md->inst_start.assign(node_start, node_start + ninst + 1);
+    return OGB_OK;
+}
+
+int ogb_batch_linear_static_dev(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load,
+                                double rtol, int maxit, double *u_nodes, double *reacs, int *iters, double *achieved,
+                                int *status)
+{
+    if (!md || !m || !bcval || !u_nodes) return fail(OGB_E_ARG, "null argument");
+    if (nrhs < 1 || nrhs > 4) return fail(OGB_E_ARG, "nrhs must be 1..4");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
+    return batch_linear_static(md, m, nrhs, bcval, load, rtol, maxit, u_nodes, reacs, iters, achieved, status,
+                               nr_assemble, nr_forces);
+}
+
+int ogb_batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load,
+                            double rtol, int maxit, double *u_nodes, double *reacs, int *iters, double *achieved,
+                            int *status)
+{
+    if (!md || !m || !bcval || !u_nodes) return fail(OGB_E_ARG, "null argument");
+    if (nrhs < 1 || nrhs > 4) return fail(OGB_E_ARG, "nrhs must be 1..4");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    const size_t n = (size_t)md->nnodes * md->ndofpn * nrhs;
+    cudaStream_t s = md->ctx->stream;
+    DBuf<double> d_bc, d_load, d_u, d_reac;
+    OGB_CHECK(d_bc.alloc(n));
+    OGB_CHECK(d_u.alloc(n));
+    if (load) OGB_CHECK(d_load.alloc(n));
+    if (reacs) OGB_CHECK(d_reac.alloc(n));
+    OGB_CUDA(cudaMemcpyAsync(d_bc.p, bcval, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (load) OGB_CUDA(cudaMemcpyAsync(d_load.p, load, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int r = ogb_batch_linear_static_dev(md, m, nrhs, d_bc.p, load ? d_load.p : nullptr, rtol, maxit, d_u.p,
+                                        reacs ? d_reac.p : nullptr, iters, achieved, status);
+    if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
+    OGB_CUDA(cudaMemcpyAsync(u_nodes, d_u.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (reacs) OGB_CUDA(cudaMemcpyAsync(reacs, d_reac.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return r;
 }
 
 int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtol, int maxit,

@@ -135,8 +135,13 @@ struct SellMat {
     DBuf<float> v32;
     int64_t v32_version = -1;
     DBuf<int> ns_of_eq;     // node-space index of equation e (0-based)
+    int ninst = 1;          // independent instances (block-diagonal batch)
+    std::vector<int64_t> inst_row_base;   // first node-space row of each instance (+ total)
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
+
+// Instances of a batch start on multiples of INST_ALIGN node-space rows.
+constexpr int INST_ALIGN = 1024;
 
 }  // namespace ogb
 
@@ -231,6 +236,7 @@ struct ogb_model {
     ogb::DBuf<double> v_unode, v_fnode, v_bcval, v_load, v_b, v_x, v_reac;
     ogb_mtrx *bound = nullptr;
     bool nonlinear = false;
+    std::vector<int> inst_start;   // first node of each instance (+ nnodes); {0, nnodes} for one mesh
     // Newton driver
     ogb::DBuf<double> nr_X, nr_part, nr_out;
     ogb::DBuf<unsigned int> nr_count;
@@ -276,6 +282,13 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
                    ogb_solve_info *lin_info, int (*assemble)(ogb_model *, ogb_mtrx *),
                    int (*forces)(ogb_model *, const double *, double *),
                    int (*solve)(ogb_mtrx *, double, int, int, ogb_solve_info *));
+
+// batch.cu
+int batch_pcg_fp64(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int *iters,
+                   double *achieved, int *status);
+int batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load, double rtol,
+                        int maxit, double *u_nodes, double *reacs, int *iters, double *achieved, int *status,
+                        int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *));
 
 // helpers in capi.cu
 inline void count_launch(ogb_ctx *ctx, int n = 1) { ctx->launches += n; }

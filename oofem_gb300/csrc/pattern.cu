@@ -11,6 +11,8 @@
 //   * location-array builder (drop-in SparseMtrx path): the same on equations.
 // No sort library and no floating-point atomics: counts use integer atomics,
 // lists are put in a canonical order by a per-segment insertion sort.
+#include <vector>
+
 #include "internal.cuh"
 
 namespace ogb {
@@ -562,12 +564,21 @@ __global__ void k_act_flags(int nnodes, int ndofpn, const int *eq, int64_t *flag
     flag[A] = A < nnodes ? (nfree_of(eq, ndofpn, A) > 0) : 0;
 }
 
-__global__ void k_act_index(int nnodes, int ndofpn, const int *eq, const int64_t *scan, int *act, int *rownode)
+// Node-space row of every active node: its rank among the active nodes of its
+// instance plus the instance's row base (instances start on 1024-row boundaries).
+__global__ void k_act_index(int nnodes, int ndofpn, const int *eq, const int64_t *scan, int ninst,
+                            const int *inst_start, const int64_t *inst_rank0, const int64_t *inst_base, int *act,
+                            int *rownode)
 {
     int A = blockIdx.x * blockDim.x + threadIdx.x;
     if (A >= nnodes) return;
     if (nfree_of(eq, ndofpn, A) > 0) {
-        int a = (int)scan[A];
+        int lo = 0, hi = ninst - 1;
+        while (lo < hi) {   // last instance whose first node is <= A
+            int mid = (lo + hi + 1) >> 1;
+            if (inst_start[mid] <= A) lo = mid; else hi = mid - 1;
+        }
+        int a = (int)(scan[A] - inst_rank0[lo] + inst_base[lo]);
         act[A] = a;
         rownode[a] = A;
     } else {
@@ -575,13 +586,14 @@ __global__ void k_act_index(int nnodes, int ndofpn, const int *eq, const int64_t
     }
 }
 
-// Width (active neighbours) of every row; padding rows get one (identity) block.
+// Width (active neighbours) of every row; padding rows (rownode < 0) get one
+// identity block.
 __global__ void k_row_width(int nrows_pad, int nact, const int *rownode, const int64_t *nb_ptr, const int *nb_col,
                             const int *act, int *width)
 {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nrows_pad) return;
-    if (a >= nact) {
+    if (rownode[a] < 0) {
         width[a] = 1;
         return;
     }
@@ -615,7 +627,7 @@ __global__ void k_fill_sell(int nrows_pad, int nact, const int *rownode, const i
     int64_t base = sl_ptr[s];
     int w = sl_width[s];
     int kk = 0;
-    if (a < nact) {
+    if (rownode[a] >= 0) {
         int A = rownode[a];
         for (int64_t k = nb_ptr[A]; k < nb_ptr[A + 1]; ++k) {
             int B = nb_col[k];
@@ -670,15 +682,38 @@ int build_sell(ogb_model *md, ogb_mtrx *m)
     int64_t nact = 0;
     OGB_CHECK(exclusive_scan_i64(ctx, flag.p, flag.p, nn + 1, &nact));
     S.nact = (int)nact;
-    int nslices = (int)ceil_div(nact > 0 ? nact : 1, 32);
-    nslices = (int)(ceil_div(nslices, 32) * 32);   // node-space length a multiple of CHUNK
+    // instances (independent meshes of a batch): each starts on a 1024-row boundary
+    // of node space, so every reduction unit of the solver belongs to one instance
+    const int ninst = (int)md->inst_start.size() - 1;
+    std::vector<int64_t> rank(nn + 1);
+    OGB_CUDA(cudaMemcpyAsync(rank.data(), flag.p, (nn + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    OGB_CUDA(cudaStreamSynchronize(st));
+    std::vector<int64_t> rank0(ninst), base(ninst + 1, 0);
+    S.inst_row_base.assign(ninst + 1, 0);
+    for (int i = 0; i < ninst; ++i) {
+        rank0[i] = rank[md->inst_start[i]];
+        int64_t na = rank[md->inst_start[i + 1]] - rank0[i];
+        base[i + 1] = base[i] + ceil_div(na > 0 ? na : 1, INST_ALIGN) * INST_ALIGN;
+    }
+    S.inst_row_base = base;
+    S.ninst = ninst;
+    const int nslices = (int)(base[ninst] / 32);
     S.nslices = nslices;
     const int nrows_pad = nslices * 32;
-    DBuf<int> rownode, width;
+    DBuf<int> rownode, width, d_start;
+    DBuf<int64_t> d_rank0, d_base;
     OGB_CHECK(md->act.alloc(nn));
     OGB_CHECK(rownode.alloc(nrows_pad));
     OGB_CHECK(width.alloc(nrows_pad));
-    k_act_index<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, flag.p, md->act.p, rownode.p);
+    OGB_CHECK(d_start.alloc(ninst + 1));
+    OGB_CHECK(d_rank0.alloc(ninst));
+    OGB_CHECK(d_base.alloc(ninst + 1));
+    OGB_CUDA(cudaMemcpyAsync(d_start.p, md->inst_start.data(), (ninst + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    OGB_CUDA(cudaMemcpyAsync(d_rank0.p, rank0.data(), ninst * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    OGB_CUDA(cudaMemcpyAsync(d_base.p, base.data(), (ninst + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    OGB_CUDA(cudaMemsetAsync(rownode.p, 0xff, nrows_pad * sizeof(int), st));   // -1: padding row
+    k_act_index<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, flag.p, ninst, d_start.p, d_rank0.p, d_base.p,
+                                               md->act.p, rownode.p);
     k_row_width<<<nblk(nrows_pad), NTHREADS, 0, st>>>(nrows_pad, S.nact, rownode.p, md->nb_ptr.p, md->nb_col.p,
                                                       md->act.p, width.p);
     OGB_CHECK(S.sl_ptr.alloc(nslices + 1));
@@ -707,7 +742,7 @@ int build_sell(ogb_model *md, ogb_mtrx *m)
     k_ns_of_eq<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, md->act.p, S.ns_of_eq.p);
     count_launch(ctx, 2);
     OGB_CUDA(cudaGetLastError());
-    OGB_CUDA(cudaStreamSynchronize(st));
+    OGB_CUDA(cudaStreamSynchronize(st));   // the temporaries above are freed on return
     S.v32_version = -1;
     m->has_sell = true;
     return OGB_OK;

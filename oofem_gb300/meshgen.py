@@ -244,6 +244,35 @@ def rve_bc_values(mesh: Mesh, load_case: int) -> np.ndarray:
     return vals
 
 
+def rve_batch(count: int, seed: int = 0, side_min: int = 32, side_max: int = 256,
+              vf: float = 0.30) -> List[Mesh]:
+    """``count`` RVEs (quad_rve) with sides n_i ~ U{side_min..side_max} drawn
+    from ``seed``; RVE i takes inclusion seed ``seed * 100003 + i``."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(side_min, side_max + 1, size=count)
+    return [quad_rve(int(n), seed=seed * 100003 + i, vf=vf) for i, n in enumerate(sides)]
+
+
+def concat_meshes(meshes: List[Mesh]):
+    """One mesh holding independent meshes back to back (nodes, elements and
+    material tables in order); returns (mesh, node_start) with node_start[i] the
+    first node of mesh i and node_start[-1] the node count."""
+    et = meshes[0].elem_type
+    if any(m.elem_type != et or m.thickness != meshes[0].thickness for m in meshes):
+        raise ValueError("instances must share element type and thickness")
+    node_start = np.zeros(len(meshes) + 1, np.int32)
+    node_start[1:] = np.cumsum([m.nnodes for m in meshes])
+    mat_off = np.cumsum([0] + [len(m.materials) for m in meshes])
+    conn = np.concatenate([m.conn + node_start[i] for i, m in enumerate(meshes)]).astype(np.int32)
+    emat = np.concatenate([m.elem_mat + mat_off[i] for i, m in enumerate(meshes)]).astype(np.int32)
+    mats = [mat for m in meshes for mat in m.materials]
+    big = Mesh(et, np.concatenate([m.coords for m in meshes]), conn, emat, mats,
+               np.concatenate([m.bc_mask for m in meshes]), np.concatenate([m.bc_value for m in meshes]),
+               np.concatenate([m.nodal_load for m in meshes]), thickness=meshes[0].thickness,
+               name=f"batch_{len(meshes)}")
+    return big, node_start
+
+
 def tet_det_ref(x: np.ndarray) -> np.ndarray:
     """detJ of FEI3dTetLin::evaldNdx (fei3dtetlin.C:140-142), x: (..., 4, 3)."""
     x1, x2, x3, x4 = x[..., 0, 0], x[..., 1, 0], x[..., 2, 0], x[..., 3, 0]

@@ -96,6 +96,9 @@ SIGNATURES = {
     "ogb_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_linear_static_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
+    "ogb_model_set_instances": (_i, [_vp, _i, _vp]),
+    "ogb_batch_linear_static": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _vp]),
+    "ogb_batch_linear_static_dev": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -372,6 +375,34 @@ class GpuModel:
         if code not in SOLVER_STATUS:
             _check(code)
         return u, reac, info
+
+    def set_instances(self, node_start):
+        """Declare the mesh as independent instances (node ranges); before build_matrix."""
+        ns = np.ascontiguousarray(node_start, dtype=np.int32)
+        self._ninst = len(ns) - 1
+        _check(self.lib.ogb_model_set_instances(self.h, self._ninst, _ptr(ns)))
+
+    def batch_linear_static(self, A: GpuCsrMtrx, bc_values, loads=None, rtol=1e-12, maxit=100000,
+                            want_reactions=True):
+        """LinearStatic of every instance and load case in one batched PCG.
+
+        bc_values / loads: (nrhs, nnodes, ndofpn). Returns (u, reactions, iterations,
+        achieved, status) with per-pair arrays of shape (ninst, nrhs)."""
+        bcv = np.ascontiguousarray(bc_values, dtype=np.float64)
+        nrhs = bcv.shape[0]
+        ld = None if loads is None else np.ascontiguousarray(loads, dtype=np.float64)
+        ninst = getattr(self, "_ninst", 1)
+        u = np.zeros_like(bcv)
+        reac = np.zeros_like(bcv) if want_reactions else None
+        its = np.zeros((ninst, nrhs), np.int32)
+        ach = np.zeros((ninst, nrhs))
+        st = np.zeros((ninst, nrhs), np.int32)
+        code = self.lib.ogb_batch_linear_static(self.h, A.h, nrhs, _ptr(bcv), _ptr(ld) if ld is not None else None,
+                                                rtol, maxit, _ptr(u), _ptr(reac) if reac is not None else None,
+                                                _ptr(its), _ptr(ach), _ptr(st))
+        if code not in SOLVER_STATUS:
+            _check(code)
+        return u, reac, its, ach, st
 
     def reset_state(self):
         _check(self.lib.ogb_model_reset_state(self.h))

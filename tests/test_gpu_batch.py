@@ -1,0 +1,113 @@
+"""Batched solves (independent meshes x load cases in one batched PCG) against
+the oracle's separate LinearStatic runs and against the single-mesh GPU path.
+
+Each (instance, load case) pair runs its own CG with its own convergence test,
+so its iteration count is that of a separate solve (within one or two
+iterations: the batched dot products sum in another order) and its
+displacements agree with the oracle's to the solve tolerance."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    s = np.abs(b).max()
+    return np.abs(a - b).max() / (s if s > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def ctx(native_lib):
+    return native_lib.Context(0)
+
+
+def _oracle_case(oracle, mesh, bc_value, load, rtol):
+    m = oracle.mesh_dict(mesh)
+    m["bc_value"] = bc_value
+    m["nodal_load"] = load
+    return oracle.linear_static(m, rtol=rtol)
+
+
+def test_rve_batch_three_load_cases(ctx, native_lib, oracle):
+    from oofem_gb300 import meshgen as mg
+    meshes = mg.rve_batch(5, seed=3, side_min=4, side_max=24)
+    meshes.append(mg.quad_rve(1, seed=7))            # no free DOF at all
+    meshes.insert(2, mg.quad_rve(37, seed=11))       # spans two 1024-row blocks
+    big, ns = mg.concat_meshes(meshes)
+    model = native_lib.GpuModel(ctx, big)
+    model.set_instances(ns)
+    A = native_lib.GpuCsrMtrx(ctx)
+    nrhs = 3
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(nrhs)])
+    rtol = 1e-13
+    u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=rtol)
+    assert (st == 0).all(), st
+    assert (ach <= rtol).all()
+    for i, m in enumerate(meshes):
+        sl = slice(ns[i], ns[i + 1])
+        for lc in range(nrhs):
+            ref = _oracle_case(oracle, m, mg.rve_bc_values(m, lc), np.zeros_like(m.bc_value), rtol)
+            assert ref["status"] == 0
+            assert abs(int(its[i, lc]) - ref["iters"]) <= 2, (i, lc, its[i, lc], ref["iters"])
+            assert rel(u[lc, sl], ref["u"]) < 1e-9, (i, lc)
+            assert rel(reac[lc, sl], ref["reac"]) < 1e-9, (i, lc)
+    assert (its[len(meshes) - 1] == 0).all()       # the all-prescribed RVE converges at once
+
+
+def test_hex_batch_two_rhs_matches_single_solves(ctx, native_lib):
+    """3-D path (3x3 node blocks): two jittered cantilevers of different size,
+    two load cases (the nodal load and a scaled, reversed one)."""
+    from oofem_gb300 import meshgen as mg
+    meshes = [mg.hex_cantilever(10, 3, 3, jitter=0.2, seed=1), mg.hex_cantilever(14, 4, 3, jitter=0.2, seed=2)]
+    big, ns = mg.concat_meshes(meshes)
+    model = native_lib.GpuModel(ctx, big)
+    model.set_instances(ns)
+    A = native_lib.GpuCsrMtrx(ctx)
+    loads = np.stack([big.nodal_load, -0.5 * big.nodal_load])
+    bcv = np.stack([big.bc_value, big.bc_value])
+    rtol = 1e-12
+    u, reac, its, ach, st = model.batch_linear_static(A, bcv, loads, rtol=rtol)
+    assert (st == 0).all()
+    for i, m in enumerate(meshes):
+        single = native_lib.GpuModel(ctx, m)
+        B = native_lib.GpuCsrMtrx(ctx)
+        for c, f in enumerate((1.0, -0.5)):
+            us, rs, info = single.linear_static(B, nodal_load=f * m.nodal_load, rtol=rtol)
+            assert info.status == 0
+            assert abs(int(its[i, c]) - info.iterations) <= 2
+            sl = slice(ns[i], ns[i + 1])
+            assert rel(u[c, sl], us) < 1e-9
+            assert rel(reac[c, sl], rs) < 1e-9
+    # linearity across the two load cases: u(-0.5 f) = -0.5 u(f) to the solve tolerance
+    assert rel(u[1], -0.5 * u[0]) < 1e-9
+
+
+def test_batch_is_deterministic(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    meshes = mg.rve_batch(4, seed=5, side_min=8, side_max=40)
+    big, ns = mg.concat_meshes(meshes)
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
+    out = []
+    for _ in range(2):
+        model = native_lib.GpuModel(ctx, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(ctx)
+        out.append(model.batch_linear_static(A, bcv, rtol=1e-10)[0])
+    assert np.array_equal(out[0], out[1])
+
+
+def test_set_instances_rejects_coupled_and_late(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    m = mg.quad_rve(6, seed=1)
+    model = native_lib.GpuModel(ctx, m)
+    with pytest.raises(native_lib.OgbError) as e:
+        model.set_instances([0, 20, m.nnodes])      # cuts through elements
+    assert e.value.code == -8
+    with pytest.raises(native_lib.OgbError) as e:
+        model.set_instances([0, m.nnodes + 1])
+    assert e.value.code == -1
+    A = native_lib.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    with pytest.raises(native_lib.OgbError) as e:
+        model.set_instances([0, m.nnodes])
+    assert e.value.code == -3
