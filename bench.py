@@ -11,6 +11,13 @@ scatter and reactions. value = free DOFs / step time (DOF/s).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 N > 1 runs independent replicas, one per GPU (the path has no exchange step).
+
+  python bench.py --workload rve_batch
+
+measures the batched solve instead: 256 PlaneStress2d RVEs (sides uniform in
+32..256 from seed 0, inclusions E = 300e9 at area fraction 0.3 in a matrix
+E = 30e9), three prescribed-strain load cases each, one batched FP64 PCG to
+1e-8 for all 768 (RVE, load case) pairs; value = free DOFs x load cases / step.
 """
 from __future__ import annotations
 
@@ -34,10 +41,8 @@ RTOL = 1e-8
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from oofem_gb300 import replicas
+    return replicas.env()
 
 
 class ClockSampler:
@@ -204,10 +209,8 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    from oofem_gb300 import replicas
+    barrier = replicas.barrier
 
     if args.nx:
         WORKLOAD.update(nx=args.nx, ny=args.ny, nz=args.nz)
@@ -270,12 +273,9 @@ def run_gpu(args):
     clk = clocks.stop()
     # FP64 drop-in path: iteration count and DOF/s for the mixed/FP64 ratio
     ms64, infos64, _, _ = timed(native.PREC_FP64, 1, 1)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * nfree / (ms * 1e-3)
+    # replicas: total free DOFs of all ranks over the slowest rank's step time
+    value = replicas.job_throughput(nfree, ms * 1e-3)
+    ms = replicas.max_over_ranks(ms)
 
     # end to end through the host API: mesh upload, pattern, assembly, solve, copy back
     def e2e_once():
@@ -297,6 +297,8 @@ def run_gpu(args):
             e2e_once()
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / n_e2e
+    if not args.no_e2e:
+        e2e_s = replicas.max_over_ranks(e2e_s)
     h2d = (mesh.coords.nbytes + mesh.conn.nbytes + mesh.elem_mat.nbytes + mesh.material_table().nbytes
            + mesh.bc_mask.nbytes + mesh.bc_value.nbytes + mesh.nodal_load.nbytes)
     d2h = 2 * mesh.bc_value.nbytes
@@ -342,6 +344,117 @@ def run_gpu(args):
     print(json.dumps(out))
 
 
+def run_gpu_batch(args):
+    """256-RVE sweep with three load cases per RVE through the batched solve."""
+    import ctypes as C
+    import torch
+    from oofem_gb300 import meshgen as mg, native
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nrve, nrhs = args.rve_count, 3
+    meshes = mg.rve_batch(nrve, seed=rank)
+    big, ns = mg.concat_meshes(meshes)
+    nfree = big.nfree
+    bcv_h = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(nrhs)])
+    ctx = native.Context(local)
+    model = native.GpuModel(ctx, big)
+    model.set_instances(ns)
+    A = native.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    lib = ctx.lib
+    bcv = torch.from_numpy(bcv_h.ravel()).to(dev)
+    u = torch.zeros_like(bcv)
+    reac = torch.zeros_like(bcv)
+    its = np.zeros(nrve * nrhs, np.int32)
+    ach = np.zeros(nrve * nrhs)
+    st = np.zeros(nrve * nrhs, np.int32)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def step(prec):
+        code = lib.ogb_batch_linear_static_dev(model.h, A.h, nrhs, C.c_void_p(bcv.data_ptr()), None, RTOL, 200000,
+                                               prec, C.c_void_p(u.data_ptr()), C.c_void_p(reac.data_ptr()),
+                                               its.ctypes.data_as(C.c_void_p), ach.ctypes.data_as(C.c_void_p),
+                                               st.ctypes.data_as(C.c_void_p))
+        if code != 0:
+            raise native.OgbError(code, lib.ogb_last_error().decode())
+
+    def timed(prec, k, w):
+        for _ in range(w):
+            step(prec)
+        torch.cuda.synchronize()
+        l0 = ctx.kernel_launches()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(k):
+                step(prec)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / k, (ctx.kernel_launches() - l0) / k, its.copy(), ach.copy(), st.copy()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, launches, its_m, ach_m, st_m = timed(native.PREC_MIXED, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms64, _, its64, ach64, st64 = timed(native.PREC_FP64, 1, 1)
+    value = nfree * nrhs / (ms * 1e-3)
+    # end to end through the host API (host arrays in and out, model upload included)
+    e2e_s = float("nan")
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        c2 = native.Context(local)
+        m2 = native.GpuModel(c2, big)
+        m2.set_instances(ns)
+        A2 = native.GpuCsrMtrx(c2)
+        m2.batch_linear_static(A2, bcv_h, rtol=RTOL, maxit=200000, precision=native.PREC_MIXED)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        A2.close()
+        m2.close()
+        c2.close()
+    h2d = (big.coords.nbytes + big.conn.nbytes + big.elem_mat.nbytes + big.material_table().nbytes
+           + big.bc_mask.nbytes + bcv_h.nbytes)
+    d2h = 2 * bcv_h.nbytes
+    cb = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        done_dofs = 0
+        k = 0
+        while k < nrve and (time.perf_counter() - t0) < 15.0:
+            md = O.mesh_dict(meshes[k])
+            for lc in range(nrhs):
+                md["bc_value"] = mg.rve_bc_values(meshes[k], lc)
+                O.linear_static(md, rtol=RTOL)
+            done_dofs += meshes[k].nfree * nrhs
+            k += 1
+        t_cpu = time.perf_counter() - t0
+        cb = {"value": done_dofs / t_cpu, "unit": "DOF/s", "cores": 1, "kind": "port",
+              "sample": f"oracle LinearStatic (serial C) on the first {k} RVEs of the batch x {nrhs} load cases"}
+    out = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "config": {"workload": f"rve_batch_{nrve}x{nrhs}rhs_sides32-256_seed{rank}", "rves": nrve,
+                   "load_cases": nrhs, "free_dofs": nfree, "elements": big.nelem, "nnz": A.nnz, "rtol": RTOL,
+                   "precision": "mixed FP32 batched PCG + FP64 residual replacement",
+                   "l2": "inputs larger than L2 (FP32 matrix %.2f GB)" % (A.nnz * 4.5 / 1e9)},
+        "solve": {"max_iterations": int(its_m.max()), "mean_iterations": float(its_m.mean()),
+                  "all_converged": bool((st_m == 0).all()), "max_achieved": float(ach_m.max())},
+        "fp64": {"value": nfree * nrhs / (ms64 * 1e-3), "ms_per_step": ms64, "max_iterations": int(its64.max()),
+                 "mean_iterations": float(its64.mean()), "all_converged": bool((st64 == 0).all())},
+        "mixed_over_fp64": ms64 / ms,
+        "clocks": clk, "gpu_launches": int(launches),
+        "e2e": {"value": nfree * nrhs / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "seconds": e2e_s},
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -353,11 +466,15 @@ def main():
     ap.add_argument("--nx", type=int, default=0, help="profiling only: smaller cantilever")
     ap.add_argument("--ny", type=int, default=0)
     ap.add_argument("--nz", type=int, default=0)
+    ap.add_argument("--workload", default="cantilever", choices=["cantilever", "rve_batch"])
+    ap.add_argument("--rve-count", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "rve_batch":
+        run_gpu_batch(args)
     else:
         run_gpu(args)
 

@@ -178,6 +178,19 @@ OGB_API int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr_dev, const int *c
                                   const double *b_dev, double *x_dev, double rtol, int maxit, void *stream,
                                   ogb_solve_info *info);
 
+/* SparseLinearSystemNM::solve(A, B, X) (sparselinsystemnm.h:91, default column
+ * loop sparselinsystemnm.C:47-69): nrhs right-hand sides at once. B and X are
+ * column-major neq x nrhs (FloatMatrix storage); X holds the initial guesses and
+ * receives the solutions. A matrix assembled from a model goes through the
+ * batched PCG (four columns per pass, the matrix streamed once for all of them);
+ * any other matrix runs the reference's column loop. iterations / achieved /
+ * status (optional): nrhs entries. Returns OGB_OK when every column converged,
+ * else the first failing column's status. */
+OGB_API int ogb_pcg_solve_multi(ogb_mtrx *m, int nrhs, const double *B, double *X, double rtol, int maxit,
+                                int precision, int *iterations, double *achieved, int *status);
+OGB_API int ogb_pcg_solve_multi_dev(ogb_mtrx *m, int nrhs, const double *B_dev, double *X_dev, double rtol,
+                                    int maxit, int precision, int *iterations, double *achieved, int *status);
+
 /* ---- element backend: LSpace / PlaneStress2d / LTRSpace element loops
  *      (NLStructuralElement::computeStiffnessMatrix nlstructuralelement.C:332-446,
  *      ::giveInternalForcesVector :151-240; EngngModel::assemble engngm.C:889-1037,
@@ -253,9 +266,12 @@ OGB_API int ogb_linear_static_dev(ogb_model *md, ogb_mtrx *m, const double *bc_v
  * OOFEM run holds one domain, a batch of runs is a loop of separate runs. */
 OGB_API int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_start);
 /* LinearStatic for every instance and nrhs load cases (1..4) in one batched
- * FP64 Jacobi-PCG: each (instance, load case) pair k = inst * nrhs + c runs its
- * own CG with its own convergence test and stops when it converges, as a
- * separate IMLSolver solve would (iml/cg.h:22-71). Replaces the loop of
+ * Jacobi-PCG: each (instance, load case) pair k = inst * nrhs + c runs its own
+ * CG with its own convergence test and stops when it converges. OGB_PREC_FP64:
+ * as a separate IMLSolver solve would (iml/cg.h:22-71); OGB_PREC_MIXED: FP32
+ * matrix and Krylov vectors, FP64 solution, convergence decided on the FP64
+ * residual ||b - K x|| / ||b|| <= rtol (periodic residual replacement).
+ * Replaces the loop of
  * SparseLinearSystemNM::solve(A, B, X) (sparselinsystemnm.h:91, the column loop
  * of sparselinsystemnm.C:47-69) and the loop over independent runs.
  * bc_values / loads / u_nodes / reactions: nrhs consecutive nnodes x ndofpn
@@ -264,12 +280,14 @@ OGB_API int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_st
  * OGB_E_ZERODIAG): ninst * nrhs entries, optional. Returns OGB_OK when every
  * pair converged, else the first failing pair's status. */
 OGB_API int ogb_batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bc_values,
-                                    const double *loads, double rtol, int maxit, double *u_nodes,
-                                    double *reactions, int *iterations, double *achieved, int *status);
+                                    const double *loads, double rtol, int maxit, int precision,
+                                    double *u_nodes, double *reactions, int *iterations, double *achieved,
+                                    int *status);
 /* Same with device-resident bc_values / loads / u_nodes / reactions. */
 OGB_API int ogb_batch_linear_static_dev(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bc_values_dev,
-                                        const double *loads_dev, double rtol, int maxit, double *u_nodes_dev,
-                                        double *reactions_dev, int *iterations, double *achieved, int *status);
+                                        const double *loads_dev, double rtol, int maxit, int precision,
+                                        double *u_nodes_dev, double *reactions_dev, int *iterations,
+                                        double *achieved, int *status);
 
 #ifdef __cplusplus
 }

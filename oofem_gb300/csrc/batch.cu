@@ -18,6 +18,7 @@
 // atomics), and the per-instance epilogues run in parallel across the grid.
 #include <math.h>
 
+#include <functional>
 #include <vector>
 
 #include "internal.cuh"
@@ -29,21 +30,24 @@ namespace {
 
 struct BatchScal {
     double bnorm2, rho, pq, rnorm2, alpha, beta;
-    int done, iters;   // done: 0 running, 1 converged, 2 breakdown, 3 zero pivot, 4 iteration limit
+    int done;    // 0 running, 1 converged, 2 breakdown, 3 zero pivot, 4 iteration limit
+    int iters;
+    int pause;   // mixed precision: waits for the next FP64 residual replacement
+    int pad_;
 };
 
 constexpr int UNIT = NTHREADS;               // scalar rows per vector block
 constexpr int SPMV_SLICES = NTHREADS / 32;   // slices (of 32 node rows) per SpMV block
 constexpr int MAXNR = 4;
 constexpr int BBATCH = 16;                   // iterations per captured graph
+constexpr int REPLACE_EVERY = 64;            // mixed precision: FP64 residual replacement period
 
-// Block sums of NV values, published for block `unit`; true in every thread of
-// the block that completed its instance (count reaches the instance's units).
+// Publish the block sums v (valid in thread 0) for block `unit`; true in every
+// thread of the block that completed its instance (count reaches its units).
 template <int NV>
-__device__ __forceinline__ bool publish_inst(double (&v)[NV], double *part, int64_t unit, unsigned int *cnt,
+__device__ __forceinline__ bool publish_inst(const double (&v)[NV], double *part, int64_t unit, unsigned int *cnt,
                                              int64_t inst_units)
 {
-    block_sum<NV>(v);
     __shared__ bool s_last;
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -70,59 +74,108 @@ __device__ __forceinline__ void inst_sums(const double *part, int64_t u0, int64_
     block_sum<NV>(out);
 }
 
-// q = K p for all right-hand sides; with DOT, also p.q per pair and alpha.
-template <int ND, int NR, bool DOT>
+// Instance skip test (the same for every block of the instance within one
+// launch). mode 1: no pair of the instance is running (all converged, failed or
+// waiting for a residual replacement); mode 2: every pair is finished.
+template <int NR>
+__device__ __forceinline__ bool inst_skip(const BatchScal *sc, int inst, int mode)
+{
+    bool all = true;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        const BatchScal &q = sc[inst * NR + c];
+        all = all && (q.done != 0 || (mode == 1 && q.pause != 0));
+    }
+    return all;
+}
+template <int NR>
+__device__ __forceinline__ bool pair_running(const BatchScal &q)
+{
+    return q.done == 0 && q.pause == 0;
+}
+
+// q = K p for all right-hand sides: matrix values V, vectors X, products and
+// sums in V. DOT: also p.q per pair (block sums in V per warp, FP64 above) and
+// alpha for running pairs. DIFF: the FP32 difference form (the diagonal slot
+// holds the block row sum, off-diagonal products act on x_B - x_A). skip: the
+// inst_skip mode (0 = never). Block columns are prefetched one group ahead.
+template <int ND, int NR, bool DOT, class V, class X, bool DIFF>
 __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *__restrict__ sl_ptr,
                                                     const int *__restrict__ sl_width, const int *__restrict__ col,
-                                                    const double *__restrict__ val, const double *__restrict__ x,
-                                                    double *__restrict__ y, double *part, unsigned int *cnt,
+                                                    const V *__restrict__ val, const X *__restrict__ x,
+                                                    X *__restrict__ y, double *part, unsigned int *cnt,
                                                     BatchScal *sc, const int *__restrict__ unit_inst,
-                                                    const int64_t *__restrict__ unit_ptr)
+                                                    const int64_t *__restrict__ unit_ptr, int skip)
 {
+    if (skip && inst_skip<NR>(sc, unit_inst[blockIdx.x], skip)) return;
+    constexpr int W = ND * NR;               // vector entries per node row
+    constexpr int G = W <= 6 ? 4 : 2;        // blocks per prefetch group
     const int s = blockIdx.x * SPMV_SLICES + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
-    double acc[NR];
+    V dot[NR];
 #pragma unroll
-    for (int c = 0; c < NR; ++c) acc[c] = 0.0;
+    for (int c = 0; c < NR; ++c) dot[c] = 0;
     if (s < nslices) {
         const int64_t base = sl_ptr[s];
         const int w = sl_width[s];
-        double yy[ND][NR];
+        const int arow = s * 32 + r;
+        V yy[ND][NR], xa[W];
 #pragma unroll
         for (int i = 0; i < ND; ++i)
 #pragma unroll
-            for (int c = 0; c < NR; ++c) yy[i][c] = 0.0;
-        const double *vp = val + base * (ND * ND) + r;
+            for (int c = 0; c < NR; ++c) yy[i][c] = 0;
+#pragma unroll
+        for (int j = 0; j < W; ++j) xa[j] = DIFF ? (V)x[(int64_t)arow * W + j] : (V)0;
+        const V *vp = val + base * (ND * ND) + r;
         const int *cp = col + base + r;
-        for (int k = 0; k < w; ++k) {
-            const int cc = __ldcs(cp + 32 * k);
-            double xb[ND * NR];
-            const double *xp = x + (int64_t)cc * (ND * NR);
+        int cn[G];
 #pragma unroll
-            for (int j = 0; j < ND * NR; ++j) xb[j] = __ldg(xp + j);
-            const double *vk = vp + (int64_t)k * (32 * ND * ND);
+        for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
+        for (int k0 = 0; k0 < w; k0 += G) {
+            int cc[G];
 #pragma unroll
-            for (int i = 0; i < ND; ++i)
+            for (int g = 0; g < G; ++g) {
+                cc[g] = cn[g];
+                cn[g] = k0 + G + g < w ? __ldcs(cp + 32 * (k0 + G + g)) : arow;
+            }
+            V xb[G][W];
 #pragma unroll
-                for (int j = 0; j < ND; ++j) {
-                    const double v = __ldcs(vk + 32 * (i * ND + j));
+            for (int g = 0; g < G; ++g)
 #pragma unroll
-                    for (int c = 0; c < NR; ++c) yy[i][c] = fma(v, xb[j * NR + c], yy[i][c]);
+                for (int j = 0; j < W; ++j) {
+                    xb[g][j] = (V)__ldg(x + (int64_t)cc[g] * W + j);
+                    if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
                 }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (k0 + g < w) {
+                    const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                    for (int i = 0; i < ND; ++i)
+#pragma unroll
+                        for (int j = 0; j < ND; ++j) {
+                            const V v = __ldcs(vk + 32 * (i * ND + j));
+#pragma unroll
+                            for (int c = 0; c < NR; ++c) yy[i][c] = fma(v, xb[g][j * NR + c], yy[i][c]);
+                        }
+                }
+            }
         }
         const int64_t a = (int64_t)s * 32 + r;
 #pragma unroll
         for (int i = 0; i < ND; ++i)
 #pragma unroll
             for (int c = 0; c < NR; ++c) {
-                y[(a * ND + i) * NR + c] = yy[i][c];
-                if (DOT) acc[c] = fma(x[(a * ND + i) * NR + c], yy[i][c], acc[c]);
+                y[(a * ND + i) * NR + c] = (X)yy[i][c];
+                if (DOT) dot[c] = fma((V)x[(a * ND + i) * NR + c], yy[i][c], dot[c]);
             }
     }
     if (!DOT) return;
     const int inst = unit_inst[blockIdx.x];
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
-    if (!publish_inst<NR>(acc, part, blockIdx.x, cnt + inst, u1 - u0)) return;
+    double bs[NR];
+    block_sum_t<NR, V>(dot, bs);
+    if (!publish_inst<NR>(bs, part, blockIdx.x, cnt + inst, u1 - u0)) return;
     double t[NR];
     inst_sums<NR>(part, u0, u1, t);
     if (threadIdx.x != 0) return;
@@ -130,7 +183,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         BatchScal &q = sc[inst * NR + c];
-        if (q.done) continue;
+        if (!pair_running<NR>(q)) continue;
         q.pq = t[c];
         if (!(t[c] > 0.0) || !isfinite(t[c])) q.done = 2;
         else q.alpha = q.rho / t[c];
@@ -164,6 +217,7 @@ __global__ void __launch_bounds__(NTHREADS) k_binit(const double *__restrict__ b
     }
     const int inst = unit_inst[blockIdx.x];
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
+    block_sum<3 * NR>(v);
     if (!publish_inst<3 * NR>(v, part, blockIdx.x, cnt + inst, u1 - u0)) return;
     double t[3 * NR];
     inst_sums<3 * NR>(part, u0, u1, t);
@@ -195,8 +249,9 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate(double *__restrict__ x, do
                                                       const int *__restrict__ unit_inst,
                                                       const int64_t *__restrict__ unit_ptr, double rtol, int maxit)
 {
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
     const int inst = unit_inst[blockIdx.x];
+    if (inst_skip<NR>(sc, inst, 1)) return;
+    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
     const double di = dinv[row];
     double v[2 * NR];
 #pragma unroll
@@ -216,6 +271,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate(double *__restrict__ x, do
         v[NR + c] = rr * zz;
     }
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
+    block_sum<2 * NR>(v);
     if (!publish_inst<2 * NR>(v, part, blockIdx.x, cnt + inst, u1 - u0)) return;
     double t[2 * NR];
     inst_sums<2 * NR>(part, u0, u1, t);
@@ -243,8 +299,9 @@ template <int NR>
 __global__ void __launch_bounds__(NTHREADS) k_bpupdate(const double *__restrict__ z, double *__restrict__ p,
                                                        const BatchScal *sc, const int *__restrict__ unit_inst)
 {
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
     const int inst = unit_inst[blockIdx.x];
+    if (inst_skip<NR>(sc, inst, 1)) return;
+    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         const int done = sc[inst * NR + c].done;
@@ -255,10 +312,11 @@ __global__ void __launch_bounds__(NTHREADS) k_bpupdate(const double *__restrict_
     }
 }
 
-// Inverse of the point diagonal of every node row (padding rows hold identity).
-template <int ND>
+// Inverse of the point diagonal of every node row (padding rows hold identity),
+// from the FP64 values, stored as T.
+template <int ND, class T>
 __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const double *__restrict__ val,
-                        double *__restrict__ dinv, int *zero_diag)
+                        T *__restrict__ dinv, int *zero_diag)
 {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nrows) return;
@@ -270,10 +328,156 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
         const double v = vb[32 * (d * ND + d)];
         if (v == 0.0) {
             atomicExch(zero_diag, 1);
-            dinv[(int64_t)a * ND + d] = 0.0;
+            dinv[(int64_t)a * ND + d] = 0;
         } else {
-            dinv[(int64_t)a * ND + d] = 1.0 / v;
+            dinv[(int64_t)a * ND + d] = (T)(1.0 / v);
         }
+    }
+}
+
+// ---- mixed precision: FP32 matrix (difference form) and FP32 r, z, p, q per
+// pair, FP64 solution x. Every REPLACE_EVERY iterations, and whenever no pair is
+// running, the true residual b - K64 x is formed in FP64 for every unfinished
+// pair; convergence is decided on it only. A pair whose recursive residual
+// reaches half the tolerance (or the iteration limit) pauses until then; a
+// paused pair that is not converged restarts its search direction from the
+// replaced residual, a running pair keeps it.
+
+// Residual replacement (init: the first one, which also sets ||b|| and p = z).
+template <int NR>
+__global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict__ b, const double *__restrict__ q64,
+                                                       const float *__restrict__ dinv, float *__restrict__ r,
+                                                       float *__restrict__ z, float *__restrict__ p, double *part,
+                                                       unsigned int *cnt, BatchScal *sc,
+                                                       const int *__restrict__ unit_inst,
+                                                       const int64_t *__restrict__ unit_ptr, double rtol, int maxit,
+                                                       int init)
+{
+    const int inst = unit_inst[blockIdx.x];
+    if (inst_skip<NR>(sc, inst, 2)) return;
+    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
+    const float di = dinv[row];
+    double v[3 * NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        v[c] = 0.0;
+        v[NR + c] = 0.0;
+        v[2 * NR + c] = 0.0;
+        const BatchScal &s = sc[inst * NR + c];
+        if (s.done) continue;
+        const int64_t k = row * NR + c;
+        const double bb = b[k];
+        const double r6 = bb - q64[k];
+        const float rf = (float)r6;
+        const float zf = rf * di;
+        r[k] = rf;
+        z[k] = zf;
+        if (init || s.pause) p[k] = zf;
+        v[c] = bb * bb;
+        v[NR + c] = r6 * r6;
+        v[2 * NR + c] = (double)(rf * zf);
+    }
+    const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
+    block_sum<3 * NR>(v);
+    if (!publish_inst<3 * NR>(v, part, blockIdx.x, cnt + inst, u1 - u0)) return;
+    double t[3 * NR];
+    inst_sums<3 * NR>(part, u0, u1, t);
+    if (threadIdx.x != 0) return;
+    cnt[inst] = 0;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        BatchScal &s = sc[inst * NR + c];
+        if (s.done) continue;
+        if (init) {
+            s.bnorm2 = t[c];
+            s.iters = 0;
+        }
+        double normb = sqrt(s.bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        s.rnorm2 = t[NR + c];
+        const double rz = t[2 * NR + c];
+        if (sqrt(t[NR + c]) / normb <= rtol) s.done = 1;
+        else if (!isfinite(t[NR + c]) || !isfinite(rz) || !(rz > 0.0)) s.done = 2;
+        else if (s.iters >= maxit) s.done = 4;
+        else {
+            s.rho = rz;
+            s.pause = 0;
+        }
+    }
+}
+
+// x64 += alpha p, r -= alpha q, z = D^-1 r for running pairs (FP32 but x);
+// per pair ||r||^2 and r.z (FP32 per thread and warp, FP64 above), the pause
+// test and beta.
+template <int NR>
+__global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, float *__restrict__ r,
+                                                        float *__restrict__ z, const float *__restrict__ p,
+                                                        const float *__restrict__ q, const float *__restrict__ dinv,
+                                                        double *part, unsigned int *cnt, BatchScal *sc,
+                                                        const int *__restrict__ unit_inst,
+                                                        const int64_t *__restrict__ unit_ptr, double rtol, int maxit)
+{
+    const int inst = unit_inst[blockIdx.x];
+    if (inst_skip<NR>(sc, inst, 1)) return;
+    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
+    const float di = dinv[row];
+    float v[2 * NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        v[c] = 0.f;
+        v[NR + c] = 0.f;
+        const BatchScal &s = sc[inst * NR + c];
+        if (!pair_running<NR>(s)) continue;
+        const double alpha = s.alpha;
+        const int64_t k = row * NR + c;
+        const float pp = p[k];
+        x[k] = fma(alpha, (double)pp, x[k]);
+        const float rr = fmaf(-(float)alpha, q[k], r[k]);
+        const float zz = rr * di;
+        r[k] = rr;
+        z[k] = zz;
+        v[c] = rr * rr;
+        v[NR + c] = rr * zz;
+    }
+    const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
+    double bs[2 * NR];
+    block_sum_t<2 * NR, float>(v, bs);
+    if (!publish_inst<2 * NR>(bs, part, blockIdx.x, cnt + inst, u1 - u0)) return;
+    double t[2 * NR];
+    inst_sums<2 * NR>(part, u0, u1, t);
+    if (threadIdx.x != 0) return;
+    cnt[inst] = 0;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        BatchScal &s = sc[inst * NR + c];
+        if (!pair_running<NR>(s)) continue;
+        s.rnorm2 = t[c];
+        s.iters += 1;
+        double normb = sqrt(s.bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        const double half = 0.5 * rtol * normb;
+        if (!isfinite(t[c]) || !isfinite(t[NR + c])) s.done = 2;
+        else if (t[c] <= half * half || !(t[NR + c] > 0.0) || s.iters >= maxit) s.pause = 1;
+        else {
+            s.beta = t[NR + c] / s.rho;
+            s.rho = t[NR + c];
+        }
+    }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(NTHREADS) k_bpupdate32(const float *__restrict__ z, float *__restrict__ p,
+                                                         const BatchScal *sc, const int *__restrict__ unit_inst)
+{
+    const int inst = unit_inst[blockIdx.x];
+    if (inst_skip<NR>(sc, inst, 1)) return;
+    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        const BatchScal &s = sc[inst * NR + c];
+        if (!pair_running<NR>(s)) continue;
+        const int64_t k = row * NR + c;
+        p[k] = fmaf((float)s.beta, p[k], z[k]);
     }
 }
 
@@ -281,12 +485,40 @@ struct BatchWork {
     DBuf<int> vinst, sinst, zero;
     DBuf<int64_t> vptr, sptr;
     DBuf<BatchScal> sc;
-    DBuf<double> part, r, z, p, q, dinv;
+    DBuf<double> part, r, z, p, q, dinv, q64;
+    DBuf<float> r32, z32, p32, q32, dinv32;
     DBuf<unsigned int> cnt;
 };
 
+// Captures `iteration` BBATCH times into an executable graph (exec stays null
+// when graphs are off).
+template <class F>
+int capture_batch(ogb_ctx *ctx, F &&iteration, cudaGraphExec_t &exec)
+{
+    exec = nullptr;
+    if (!ctx->use_graphs) return OGB_OK;
+    cudaGraph_t g = nullptr;
+    OGB_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < BBATCH; ++k) iteration();
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return OGB_OK;
+}
+
+struct ExecGuard {
+    cudaGraphExec_t e = nullptr;
+    ~ExecGuard()
+    {
+        if (e) cudaGraphExecDestroy(e);
+    }
+};
+
 template <int ND, int NR>
-int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, std::vector<BatchScal> &res)
+int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, bool mixed,
+              std::vector<BatchScal> &res)
 {
     ogb_ctx *ctx = m->ctx;
     cudaStream_t st = ctx->stream;
@@ -314,12 +546,21 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, s
     OGB_CHECK(w.sc.alloc(npair));
     OGB_CHECK(w.zero.alloc(1));
     OGB_CHECK(w.part.alloc((size_t)nvu * 3 * NR));
-    OGB_CHECK(w.r.alloc(nv));
-    OGB_CHECK(w.z.alloc(nv));
-    OGB_CHECK(w.p.alloc(nv));
-    OGB_CHECK(w.q.alloc(nv));
-    OGB_CHECK(w.dinv.alloc(nrows));
     OGB_CHECK(w.cnt.alloc(ninst));
+    if (mixed) {
+        OGB_CHECK(w.r32.alloc(nv));
+        OGB_CHECK(w.z32.alloc(nv));
+        OGB_CHECK(w.p32.alloc(nv));
+        OGB_CHECK(w.q32.alloc(nv));
+        OGB_CHECK(w.dinv32.alloc(nrows));
+        OGB_CHECK(w.q64.alloc(nv));
+    } else {
+        OGB_CHECK(w.r.alloc(nv));
+        OGB_CHECK(w.z.alloc(nv));
+        OGB_CHECK(w.p.alloc(nv));
+        OGB_CHECK(w.q.alloc(nv));
+        OGB_CHECK(w.dinv.alloc(nrows));
+    }
     OGB_CUDA(cudaMemcpyAsync(w.vinst.p, vinst.data(), nvu * sizeof(int), cudaMemcpyHostToDevice, st));
     OGB_CUDA(cudaMemcpyAsync(w.sinst.p, sinst.data(), nsu * sizeof(int), cudaMemcpyHostToDevice, st));
     OGB_CUDA(cudaMemcpyAsync(w.vptr.p, vptr.data(), (ninst + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
@@ -328,59 +569,86 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, s
     OGB_CUDA(cudaMemsetAsync(w.zero.p, 0, sizeof(int), st));
     OGB_CUDA(cudaMemsetAsync(w.cnt.p, 0, ninst * sizeof(unsigned int), st));
     const int nr = S.nslices * 32;
-    k_bdiag<ND><<<(unsigned)ceil_div(nr, NTHREADS), NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
-    k_bspmv<ND, NR, false><<<nsu, NTHREADS, 0, st>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v64.p, x, w.q.p,
-                                                     nullptr, nullptr, nullptr, nullptr, nullptr);
-    k_binit<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q.p, w.dinv.p, w.r.p, w.z.p, w.p.p, w.part.p, w.cnt.p, w.sc.p,
-                                          w.vinst.p, w.vptr.p, rtol);
+    const unsigned gd = (unsigned)ceil_div(nr, NTHREADS);
+    // FP64 K x for every unfinished pair (the initial residual; the replacements)
+    auto residual_spmv = [&](double *q64) {
+        k_bspmv<ND, NR, false, double, double, false><<<nsu, NTHREADS, 0, st>>>(
+            S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v64.p, x, q64, nullptr, nullptr, w.sc.p, w.sinst.p,
+            w.sptr.p, 2);
+    };
+    std::function<void()> iteration;
+    if (mixed) {
+        k_bdiag<ND, float><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv32.p, w.zero.p);
+        residual_spmv(w.q64.p);
+        k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.p32.p, w.part.p, w.cnt.p,
+                                                 w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 1);
+        const bool diff = ctx->mixed_diff;
+        iteration = [&, diff]() {
+            if (diff)
+                k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(
+                    S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
+                    w.sinst.p, w.sptr.p, 1);
+            else
+                k_bspmv<ND, NR, true, float, float, false><<<nsu, NTHREADS, 0, st>>>(
+                    S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
+                    w.sinst.p, w.sptr.p, 1);
+            k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
+                                                      w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit);
+            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p);
+        };
+    } else {
+        k_bdiag<ND, double><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
+        residual_spmv(w.q.p);
+        k_binit<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q.p, w.dinv.p, w.r.p, w.z.p, w.p.p, w.part.p, w.cnt.p, w.sc.p,
+                                              w.vinst.p, w.vptr.p, rtol);
+        iteration = [&]() {
+            k_bspmv<ND, NR, true, double, double, false><<<nsu, NTHREADS, 0, st>>>(
+                S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v64.p, w.p.p, w.q.p, w.part.p, w.cnt.p, w.sc.p,
+                w.sinst.p, w.sptr.p, 1);
+            k_bupdate<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r.p, w.z.p, w.p.p, w.q.p, w.dinv.p, w.part.p, w.cnt.p, w.sc.p,
+                                                    w.vinst.p, w.vptr.p, rtol, maxit);
+            k_bpupdate<NR><<<nvu, NTHREADS, 0, st>>>(w.z.p, w.p.p, w.sc.p, w.vinst.p);
+        };
+    }
     count_launch(ctx, 3);
     OGB_CUDA(cudaGetLastError());
-    auto iteration = [&]() {
-        k_bspmv<ND, NR, true><<<nsu, NTHREADS, 0, st>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v64.p, w.p.p,
-                                                        w.q.p, w.part.p, w.cnt.p, w.sc.p, w.sinst.p, w.sptr.p);
-        k_bupdate<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r.p, w.z.p, w.p.p, w.q.p, w.dinv.p, w.part.p, w.cnt.p, w.sc.p,
-                                                w.vinst.p, w.vptr.p, rtol, maxit);
-        k_bpupdate<NR><<<nvu, NTHREADS, 0, st>>>(w.z.p, w.p.p, w.sc.p, w.vinst.p);
-    };
-    // BBATCH iterations per host check, replayed from a captured graph
-    cudaGraphExec_t exec = nullptr;
-    struct ExecGuard {
-        cudaGraphExec_t &e;
-        ~ExecGuard()
-        {
-            if (e) cudaGraphExecDestroy(e);
-        }
-    } guard{exec};
-    if (ctx->use_graphs) {
-        cudaGraph_t g = nullptr;
-        OGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < BBATCH; ++k) iteration();
-        cudaError_t e = cudaStreamEndCapture(st, &g);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-    }
+    ExecGuard graph;
+    OGB_CHECK(capture_batch(ctx, iteration, graph.e));
     int zero = 0;
     OGB_CUDA(cudaMemcpyAsync(&zero, w.zero.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     res.resize(npair);
-    for (int it = 0;; it += BBATCH) {
+    int since = 0;   // iterations since the last residual replacement
+    for (int it = 0;;) {
         OGB_CUDA(cudaMemcpyAsync(res.data(), w.sc.p, npair * sizeof(BatchScal), cudaMemcpyDeviceToHost, st));
         OGB_CUDA(cudaStreamSynchronize(st));
         if (zero) {
             for (auto &s : res) s.done = 3;
             break;
         }
-        bool all = true;
-        for (auto &s : res) all = all && s.done;
-        if (all || it >= maxit) break;
-        if (exec) {
-            OGB_CUDA(cudaGraphLaunch(exec, st));
+        bool all = true, running = false;
+        for (auto &s : res) {
+            all = all && s.done;
+            running = running || (s.done == 0 && s.pause == 0);
+        }
+        if (all || it > maxit + 2 * REPLACE_EVERY) break;
+        if (mixed && (!running || since >= REPLACE_EVERY)) {
+            residual_spmv(w.q64.p);
+            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.p32.p, w.part.p,
+                                                     w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
+            count_launch(ctx, 2);
+            OGB_CUDA(cudaGetLastError());
+            since = 0;
+            continue;
+        }
+        if (graph.e) {
+            OGB_CUDA(cudaGraphLaunch(graph.e, st));
         } else {
             for (int k = 0; k < BBATCH; ++k) iteration();
         }
         count_launch(ctx, 3 * BBATCH);
         OGB_CUDA(cudaGetLastError());
+        it += BBATCH;
+        since += BBATCH;
     }
     return OGB_OK;
 }
@@ -421,19 +689,38 @@ __global__ void k_breactions(int n, const int *__restrict__ eq, const double *__
 }
 
 inline unsigned nblk(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
+// Column c of a column-major equation-space block <-> node space with nr interleaved columns.
+__global__ void k_eq_to_ns_col(int neq, const int *__restrict__ ns_of_eq, int nr, int c, const double *__restrict__ xe,
+                               double *__restrict__ xn)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < neq) xn[(int64_t)ns_of_eq[e] * nr + c] = xe[e];
+}
+
+__global__ void k_ns_to_eq_col(int neq, const int *__restrict__ ns_of_eq, int nr, int c, const double *__restrict__ xn,
+                               double *__restrict__ xe)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < neq) xe[e] = xn[(int64_t)ns_of_eq[e] * nr + c];
+}
+
 
 }  // namespace
 
-int batch_pcg_fp64(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int *iters,
-                   double *achieved, int *status)
+int batch_pcg(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int precision, int *iters,
+              double *achieved, int *status)
 {
     if (!m->has_sell) return fail(OGB_E_STATE, "batched solves need a matrix built from a model");
     if (nrhs < 1 || nrhs > MAXNR) return fail(OGB_E_ARG, "nrhs must be 1..4");
+    if (precision != OGB_PREC_FP64 && precision != OGB_PREC_MIXED) return fail(OGB_E_ARG, "unknown precision");
+    const bool mixed = precision == OGB_PREC_MIXED;
+    if (mixed && m->sell.v32_version != m->version)
+        return fail(OGB_E_STATE, "the FP32 copy of the matrix is not current (assemble through the model)");
     std::vector<BatchScal> res;
     int r = OGB_E_ARG;
     const int nd = m->sell.nd;
 #define OGB_BATCH_CASE(ND_, NR_) \
-    if (nd == ND_ && nrhs == NR_) r = run_batch<ND_, NR_>(m, b, x, rtol, maxit, res);
+    if (nd == ND_ && nrhs == NR_) r = run_batch<ND_, NR_>(m, b, x, rtol, maxit, mixed, res);
     OGB_BATCH_CASE(3, 1) OGB_BATCH_CASE(3, 2) OGB_BATCH_CASE(3, 3) OGB_BATCH_CASE(3, 4)
     OGB_BATCH_CASE(2, 1) OGB_BATCH_CASE(2, 2) OGB_BATCH_CASE(2, 3) OGB_BATCH_CASE(2, 4)
 #undef OGB_BATCH_CASE
@@ -455,12 +742,66 @@ int batch_pcg_fp64(ogb_mtrx *m, int nrhs, const double *b, double *x, double rto
     return worst;
 }
 
+// SparseLinearSystemNM::solve(A, B, X) (sparselinsystemnm.h:91) on a matrix
+// assembled from a model: B and X are device, column-major neq x nrhs, X holds
+// the initial guesses and receives the solutions. Columns go through the
+// batched solve four at a time; per column, the iteration count and achieved
+// residual are the largest over the instances and the status the first failure.
+int pcg_solve_multi(ogb_mtrx *m, int nrhs, const double *B, double *X, double rtol, int maxit, int precision,
+                    int *iters, double *achieved, int *status)
+{
+    ogb_ctx *ctx = m->ctx;
+    cudaStream_t s = ctx->stream;
+    if (!(m->has_sell && m->sell.v32_version == m->version))
+        return fail(OGB_E_STATE, "node-block copy not current");
+    const int neq = m->neq, ninst = m->sell.ninst;
+    int worst = OGB_OK;
+    for (int c0 = 0; c0 < nrhs; c0 += MAXNR) {
+        const int nr = nrhs - c0 < MAXNR ? nrhs - c0 : MAXNR;
+        const int64_t nv = m->sell.nns() * nr;
+        DBuf<double> b, x;
+        OGB_CHECK(b.alloc(nv));
+        OGB_CHECK(x.alloc(nv));
+        OGB_CUDA(cudaMemsetAsync(b.p, 0, nv * sizeof(double), s));
+        OGB_CUDA(cudaMemsetAsync(x.p, 0, nv * sizeof(double), s));
+        for (int c = 0; c < nr; ++c) {
+            k_eq_to_ns_col<<<nblk(neq), NTHREADS, 0, s>>>(neq, m->sell.ns_of_eq.p, nr, c, B + (size_t)(c0 + c) * neq, b.p);
+            k_eq_to_ns_col<<<nblk(neq), NTHREADS, 0, s>>>(neq, m->sell.ns_of_eq.p, nr, c, X + (size_t)(c0 + c) * neq, x.p);
+        }
+        count_launch(ctx, 2 * nr);
+        std::vector<int> it(ninst * nr), st(ninst * nr);
+        std::vector<double> ac(ninst * nr);
+        int r = batch_pcg(m, nr, b.p, x.p, rtol, maxit, precision, it.data(), ac.data(), st.data());
+        if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
+        if (r != OGB_OK && worst == OGB_OK) worst = r;
+        for (int c = 0; c < nr; ++c) {
+            k_ns_to_eq_col<<<nblk(neq), NTHREADS, 0, s>>>(neq, m->sell.ns_of_eq.p, nr, c, x.p, X + (size_t)(c0 + c) * neq);
+            int imax = 0, scode = OGB_OK;
+            double amax = 0.0;
+            for (int i = 0; i < ninst; ++i) {
+                const int k = i * nr + c;
+                imax = it[k] > imax ? it[k] : imax;
+                amax = ac[k] > amax ? ac[k] : amax;
+                if (st[k] != OGB_OK && scode == OGB_OK) scode = st[k];
+            }
+            if (iters) iters[c0 + c] = imax;
+            if (achieved) achieved[c0 + c] = amax;
+            if (status) status[c0 + c] = scode;
+        }
+        count_launch(ctx, nr);
+        OGB_CUDA(cudaGetLastError());
+        OGB_CUDA(cudaStreamSynchronize(s));   // b and x are freed at the end of the chunk
+    }
+    return worst;
+}
+
 // LinearStatic (linearstatic.C:177-253) for every instance and load case of a
 // batch at once: one stiffness assembly, nrhs internal-force evaluations of
 // the prescribed fields, one batched solve, nrhs scatters (and reactions).
 // bcval, load, u_nodes, reacs: device, nrhs consecutive node vectors.
 int batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load, double rtol,
-                        int maxit, double *u_nodes, double *reacs, int *iters, double *achieved, int *status,
+                        int maxit, int precision, double *u_nodes, double *reacs, int *iters, double *achieved,
+                        int *status,
                         int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *))
 {
     ogb_ctx *ctx = md->ctx;
@@ -485,7 +826,7 @@ int batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcva
     }
     OGB_CUDA(cudaGetLastError());
     OGB_CHECK(check_device_status(ctx, "assembly"));
-    int r = batch_pcg_fp64(m, nrhs, b.p, x.p, rtol, maxit, iters, achieved, status);
+    int r = batch_pcg(m, nrhs, b.p, x.p, rtol, maxit, precision, iters, achieved, status);
     if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
     for (int c = 0; c < nrhs; ++c) {
         double *u = u_nodes + (size_t)c * n;

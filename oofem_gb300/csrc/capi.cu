@@ -601,6 +601,51 @@ int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b, double *x, double rtol, int 
     return r;
 }
 
+int ogb_pcg_solve_multi_dev(ogb_mtrx *m, int nrhs, const double *B, double *X, double rtol, int maxit,
+                            int precision, int *iterations, double *achieved, int *status)
+{
+    if (!m || !B || !X || nrhs < 0) return fail(OGB_E_ARG, "bad argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    if (nrhs == 0) return OGB_OK;
+    if (m->has_sell && m->sell.v32_version == m->version)
+        return pcg_solve_multi(m, nrhs, B, X, rtol, maxit, precision, iterations, achieved, status);
+    // no current node-block copy (location-array matrix, or values changed
+    // through set_at): the reference's column loop (sparselinsystemnm.C:47-69)
+    int worst = OGB_OK;
+    for (int c = 0; c < nrhs; ++c) {
+        ogb_solve_info info{};
+        int r = ogb_pcg_solve_dev(m, B + (size_t)c * m->neq, X + (size_t)c * m->neq, rtol, maxit, precision, &info);
+        if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
+        if (iterations) iterations[c] = info.iterations;
+        if (achieved) achieved[c] = info.achieved;
+        if (status) status[c] = r;
+        if (r != OGB_OK && worst == OGB_OK) worst = r;
+    }
+    return worst;
+}
+
+int ogb_pcg_solve_multi(ogb_mtrx *m, int nrhs, const double *B, double *X, double rtol, int maxit, int precision,
+                        int *iterations, double *achieved, int *status)
+{
+    if (!m || !B || !X || nrhs < 0) return fail(OGB_E_ARG, "bad argument");
+    if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
+    OGB_CUDA(cudaSetDevice(m->ctx->device));
+    const size_t n = (size_t)m->neq * nrhs;
+    if (n == 0) return OGB_OK;
+    cudaStream_t s = m->ctx->stream;
+    DBuf<double> dB, dX;
+    OGB_CHECK(dB.alloc(n));
+    OGB_CHECK(dX.alloc(n));
+    OGB_CUDA(cudaMemcpyAsync(dB.p, B, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    OGB_CUDA(cudaMemcpyAsync(dX.p, X, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int r = ogb_pcg_solve_multi_dev(m, nrhs, dB.p, dX.p, rtol, maxit, precision, iterations, achieved, status);
+    if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
+    OGB_CUDA(cudaMemcpyAsync(X, dX.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return r;
+}
+
 // ------------------------------------------------------------------ element backend
 int ogb_model_create(ogb_ctx *ctx, int etype, int nnodes, const double *coords, int nelem, const int *conn,
                      const int *elem_mat, int nmat, const double *mats, double thickness, const uint8_t *bc_mask,
@@ -892,20 +937,20 @@ int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_start)
 }
 
 int ogb_batch_linear_static_dev(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load,
-                                double rtol, int maxit, double *u_nodes, double *reacs, int *iters, double *achieved,
-                                int *status)
+                                double rtol, int maxit, int precision, double *u_nodes, double *reacs, int *iters,
+                                double *achieved, int *status)
 {
     if (!md || !m || !bcval || !u_nodes) return fail(OGB_E_ARG, "null argument");
     if (nrhs < 1 || nrhs > 4) return fail(OGB_E_ARG, "nrhs must be 1..4");
     OGB_CUDA(cudaSetDevice(md->ctx->device));
     if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
-    return batch_linear_static(md, m, nrhs, bcval, load, rtol, maxit, u_nodes, reacs, iters, achieved, status,
-                               nr_assemble, nr_forces);
+    return batch_linear_static(md, m, nrhs, bcval, load, rtol, maxit, precision, u_nodes, reacs, iters, achieved,
+                               status, nr_assemble, nr_forces);
 }
 
 int ogb_batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load,
-                            double rtol, int maxit, double *u_nodes, double *reacs, int *iters, double *achieved,
-                            int *status)
+                            double rtol, int maxit, int precision, double *u_nodes, double *reacs, int *iters,
+                            double *achieved, int *status)
 {
     if (!md || !m || !bcval || !u_nodes) return fail(OGB_E_ARG, "null argument");
     if (nrhs < 1 || nrhs > 4) return fail(OGB_E_ARG, "nrhs must be 1..4");
@@ -919,7 +964,7 @@ int ogb_batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *
     if (reacs) OGB_CHECK(d_reac.alloc(n));
     OGB_CUDA(cudaMemcpyAsync(d_bc.p, bcval, n * sizeof(double), cudaMemcpyHostToDevice, s));
     if (load) OGB_CUDA(cudaMemcpyAsync(d_load.p, load, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    int r = ogb_batch_linear_static_dev(md, m, nrhs, d_bc.p, load ? d_load.p : nullptr, rtol, maxit, d_u.p,
+    int r = ogb_batch_linear_static_dev(md, m, nrhs, d_bc.p, load ? d_load.p : nullptr, rtol, maxit, precision, d_u.p,
                                         reacs ? d_reac.p : nullptr, iters, achieved, status);
     if (r != OGB_OK && r != OGB_E_NOTCONV && r != OGB_E_BREAKDOWN && r != OGB_E_ZERODIAG) return r;
     OGB_CUDA(cudaMemcpyAsync(u_nodes, d_u.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));

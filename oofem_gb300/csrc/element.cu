@@ -425,6 +425,46 @@ __global__ void __launch_bounds__(NTHREADS) k_elem_stiffness(
 
     const int le = threadIdx.x / NPE, a = threadIdx.x % NPE, e = e0 + le;
     if (e >= nelem) return;
+    if constexpr (ET == OGB_LSPACE && !PER_GP_D) {
+        // Isotropic D (D = 2G I_dev + K 1(x)1, isolinearelasticmaterial.C:80-88): with
+        // lambda = D_12 and mu = D_44,
+        //   K_ab^ij = sum_gp dV [lambda g_a^i g_b^j + mu g_a^j g_b^i + mu delta_ij g_a.g_b]
+        // = lambda A_ab^ij + mu A_ab^ji + mu delta_ij tr A_ab,  A_ab^ij = sum_gp dV g_a^i g_b^j,
+        // the same B^T D B dV sum in a third of the FP64 operations of the dense product.
+        const double *Dm = Dmat + 36 * __ldg(emat + e);
+        const double lam = __ldg(Dm + 1), mu = __ldg(Dm + 21);
+        double A[NPE][3][3];
+#pragma unroll
+        for (int b = 0; b < NPE; ++b)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) A[b][i][j] = 0.0;
+#pragma unroll 1
+        for (int gp = 0; gp < NGP; ++gp) {
+            const double dv = s_dv[le][gp];
+            const double ga[3] = {dv * s_g[le][gp][a][0], dv * s_g[le][gp][a][1], dv * s_g[le][gp][a][2]};
+#pragma unroll
+            for (int b = 0; b < NPE; ++b) {
+                const double h[3] = {s_g[le][gp][b][0], s_g[le][gp][b][1], s_g[le][gp][b][2]};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) A[b][i][j] = fma(ga[i], h[j], A[b][i][j]);
+            }
+        }
+        double *out = ke + (((size_t)e * NPE + a) * NPE) * 9;
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) {
+            const double mtr = mu * (A[b][0][0] + A[b][1][1] + A[b][2][2]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    out[(b * 3 + i) * 3 + j] = lam * A[b][i][j] + mu * A[b][j][i] + (i == j ? mtr : 0.0);
+        }
+        return;
+    }
     double D[NS][NS];
     if constexpr (!PER_GP_D) {
         const double *Dm = Dmat + 36 * __ldg(emat + e);

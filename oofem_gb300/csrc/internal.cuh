@@ -284,10 +284,13 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
                    int (*solve)(ogb_mtrx *, double, int, int, ogb_solve_info *));
 
 // batch.cu
-int batch_pcg_fp64(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int *iters,
-                   double *achieved, int *status);
+int batch_pcg(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int precision, int *iters,
+              double *achieved, int *status);
+int pcg_solve_multi(ogb_mtrx *m, int nrhs, const double *B, double *X, double rtol, int maxit, int precision,
+                    int *iters, double *achieved, int *status);
 int batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcval, const double *load, double rtol,
-                        int maxit, double *u_nodes, double *reacs, int *iters, double *achieved, int *status,
+                        int maxit, int precision, double *u_nodes, double *reacs, int *iters, double *achieved,
+                        int *status,
                         int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *));
 
 // helpers in capi.cu

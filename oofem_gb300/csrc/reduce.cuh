@@ -43,6 +43,42 @@ __device__ __forceinline__ void block_sum(double (&v)[NV])
     __syncthreads();
 }
 
+// Block reduction of per-thread values of type T: the warp sum stays in T (an
+// FP32 warp sum costs no FP64 instruction), the warps are added in FP64 in
+// index order. Result valid in thread 0.
+template <int NV, class T>
+__device__ __forceinline__ void block_sum_t(const T (&v)[NV], double (&out)[NV])
+{
+    __shared__ double red[NV][NTHREADS / 32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        T s = warp_sum(v[k]);
+        if (lane == 0) red[k][warp] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0;
+#pragma unroll
+            for (int w = 0; w < NTHREADS / 32; ++w) s += red[k][w];
+            out[k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Contiguous row range [lo, hi) of this block: equal shares of n rows, rounded
+// up to whole passes of NTHREADS rows (blocks past the end get an empty range).
+__device__ __forceinline__ void block_range(int64_t n, int64_t &lo, int64_t &hi)
+{
+    const int64_t share = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t per = (share + NTHREADS - 1) / NTHREADS * NTHREADS;
+    lo = (int64_t)blockIdx.x * per;
+    hi = lo + per < n ? lo + per : n;
+}
+
 // Publish this block's partials and report (to every thread of the block)
 // whether it was the last block of the grid to do so.
 template <int NV>

@@ -97,8 +97,10 @@ SIGNATURES = {
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_linear_static_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_model_set_instances": (_i, [_vp, _i, _vp]),
-    "ogb_batch_linear_static": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _vp]),
-    "ogb_batch_linear_static_dev": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _vp]),
+    "ogb_pcg_solve_multi": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp]),
+    "ogb_pcg_solve_multi_dev": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp]),
+    "ogb_batch_linear_static": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "ogb_batch_linear_static_dev": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -300,6 +302,24 @@ class GpuPcgSolver:
             _check(code)
         return code
 
+    def solve_multi(self, A: GpuCsrMtrx, B: np.ndarray, X: np.ndarray) -> int:
+        """solve(A, B, X) for a block of right-hand sides: B and X are (nrhs, neq)
+        arrays (row c = column c of the reference's FloatMatrix); X holds the
+        initial guesses and receives the solutions. Per-column iterations,
+        achieved residuals and statuses are kept in self.last_multi."""
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        assert X.dtype == np.float64 and X.flags.c_contiguous and X.shape == B.shape
+        nrhs = B.shape[0]
+        its = np.zeros(nrhs, np.int32)
+        ach = np.zeros(nrhs)
+        st = np.zeros(nrhs, np.int32)
+        code = A.lib.ogb_pcg_solve_multi(A.h, nrhs, _ptr(B), _ptr(X), self.tol, self.maxit, self.precision,
+                                         _ptr(its), _ptr(ach), _ptr(st))
+        self.last_multi = (its, ach, st)
+        if code not in SOLVER_STATUS:
+            _check(code)
+        return code
+
 
 class GpuModel:
     """Element backend for one mesh (one element type)."""
@@ -383,7 +403,7 @@ class GpuModel:
         _check(self.lib.ogb_model_set_instances(self.h, self._ninst, _ptr(ns)))
 
     def batch_linear_static(self, A: GpuCsrMtrx, bc_values, loads=None, rtol=1e-12, maxit=100000,
-                            want_reactions=True):
+                            want_reactions=True, precision=PREC_FP64):
         """LinearStatic of every instance and load case in one batched PCG.
 
         bc_values / loads: (nrhs, nnodes, ndofpn). Returns (u, reactions, iterations,
@@ -398,7 +418,8 @@ class GpuModel:
         ach = np.zeros((ninst, nrhs))
         st = np.zeros((ninst, nrhs), np.int32)
         code = self.lib.ogb_batch_linear_static(self.h, A.h, nrhs, _ptr(bcv), _ptr(ld) if ld is not None else None,
-                                                rtol, maxit, _ptr(u), _ptr(reac) if reac is not None else None,
+                                                rtol, maxit, precision, _ptr(u),
+                                                _ptr(reac) if reac is not None else None,
                                                 _ptr(its), _ptr(ach), _ptr(st))
         if code not in SOLVER_STATUS:
             _check(code)

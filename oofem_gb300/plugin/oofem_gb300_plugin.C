@@ -329,6 +329,39 @@ public:
         return CR_FAILED;
     }
 
+    /// Multiple right-hand sides (sparselinsystemnm.h:91): one batched solve on the
+    /// device instead of the default column loop (sparselinsystemnm.C:47-69).
+    ConvergedReason solve(SparseMtrx &A, FloatMatrix &B, FloatMatrix &X) override
+    {
+        auto *g = dynamic_cast< GpuCsrMtrx * >( & A );
+        if ( !g ) {
+            OOFEM_ERROR("GpuPcgSolver needs a GpuCsrMtrx (smtype 11)");
+        }
+        const int neq = A.giveNumberOfRows(), nrhs = B.giveNumberOfColumns();
+        if ( B.giveNumberOfRows() != neq ) {
+            OOFEM_ERROR("A and B matrix mismatch");
+        }
+        if ( X.giveNumberOfRows() != neq || X.giveNumberOfColumns() != nrhs ) {
+            X.resize(neq, nrhs);
+        }
+        std::vector< int > iters(nrhs), status(nrhs);
+        std::vector< double > achieved(nrhs);
+        int r = ogb_pcg_solve_multi(g->handle(), nrhs, B.givePointer(), X.givePointer(), tol, maxite, precision,
+                                    iters.data(), achieved.data(), status.data());
+        for ( int c = 0; c < nrhs; ++c ) {
+            OOFEM_LOG_INFO("GpuPcg(%s) rhs %d: status %d, nite %d, achieved tol. %g\n",
+                           precision == OGB_PREC_MIXED ? "mixed" : "fp64", c + 1, status [ c ], iters [ c ],
+                           achieved [ c ]);
+        }
+        if ( r == OGB_OK ) {
+            return CR_CONVERGED;
+        }
+        if ( r == OGB_E_NOTCONV ) {
+            return CR_DIVERGED_ITS;
+        }
+        return CR_FAILED;
+    }
+
     LinSystSolverType giveLinSystSolverType() const override { return ST_GpuPcg; }
     SparseMtrxType giveRecommendedMatrix(bool symmetric) const override { return SMT_GpuCsr; }
     const char *giveClassName() const override { return "GpuPcgSolver"; }

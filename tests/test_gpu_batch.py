@@ -111,3 +111,89 @@ def test_set_instances_rejects_coupled_and_late(ctx, native_lib):
     with pytest.raises(native_lib.OgbError) as e:
         model.set_instances([0, m.nnodes])
     assert e.value.code == -3
+
+
+def test_rve_batch_mixed_precision(ctx, native_lib, oracle):
+    """Mixed precision batch: FP32 matrix and Krylov vectors, FP64 solution,
+    convergence decided on the FP64 residual; displacements within 1e-6 of the
+    oracle's FP64 solve, every pair's FP64 relative residual <= rtol."""
+    from oofem_gb300 import meshgen as mg
+    meshes = mg.rve_batch(5, seed=4, side_min=6, side_max=30)
+    meshes.append(mg.quad_rve(1, seed=2))
+    big, ns = mg.concat_meshes(meshes)
+    model = native_lib.GpuModel(ctx, big)
+    model.set_instances(ns)
+    A = native_lib.GpuCsrMtrx(ctx)
+    nrhs = 3
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(nrhs)])
+    rtol = 1e-10
+    u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=rtol, precision=native_lib.PREC_MIXED)
+    assert (st == 0).all(), st
+    assert (ach <= rtol).all(), ach
+    for i, m in enumerate(meshes):
+        sl = slice(ns[i], ns[i + 1])
+        for lc in range(nrhs):
+            ref = _oracle_case(oracle, m, mg.rve_bc_values(m, lc), np.zeros_like(m.bc_value), 1e-13)
+            assert rel(u[lc, sl], ref["u"]) < 1e-6, (i, lc, rel(u[lc, sl], ref["u"]))
+            assert rel(reac[lc, sl], ref["reac"]) < 1e-6, (i, lc)
+
+
+def test_hex_batch_mixed_matches_fp64(ctx, native_lib):
+    from oofem_gb300 import meshgen as mg
+    meshes = [mg.hex_cantilever(12, 3, 3, jitter=0.2, seed=3), mg.hex_cantilever(8, 4, 4, jitter=0.2, seed=4)]
+    big, ns = mg.concat_meshes(meshes)
+    loads = np.stack([big.nodal_load, 2.0 * big.nodal_load])
+    bcv = np.stack([big.bc_value, big.bc_value])
+    out = {}
+    for prec in (native_lib.PREC_FP64, native_lib.PREC_MIXED):
+        model = native_lib.GpuModel(ctx, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(ctx)
+        u, reac, its, ach, st = model.batch_linear_static(A, bcv, loads, rtol=1e-10, precision=prec)
+        assert (st == 0).all() and (ach <= 1e-10).all()
+        out[prec] = u
+    assert rel(out[native_lib.PREC_MIXED], out[native_lib.PREC_FP64]) < 1e-6
+
+
+def test_solve_multi_matches_single_solves(ctx, native_lib, oracle):
+    """SparseLinearSystemNM::solve(A, B, X) with five right-hand sides: batched on a
+    model-assembled matrix (4 + 1 columns), the column loop on a location-array
+    matrix; both against separate single solves."""
+    from oofem_gb300 import meshgen as mg
+    m = mg.hex_cantilever(8, 3, 3, jitter=0.2, seed=5)
+    model = native_lib.GpuModel(ctx, m)
+    A = native_lib.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+    model.assemble_stiffness(A)
+    neq = model.neq()[0]
+    rng = np.random.default_rng(0)
+    B = rng.standard_normal((5, neq))
+    solver = native_lib.GpuPcgSolver(lstol=1e-12, lsiter=100000)
+    X = np.zeros_like(B)
+    assert solver.solve_multi(A, B, X) == 0
+    its, ach, st = solver.last_multi
+    assert (st == 0).all() and (ach <= 1e-12).all()
+    for c in range(5):
+        x = np.zeros(neq)
+        assert solver.solve(A, B[c], x) == 0
+        assert abs(int(its[c]) - solver.last.iterations) <= 2
+        assert rel(X[c], x) < 1e-9
+    # location-array matrix (no node-block copy): the column loop
+    nq, _, eq = oracle.number_equations(m.bc_mask)
+    loc = oracle.location_arrays(m.conn, eq)
+    L = native_lib.GpuCsrMtrx(ctx)
+    L.build_internal_structure(nq, loc)
+    L.assemble_begin()
+    for e in range(m.nelem):
+        ke = oracle.elem_stiffness(1, m.coords[m.conn[e]], oracle.isole_d(1, m.materials[0].E, m.materials[0].nu))
+        L.assemble(loc[e], ke)
+    L.assemble_end()
+    X2 = np.zeros_like(B)
+    assert solver.solve_multi(L, B, X2) == 0
+    assert rel(X2, X) < 1e-9
+    # mixed precision through the same entry point
+    mixed = native_lib.GpuPcgSolver(lstol=1e-10, lsiter=100000, precision=native_lib.PREC_MIXED)
+    X3 = np.zeros_like(B)
+    assert mixed.solve_multi(A, B, X3) == 0
+    assert (mixed.last_multi[1] <= 1e-10).all()
+    assert rel(X3, X) < 1e-6
