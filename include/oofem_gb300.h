@@ -95,6 +95,9 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 /*   OGB_OPT_MIXED_X64 (0/1): with FP32 vectors, accumulate the solution in FP64
  *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
 #define OGB_OPT_MIXED_X64 6
+/*   OGB_OPT_SPMV_GROUP (0, 1, 2, 4): block columns the node-block SpMV loads ahead;
+ *   0 (default) = timed once per matrix and value type by the built-in autotuner. */
+#define OGB_OPT_SPMV_GROUP 7
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
@@ -226,6 +229,12 @@ OGB_API int ogb_model_gp_state(ogb_model *md, double *state4);
 
 /* Zero the Newton solution and the material state (a fresh analysis). */
 OGB_API int ogb_model_reset_state(ogb_model *md);
+/* NonLinearStatic's `initialguess` (engngm.h:207-210, nlinearstatic.C:532-544):
+ * 0 = IG_None (default); 1 = IG_Tangent, the step starts from the free-DOF
+ * increment K^-1 (-sum_e K_e du_prescribed) that pushes the change of the
+ * prescribed values since the last converged step through the tangent of that
+ * state (EngngModel::assemblePrescribedExtrapolatedForces, engngm.C:1614-1666). */
+OGB_API int ogb_model_set_initial_guess(ogb_model *md, int type);
 /* One NonLinearStatic step with NRSolver in full Newton mode
  * (NonLinearStatic::proceedStep nlinearstatic.C:453-565 with controlmode 1,
  * stiffmode 0, no initial guess; NRSolver::solve nrsolver.C:204-402 with

@@ -109,7 +109,9 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
 {
     if (skip && inst_skip<NR>(sc, unit_inst[blockIdx.x], skip)) return;
     constexpr int W = ND * NR;               // vector entries per node row
-    constexpr int G = W <= 6 ? 4 : 2;        // blocks per prefetch group
+    // blocks per prefetch group: FP64 products are bound by the FP64 pipe and
+    // gain nothing from the extra registers of deeper prefetch
+    constexpr int G = sizeof(V) == 8 ? 1 : (W <= 6 ? 4 : 2);
     const int s = blockIdx.x * SPMV_SLICES + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
     V dot[NR];

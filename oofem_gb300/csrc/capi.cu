@@ -353,6 +353,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
     case OGB_OPT_MIXED_ORTH: ctx->mixed_orth = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_P32: ctx->mixed_p32 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_X64: ctx->mixed_x64 = value != 0; return OGB_OK;
+    case OGB_OPT_SPMV_GROUP:
+        if (value != 0 && value != 1 && value != 2 && value != 4) return fail(OGB_E_ARG, "SpMV group must be 0, 1, 2 or 4");
+        ctx->spmv_group = (int)value;
+        return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
         ctx->mixed_drop = value * 1e-6;
@@ -874,8 +878,17 @@ int ogb_model_reset_state(ogb_model *md)
     if (!md) return fail(OGB_E_ARG, "null argument");
     cudaStream_t s = md->ctx->stream;
     if (md->nr_X.p) OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, md->nr_X.n * sizeof(double), s));
+    if (md->nr_bcprev.p) OGB_CUDA(cudaMemsetAsync(md->nr_bcprev.p, 0, md->nr_bcprev.n * sizeof(double), s));
     if (md->state.p) OGB_CUDA(cudaMemsetAsync(md->state.p, 0, md->state.n * sizeof(double), s));
     OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_model_set_initial_guess(ogb_model *md, int type)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (type != 0 && type != 1) return fail(OGB_E_ARG, "initial guess must be 0 (IG_None) or 1 (IG_Tangent)");
+    md->initial_guess = type;
     return OGB_OK;
 }
 

@@ -136,6 +136,7 @@ struct SellMat {
     int64_t v32_version = -1;
     DBuf<int> ns_of_eq;     // node-space index of equation e (0-based)
     int ninst = 1;          // independent instances (block-diagonal batch)
+    int group[2] = {0, 0};  // tuned SpMV prefetch group for FP64 / FP32 values (0 = not yet)
     std::vector<int64_t> inst_row_base;   // first node-space row of each instance (+ total)
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
@@ -167,6 +168,7 @@ struct ogb_ctx {
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)
     bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
+    int spmv_group = 0;         // SELL SpMV prefetch group forced (1, 2, 4) or 0 = tuned per matrix
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;
@@ -239,6 +241,8 @@ struct ogb_model {
     std::vector<int> inst_start;   // first node of each instance (+ nnodes); {0, nnodes} for one mesh
     // Newton driver
     ogb::DBuf<double> nr_X, nr_part, nr_out;
+    ogb::DBuf<double> nr_bcprev, nr_du;   // prescribed values of the last converged step; increment
+    int initial_guess = 0;                 // NonLinearStatic initialGuess: 0 IG_None, 1 IG_Tangent
     ogb::DBuf<unsigned int> nr_count;
     ogb::HBuf<double> h_nr_out;
 };

@@ -108,6 +108,51 @@ __global__ void k_nr_reactions(int n, const int *__restrict__ eq, const double *
     if (i < n) reac[i] = eq[i] < 0 ? fint[i] - (load ? load[i] : 0.0) : 0.0;
 }
 
+// Prescribed increment since the last converged step: du = bcval - bcprev at
+// prescribed DOFs, 0 at free ones.
+__global__ void k_nr_prescribed_increment(int n, const int *__restrict__ eq, const double *__restrict__ bcval,
+                                          const double *__restrict__ bcprev, double *__restrict__ du)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) du[i] = eq[i] < 0 ? bcval[i] - bcprev[i] : 0.0;
+}
+
+// fe[e][a] = sum_b K_e[a][b] du[conn[e][b]] from the element matrices of the last
+// stiffness evaluation (node-block layout ke[e][a][b][i][j]); one thread per (e, a).
+template <int ND>
+__global__ void __launch_bounds__(NTHREADS) k_nr_ke_times(int nelem, int nnpe, const double *__restrict__ ke,
+                                                          const int *__restrict__ conn, const double *__restrict__ du,
+                                                          double *__restrict__ fe)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nelem * nnpe) return;
+    const int64_t e = t / nnpe;
+    const int a = (int)(t % nnpe);
+    double f[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) f[i] = 0.0;
+    const double *kb = ke + (size_t)t * nnpe * ND * ND;
+    for (int b = 0; b < nnpe; ++b) {
+        const int B = conn[e * nnpe + b];
+        double u[ND];
+#pragma unroll
+        for (int j = 0; j < ND; ++j) u[j] = du[(int64_t)B * ND + j];
+#pragma unroll
+        for (int i = 0; i < ND; ++i)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) f[i] += kb[(b * ND + i) * ND + j] * u[j];
+    }
+#pragma unroll
+    for (int i = 0; i < ND; ++i) fe[(size_t)t * ND + i] = f[i];
+}
+
+// b[eq-1] = -f at free DOFs.
+__global__ void k_nr_neg_free(int n, const int *__restrict__ eq, const double *__restrict__ f, double *__restrict__ b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && eq[i] > 0) b[eq[i] - 1] = -f[i];
+}
+
 }  // namespace
 
 int nr_ensure(ogb_model *md)
@@ -123,6 +168,12 @@ int nr_ensure(ogb_model *md)
     }
     OGB_CHECK(md->nr_out.alloc(16));
     OGB_CHECK(md->h_nr_out.alloc(16));
+    const size_t n = (size_t)md->nnodes * md->ndofpn;
+    if (!md->nr_bcprev.p) {
+        OGB_CHECK(md->nr_bcprev.alloc(n));
+        OGB_CUDA(cudaMemsetAsync(md->nr_bcprev.p, 0, n * sizeof(double), md->ctx->stream));
+    }
+    OGB_CHECK(md->nr_du.alloc(n));
     return OGB_OK;
 }
 
@@ -148,9 +199,34 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
         if (md->h_eq[i] > 0) nfree[i % nd]++;
     // tangent at the start of the step (temp state == committed state)
     OGB_CHECK(assemble(md, m));
+    ogb_solve_info last{};
+    if (md->initial_guess == 1) {
+        // IG_Tangent (nlinearstatic.C:532-544): X += K^-1 (-sum_e K_e du_p)
+        k_nr_prescribed_increment<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, bcval, md->nr_bcprev.p, md->nr_du.p);
+        const int64_t nt = (int64_t)md->nelem * md->nnpe;
+        if (nd == 3)
+            k_nr_ke_times<3><<<nblk(nt), NTHREADS, 0, s>>>(md->nelem, md->nnpe, md->ke.p, md->conn.p, md->nr_du.p,
+                                                           md->fe.p);
+        else
+            k_nr_ke_times<2><<<nblk(nt), NTHREADS, 0, s>>>(md->nelem, md->nnpe, md->ke.p, md->conn.p, md->nr_du.p,
+                                                           md->fe.p);
+        count_launch(ctx, 2);
+        OGB_CHECK(launch_gather_vector(md, md->v_fnode.p));
+        OGB_CUDA(cudaMemsetAsync(m->w_b.p, 0, (size_t)m->npad * sizeof(double), s));
+        k_nr_neg_free<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->v_fnode.p, m->w_b.p);
+        OGB_CUDA(cudaMemsetAsync(m->w_x.p, 0, (size_t)m->npad * sizeof(double), s));
+        count_launch(ctx);
+        OGB_CUDA(cudaGetLastError());
+        int r = solve(m, lin_rtol, 1000000, precision, &last);
+        if (r != OGB_OK) {
+            if (iterations) *iterations = 0;
+            return r;
+        }
+        k_nr_add<<<nblk(md->neq), NTHREADS, 0, s>>>(md->neq, md->nr_X.p, m->w_x.p);
+        count_launch(ctx);
+    }
     double *out = md->nr_out.p;
     int nite = 0;
-    ogb_solve_info last{};
     for (;;) {
         k_nr_assemble_u<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->nr_X.p, bcval, u_node);
         count_launch(ctx);
@@ -203,6 +279,7 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
         ++nite;
     }
     OGB_CHECK(ogb_model_commit_state(md));
+    OGB_CUDA(cudaMemcpyAsync(md->nr_bcprev.p, bcval, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     if (reac) {
         k_nr_reactions<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->v_fnode.p, load, reac);
         count_launch(ctx);

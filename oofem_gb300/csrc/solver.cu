@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(NTHREADS) k_spmv(int nchunks, const int64_t *_
 // and the product is (K x)_A = sum_{B != A} K_AB (x_B - x_A) + S_A x_A, which is
 // K x exactly but keeps the products small for smooth fields, so FP32 storage
 // loses far less on the near-rigid modes that decide CG convergence.
-template <int ND, class V, class X, class ACC, bool DOT, bool DIFF = false>
+template <int ND, class V, class X, class ACC, bool DOT, bool DIFF, int G>
 __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64_t *__restrict__ sl_ptr,
                                                         const int *__restrict__ sl_width, const int *__restrict__ col,
                                                         const V *__restrict__ val, const X *__restrict__ x,
@@ -112,9 +112,9 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
     if (DOT && halted(sc)) return;
     // Blocks are taken in groups of G: the G block columns of the next group are
     // loaded while the current group's gathers and products run, so the
-    // column -> x dependency does not stall every block (the stream reaches
-    // ~0.99 of the copy rate this way, against ~0.9 for a plain unrolled loop).
-    constexpr int G = 4;
+    // column -> x dependency does not stall every block (an FP32 stream reaches
+    // ~0.99 of the copy rate with G = 4, against ~0.9 for a plain unrolled loop).
+    // G is picked per matrix and value type by timing (sell_autotune).
     const int s = blockIdx.x * (NTHREADS / 32) + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
     double dot = 0.0;
@@ -656,6 +656,87 @@ Op make_op(ogb_mtrx *m, bool use_sell)
     return op;
 }
 
+template <class V, class X, class ACC, bool DOT, bool DIFF, int ND>
+void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int G, const V *val, const X *x, X *y, double *part,
+                    unsigned int *count, PcgScal *sc)
+{
+    switch (G) {
+    case 1:
+        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 1><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
+                                                                        val, x, y, part, count, sc);
+        break;
+    case 2:
+        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 2><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
+                                                                        val, x, y, part, count, sc);
+        break;
+    default:
+        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 4><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
+                                                                        val, x, y, part, count, sc);
+        break;
+    }
+}
+
+template <class V, class X, class ACC, bool DOT, bool DIFF>
+void launch_sell(cudaStream_t s, int g, const SellMat &S, int G, const V *val, const X *x, X *y, double *part,
+                 unsigned int *count, PcgScal *sc)
+{
+    if (S.nd == 3) launch_sell_nd<V, X, ACC, DOT, DIFF, 3>(s, g, S, G, val, x, y, part, count, sc);
+    else launch_sell_nd<V, X, ACC, DOT, DIFF, 2>(s, g, S, G, val, x, y, part, count, sc);
+}
+
+// Prefetch group of the SELL SpMV for value type V: the context's forced
+// choice, else the matrix's tuned one (4 until tuned).
+template <class V>
+int sell_group(const ogb_ctx *ctx, const SellMat &S)
+{
+    if (ctx->spmv_group) return ctx->spmv_group;
+    const int g = S.group[sizeof(V) == 4 ? 1 : 0];
+    return g ? g : 4;
+}
+
+// Autotuner: times the SpMV of this matrix and value type with prefetch groups
+// 1, 2 and 4 (three launches each after one warm-up, CUDA events on the
+// context stream) and keeps the fastest. Runs once per matrix structure and
+// value type, outside graph capture; x and y are scratch vectors.
+template <class V, class X, class ACC, bool DIFF>
+int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y)
+{
+    if (!op.sell || ctx->spmv_group) return OGB_OK;
+    SellMat &S = const_cast<SellMat &>(*op.S);
+    int &slot = S.group[sizeof(V) == 4 ? 1 : 0];
+    if (slot) return OGB_OK;
+    cudaStream_t s = ctx->stream;
+    const int g = op.spmv_grid();
+    cudaEvent_t e0, e1;
+    OGB_CUDA(cudaEventCreate(&e0));
+    OGB_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_g = 4;
+    for (int G : {1, 2, 4}) {
+        launch_sell<V, X, ACC, false, DIFF>(s, g, S, G, val, x, y, nullptr, nullptr, nullptr);
+        cudaEventRecord(e0, s);
+        for (int k = 0; k < 3; ++k) launch_sell<V, X, ACC, false, DIFF>(s, g, S, G, val, x, y, nullptr, nullptr, nullptr);
+        cudaEventRecord(e1, s);
+        count_launch(ctx, 4);
+        cudaError_t e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(e, "SpMV autotune");
+        }
+        if (G == 1 || ms < best) {
+            best = ms;
+            best_g = G;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    slot = best_g;
+    return OGB_OK;
+}
+
 template <class V, class X, bool DOT, class ACC = V, bool DIFF = false>
 int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double *part, unsigned int *count,
              PcgScal *sc)
@@ -666,12 +747,7 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
     prof_begin(ctx);
     if (op.sell) {
         const SellMat &S = *op.S;
-        if (S.nd == 3)
-            k_sell_spmv<3, V, X, ACC, DOT, DIFF><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y,
-                                                              part, count, sc);
-        else
-            k_sell_spmv<2, V, X, ACC, DOT, DIFF><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y,
-                                                              part, count, sc);
+        launch_sell<V, X, ACC, DOT, DIFF>(s, g, S, sell_group<V>(ctx, S), val, x, y, part, count, sc);
         // algorithmic bytes: every stored value and block column once (the SELL
         // padding slots are not counted), x once and y once
         bytes = (double)op.nzt * sizeof(V) + (double)op.nzt / (S.nd * S.nd) * sizeof(int) +
@@ -823,6 +899,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
     PcgScal *sc = m->w_scal.p;
     double *r = m->w_r.p, *z = m->w_z.p, *p = m->w_p.p, *q = m->w_q.p, *dinv = m->w_dinv.p;
     OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
+    OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, val, p, q)));
     OGB_CHECK((launch_diag_inv<double, double>(ctx, op, val, dinv, sc)));
     OGB_CHECK((apply_op<double, double, false>(ctx, op, val, x, q, nullptr, nullptr, nullptr)));
     k_pcg_init<double><<<g, NTHREADS, 0, s>>>(nch, b, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol);
@@ -893,6 +970,9 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
     OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
     const bool diff = op.sell && ctx->mixed_diff;
+    if (diff) OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q)));
+    else OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q)));
+    OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, v64, x, q64)));
     int iters = 0, replacements = 0, status = OGB_E_NOTCONV;
     double achieved = 0.0;
     bool first = true;

@@ -32,6 +32,7 @@ OPT_MIXED_ORTH = 3
 OPT_MIXED_DROP_PPM = 4
 OPT_MIXED_P32 = 5
 OPT_MIXED_X64 = 6
+OPT_SPMV_GROUP = 7
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
@@ -92,6 +93,7 @@ SIGNATURES = {
     "ogb_model_commit_state": (_i, [_vp]),
     "ogb_model_gp_state": (_i, [_vp, _vp]),
     "ogb_model_reset_state": (_i, [_vp]),
+    "ogb_model_set_initial_guess": (_i, [_vp, _i]),
     "ogb_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
@@ -427,6 +429,10 @@ class GpuModel:
 
     def reset_state(self):
         _check(self.lib.ogb_model_reset_state(self.h))
+
+    def set_initial_guess(self, kind: int):
+        """NonLinearStatic initialguess: 0 IG_None, 1 IG_Tangent."""
+        _check(self.lib.ogb_model_set_initial_guess(self.h, int(kind)))
 
     def nonlinear_step(self, A: GpuCsrMtrx, bc_value, nodal_load=None, rtolf=1e-8, maxiter=50,
                        lin_rtol=1e-12, precision=PREC_FP64):

@@ -230,13 +230,18 @@ def check_convergence(rhs_node, RT_node, eq, enorm, rtolf, nite):
     return ok, errs
 
 
-def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: int):
-    """NonLinearStatic (controlmode 1, no initial guess, tangent stiffness) with
-    NRSolver in full Newton mode (manrmsteps 1: tangent re-assembled every
-    iteration after the first, nrsolver.C:204-402). Prescribed values and loads
-    follow PiecewiseLinFunction t:[0, ramp_steps] -> f:[0, 1]. The linear systems
-    are solved directly (the reference decks use the default Skyline LDL^T).
-    Returns a list of per-step dicts (u, reactions, stresses, state, iterations)."""
+def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: int, initial_guess: int = 0):
+    """NonLinearStatic (controlmode 1, tangent stiffness) with NRSolver in full
+    Newton mode (manrmsteps 1: tangent re-assembled every iteration after the
+    first, nrsolver.C:204-402). Prescribed values and loads follow
+    PiecewiseLinFunction t:[0, ramp_steps] -> f:[0, 1]. initial_guess 1 is
+    IG_Tangent (nlinearstatic.C:532-544): before the Newton loop the free DOFs
+    take K^-1 (-sum_e K_e du_prescribed), the prescribed increment since the last
+    step pushed through the tangent of the last converged state
+    (EngngModel::assemblePrescribedExtrapolatedForces, engngm.C:1614-1666). The
+    linear systems are solved directly (the reference decks use the default
+    Skyline LDL^T). Returns a list of per-step dicts (u, reactions, stresses,
+    state, iterations)."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spla
     et = int(m["etype"])
@@ -248,12 +253,28 @@ def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: i
     state = np.zeros((ne * ngp(et), NSTATE))
     free = eq > 0
     X = np.zeros(neq)
+    if initial_guess:
+        # every DOF numbered (prescribed ones too) for K_e du_p over whole elements
+        nall, _, eq_all = number_equations(np.zeros_like(bc_mask))
+        loc_all = location_arrays(np.asarray(m["conn"]), eq_all)
+        rp_all, ci_all = build_pattern(nall, loc_all)
+    u_prev = np.zeros_like(np.asarray(m["bc_value"], dtype=np.float64))
     out = []
     for t in times:
         fac = float(t) / float(ramp_steps)
         u_presc = np.where(bc_mask == 1, np.asarray(m["bc_value"]) * fac, 0.0)
         RT_node = np.where(free, np.asarray(m["nodal_load"]) * fac, 0.0)
         val = assemble_tangent(m, loc, neq, rowptr, colind, state)
+        if initial_guess:
+            v_all = assemble_tangent(m, loc_all, nall, rp_all, ci_all, state)
+            K_all = sp.csr_matrix((v_all, ci_all, rp_all), shape=(nall, nall))
+            du = np.where(bc_mask == 1, u_presc - u_prev, 0.0)
+            f = (K_all @ du.ravel()).reshape(du.shape)
+            b = np.zeros(neq)
+            b[eq[free] - 1] = -f[free]
+            K = sp.csr_matrix((val, colind, rowptr), shape=(neq, neq))
+            X += spla.spsolve(K.tocsc(), b)
+        u_prev = u_presc
         nite = 0
         while True:
             u_node = u_presc.copy()

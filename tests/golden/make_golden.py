@@ -173,13 +173,14 @@ def main():
     args = ap.parse_args()
     os.makedirs(args.work, exist_ok=True)
     patch300(args.ref_src)
-    def nonlinear(name, mesh, nsteps, rtolf=1e-8, maxiter=100):
+    def nonlinear(name, mesh, nsteps, rtolf=1e-8, maxiter=100, initial_guess=0):
         analysis = (f"NonLinearStatic nsteps {nsteps} controlmode 1 rtolf {rtolf!r} maxiter {maxiter} "
-                    f"manrmsteps 1 stiffmode 0")
+                    f"manrmsteps 1 stiffmode 0" + (" initialguess 1" if initial_guess else ""))
         ramp = f"PiecewiseLinFunction 2 nPoints 2 t 2 0.0 {float(nsteps)!r} f(t) 2 0.0 1.0"
         run_case(name, mesh, args.work, analysis=analysis, dumpK=False, bc_ltf=2, load_ltf=2,
                  extra_funcs=(ramp,), extra=dict(rtolf=np.float64(rtolf), ramp_steps=np.int32(nsteps),
-                                                 maxiter=np.int32(maxiter)))
+                                                 maxiter=np.int32(maxiter),
+                                                 initial_guess=np.int32(initial_guess)))
 
     ey = 250e6 / 210e9
     cases = {
@@ -199,6 +200,11 @@ def main():
             "mises_hex_6x3x3", mg.hex_block_pull(6, 3, 3, h=0.05, jitter=0.2, seed=8,
                                                  material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6, H=2e9),
                                                  end_disp=4 * ey * 0.3), 8),
+        "mises_hex_10x3x3_ig": lambda: nonlinear(
+            "mises_hex_10x3x3_ig", mg.hex_block_pull(10, 3, 3, h=0.05, jitter=0.2, seed=9,
+                                                     material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6,
+                                                                          H=2e9),
+                                                     end_disp=3 * ey * 0.5), 10, initial_guess=1),
         "idm1_tet_3": lambda: nonlinear(
             "idm1_tet_3", mg.tet_cube(3, jitter=0.15, seed=5,
                                       material=mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=1000.0),

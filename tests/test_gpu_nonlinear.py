@@ -14,7 +14,7 @@ from test_gpu_linear import mesh_from_golden, rel
 
 pytestmark = pytest.mark.gpu
 
-NONLINEAR_CASES = ["mises_hex_4x2x2", "mises_hex_6x3x3", "idm1_tet_3"]
+NONLINEAR_CASES = ["mises_hex_4x2x2", "mises_hex_6x3x3", "mises_hex_10x3x3_ig", "idm1_tet_3"]
 
 
 @pytest.fixture(scope="module")
@@ -41,6 +41,7 @@ def test_newton_steps_match_reference(case, ctx, native_lib):
     g = load_golden(case)
     mesh = mesh_from_golden(g)
     model = native_lib.GpuModel(ctx, mesh)
+    model.set_initial_guess(int(g.get("initial_guess", 0)))
     A = native_lib.GpuCsrMtrx(ctx)
     res = run_steps(g, model, A, native_lib)
     for k, r in enumerate(res, 1):

@@ -87,7 +87,7 @@ def test_pcg_matches_reference_iteration_count(oracle):
     assert abs(tip - (-1.16468948e-03)) < 5e-11
 
 
-NONLINEAR_CASES = ["mises_hex_4x2x2", "mises_hex_6x3x3", "idm1_tet_3"]
+NONLINEAR_CASES = ["mises_hex_4x2x2", "mises_hex_6x3x3", "mises_hex_10x3x3_ig", "idm1_tet_3"]
 
 
 @pytest.mark.parametrize("case", NONLINEAR_CASES)
@@ -99,7 +99,8 @@ def test_nonlinear_static_newton(case, oracle):
     g = load_golden(case)
     ns = int(g["nsteps"])
     times = [float(g[f"s{k}_time"]) for k in range(1, ns + 1)]
-    res = oracle.nonlinear_static(g, times, float(g["ramp_steps"]), float(g["rtolf"]), int(g["maxiter"]))
+    res = oracle.nonlinear_static(g, times, float(g["ramp_steps"]), float(g["rtolf"]), int(g["maxiter"]),
+                                  initial_guess=int(g.get("initial_guess", 0)))
     mises = "mises" in case
     for k, r in enumerate(res, 1):
         assert r["nite"] == int(g[f"s{k}_nite"])
