@@ -218,6 +218,8 @@ def run_gpu(args):
                              jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"] + rank)
     nfree = mesh.nfree
     ctx = native.Context(local)
+    if args.spmv_variant:
+        ctx.set_option(native.OPT_SPMV_VARIANT, args.spmv_variant)
     model = native.GpuModel(ctx, mesh)
     A = native.GpuCsrMtrx(ctx)
     model.build_matrix(A)
@@ -273,6 +275,33 @@ def run_gpu(args):
     clk = clocks.stop()
     # FP64 drop-in path: iteration count and DOF/s for the mixed/FP64 ratio
     ms64, infos64, _, _ = timed(native.PREC_FP64, 1, 1)
+
+    # element evaluations: stiffness (K1) + deterministic gather assembly (K4),
+    # and internal forces (K2 + node gather), CUDA events on the library stream
+    def stream_ms(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    fnode = torch.zeros_like(bcv)
+    ms_k = stream_ms(lambda: lib.ogb_model_assemble_stiffness(model.h, A.h))
+    ms_f = stream_ms(lambda: lib.ogb_model_internal_forces_dev(model.h, C.c_void_p(u.data_ptr()),
+                                                               C.c_void_p(fnode.data_ptr())))
+    nnpe, nd = mesh.nnpe, mesh.ndofpn
+    ke_bytes = mesh.nelem * (nnpe * nd) ** 2 * 8
+    # K1 writes every element matrix once, K4 reads it once and writes the CSR
+    # values and both node-block copies (FP64 + FP32) once
+    asm_bytes = 2 * ke_bytes + nnz * (8 + 8 + 4)
+    elements = {"stiffness_assembly_ms": ms_k, "element_stiffness_per_s": mesh.nelem / (ms_k * 1e-3),
+                "stiffness_assembly_gbs": asm_bytes / (ms_k * 1e-3) / 1e9,
+                "internal_forces_ms": ms_f, "element_force_evals_per_s": mesh.nelem / (ms_f * 1e-3)}
     # replicas: total free DOFs of all ranks over the slowest rank's step time
     value = replicas.job_throughput(nfree, ms * 1e-3)
     ms = replicas.max_over_ranks(ms)
@@ -335,6 +364,7 @@ def run_gpu(args):
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "spmv_launches_per_step": sp_n / args.steps if sp_n else 0,
                      "spmv_ms_per_step": sp_ms / args.steps if sp_n else 0},
+        "elements": elements,
         "clocks": clk,
         "gpu_launches": int(launches),
         "e2e": {"value": ws * nfree / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": int(h2d),
@@ -541,6 +571,8 @@ def main():
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--workload", default="cantilever", choices=["cantilever", "rve_batch", "mises_block"])
     ap.add_argument("--rve-count", type=int, default=256)
+    ap.add_argument("--spmv-variant", type=int, default=0,
+                    help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -95,9 +95,11 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 /*   OGB_OPT_MIXED_X64 (0/1): with FP32 vectors, accumulate the solution in FP64
  *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
 #define OGB_OPT_MIXED_X64 6
-/*   OGB_OPT_SPMV_GROUP (0, 1, 2, 4): block columns the node-block SpMV loads ahead;
- *   0 (default) = timed once per matrix and value type by the built-in autotuner. */
-#define OGB_OPT_SPMV_GROUP 7
+/*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
+ *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 / 5 = each slice shared by
+ *   2 / 4 warps; 0 (default) = warps per slice from the slice count, loop form
+ *   timed once per matrix and value type by the built-in autotuner. */
+#define OGB_OPT_SPMV_VARIANT 7
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
@@ -297,6 +299,23 @@ OGB_API int ogb_batch_linear_static_dev(ogb_model *md, ogb_mtrx *m, int nrhs, co
                                         const double *loads_dev, double rtol, int maxit, int precision,
                                         double *u_nodes_dev, double *reactions_dev, int *iterations,
                                         double *achieved, int *status);
+
+/* One NonLinearStatic step of every instance at once (a batch of separate runs,
+ * ogb_model_set_instances with each instance's elements contiguous): one
+ * internal-force evaluation, one tangent assembly and one batched PCG per Newton
+ * iteration for the whole batch, while each instance applies its own NRSolver
+ * test (as ogb_nonlinear_step) and stops iterating once it has converged.
+ * iterations: ninst entries (Newton iterations of each instance). OGB_OK when
+ * every instance converged (state committed); OGB_E_NOTCONV when one reached
+ * maxiter (state left uncommitted). No reference counterpart beyond the
+ * per-instance NRSolver::solve it repeats. */
+OGB_API int ogb_batch_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bc_value, const double *nodal_load,
+                                     double rtolf, int maxiter, double lin_rtol, int precision, double *u_node,
+                                     double *reactions, int *iterations);
+OGB_API int ogb_batch_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bc_value_dev,
+                                         const double *nodal_load_dev, double rtolf, int maxiter,
+                                         double lin_rtol, int precision, double *u_node_dev,
+                                         double *reactions_dev, int *iterations);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,7 @@ __device__ __forceinline__ void inst_sums(const double *part, int64_t u0, int64_
     __threadfence();
 #pragma unroll
     for (int k = 0; k < NV; ++k) out[k] = 0.0;
+#pragma unroll 4
     for (int64_t u = u0 + threadIdx.x; u < u1; u += NTHREADS)
 #pragma unroll
         for (int k = 0; k < NV; ++k) out[k] += __ldcg(part + u * NV + k);
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
     constexpr int W = ND * NR;               // vector entries per node row
     // blocks per prefetch group: FP64 products are bound by the FP64 pipe and
     // gain nothing from the extra registers of deeper prefetch
-    constexpr int G = sizeof(V) == 8 ? 1 : (W <= 6 ? 4 : 2);
+    constexpr int G = sizeof(V) == 8 ? 1 : 4;
     const int s = blockIdx.x * SPMV_SLICES + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
     V dot[NR];

@@ -353,9 +353,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
     case OGB_OPT_MIXED_ORTH: ctx->mixed_orth = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_P32: ctx->mixed_p32 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_X64: ctx->mixed_x64 = value != 0; return OGB_OK;
-    case OGB_OPT_SPMV_GROUP:
-        if (value != 0 && value != 1 && value != 2 && value != 4) return fail(OGB_E_ARG, "SpMV group must be 0, 1, 2 or 4");
-        ctx->spmv_group = (int)value;
+    case OGB_OPT_SPMV_VARIANT:
+        if (value < 0 || value > 5) return fail(OGB_E_ARG, "SpMV variant must be 0 (tuned) or 1..5");
+        ctx->spmv_group = value >= 4 ? 1 : (int)value;
+        ctx->spmv_split = value == 0 ? 0 : value == 4 ? 2 : value == 5 ? 4 : 1;
         return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
@@ -879,6 +880,7 @@ int ogb_model_reset_state(ogb_model *md)
     cudaStream_t s = md->ctx->stream;
     if (md->nr_X.p) OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, md->nr_X.n * sizeof(double), s));
     if (md->nr_bcprev.p) OGB_CUDA(cudaMemsetAsync(md->nr_bcprev.p, 0, md->nr_bcprev.n * sizeof(double), s));
+    if (md->nrb_X.p) OGB_CUDA(cudaMemsetAsync(md->nrb_X.p, 0, md->nrb_X.n * sizeof(double), s));
     if (md->state.p) OGB_CUDA(cudaMemsetAsync(md->state.p, 0, md->state.n * sizeof(double), s));
     OGB_CUDA(cudaStreamSynchronize(s));
     return OGB_OK;
@@ -939,13 +941,61 @@ int ogb_model_set_instances(ogb_model *md, int ninst, const int *node_start)
     std::vector<int> inst_of(md->nnodes);
     for (int i = 0; i < ninst; ++i)
         for (int A = node_start[i]; A < node_start[i + 1]; ++A) inst_of[A] = i;
+    // element ranges: recorded when the elements of each instance are contiguous
+    // and in instance order (as for concatenated meshes); the batched Newton
+    // step needs them
+    std::vector<int> elem_start(ninst + 1, 0);
+    bool ordered = true;
+    int prev = 0;
     for (int e = 0; e < md->nelem; ++e) {
         const int i0 = inst_of[conn[(size_t)e * md->nnpe]];
         for (int a = 1; a < md->nnpe; ++a)
             if (inst_of[conn[(size_t)e * md->nnpe + a]] != i0)
                 return fail(OGB_E_MESH, "element " + std::to_string(e) + " couples two instances");
+        if (i0 < prev) ordered = false;
+        for (int i = prev + 1; i <= i0; ++i) elem_start[i] = e;
+        prev = i0 > prev ? i0 : prev;
     }
+    for (int i = prev + 1; i <= ninst; ++i) elem_start[i] = md->nelem;
     md->inst_start.assign(node_start, node_start + ninst + 1);
+    md->inst_elem_start.clear();
+    if (ordered) md->inst_elem_start = elem_start;
+    return OGB_OK;
+}
+
+int ogb_batch_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,
+                                 int maxiter, double lin_rtol, int precision, double *u_node, double *reac,
+                                 int *iterations)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
+    if (!md->inc.p)
+        OGB_CHECK(build_incidence(md->ctx, md->nnodes, md->nelem, md->nnpe, md->conn.p, md->inc_ptr, md->inc));
+    return nonlinear_step_batch(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac, iterations,
+                                nr_assemble, nr_forces);
+}
+
+int ogb_batch_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,
+                             int maxiter, double lin_rtol, int precision, double *u_node, double *reac,
+                             int *iterations)
+{
+    if (!md || !m || !bcval || !u_node) return fail(OGB_E_ARG, "null argument");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    const size_t n = (size_t)md->nnodes * md->ndofpn;
+    cudaStream_t s = md->ctx->stream;
+    OGB_CHECK(md->v_bcval.alloc(n));
+    OGB_CHECK(md->v_load.alloc(n));
+    OGB_CHECK(md->v_unode.alloc(n));
+    OGB_CHECK(md->v_reac.alloc(n));
+    OGB_CUDA(cudaMemcpyAsync(md->v_bcval.p, bcval, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (load) OGB_CUDA(cudaMemcpyAsync(md->v_load.p, load, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int r = ogb_batch_nonlinear_step_dev(md, m, md->v_bcval.p, load ? md->v_load.p : nullptr, rtolf, maxiter, lin_rtol,
+                                         precision, md->v_unode.p, reac ? md->v_reac.p : nullptr, iterations);
+    if (r != OGB_OK) return r;
+    OGB_CUDA(cudaMemcpyAsync(u_node, md->v_unode.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (reac) OGB_CUDA(cudaMemcpyAsync(reac, md->v_reac.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
     return OGB_OK;
 }
 

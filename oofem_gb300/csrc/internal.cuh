@@ -136,7 +136,8 @@ struct SellMat {
     int64_t v32_version = -1;
     DBuf<int> ns_of_eq;     // node-space index of equation e (0-based)
     int ninst = 1;          // independent instances (block-diagonal batch)
-    int group[2] = {0, 0};  // tuned SpMV prefetch group for FP64 / FP32 values (0 = not yet)
+    int group[2] = {0, 0};  // tuned SpMV variant for FP64 / FP32 values (0 = not yet)
+    int force_split = 0;    // warps per slice forced by OGB_OPT_SPMV_VARIANT 5 / 6 (0 = rule)
     std::vector<int64_t> inst_row_base;   // first node-space row of each instance (+ total)
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
@@ -168,7 +169,8 @@ struct ogb_ctx {
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)
     bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
-    int spmv_group = 0;         // SELL SpMV prefetch group forced (1, 2, 4) or 0 = tuned per matrix
+    int spmv_group = 0;         // SELL SpMV loop variant forced (1..4) or 0 = tuned per matrix
+    int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;
@@ -239,6 +241,11 @@ struct ogb_model {
     ogb_mtrx *bound = nullptr;
     bool nonlinear = false;
     std::vector<int> inst_start;   // first node of each instance (+ nnodes); {0, nnodes} for one mesh
+    std::vector<int> inst_elem_start;   // first element of each instance (+ nelem) when contiguous, else empty
+    ogb::DBuf<int> d_inst_start, d_inst_elem_start, d_node_inst;
+    ogb::DBuf<double> nrb_X, nrb_b, nrb_x, nrb_out;   // batched Newton: node-space solution, increment
+    ogb::DBuf<unsigned int> nrb_cnt;
+    ogb::DBuf<int> nrb_active;
     // Newton driver
     ogb::DBuf<double> nr_X, nr_part, nr_out;
     ogb::DBuf<double> nr_bcprev, nr_du;   // prescribed values of the last converged step; increment
@@ -296,6 +303,10 @@ int batch_linear_static(ogb_model *md, ogb_mtrx *m, int nrhs, const double *bcva
                         int maxit, int precision, double *u_nodes, double *reacs, int *iters, double *achieved,
                         int *status,
                         int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *));
+
+int nonlinear_step_batch(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,
+                         int maxiter, double lin_rtol, int precision, double *u_node, double *reac, int *iterations,
+                         int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *));
 
 // helpers in capi.cu
 inline void count_launch(ogb_ctx *ctx, int n = 1) { ctx->launches += n; }

@@ -153,6 +153,90 @@ __global__ void k_nr_neg_free(int n, const int *__restrict__ eq, const double *_
     if (i < n && eq[i] > 0) b[eq[i] - 1] = -f[i];
 }
 
+// ---- batched Newton: independent instances, each with its own convergence test
+// u from the node-space solution X (free DOFs) and the prescribed values.
+__global__ void k_nrb_assemble_u(int n, int nd, const int *__restrict__ eq, const int *__restrict__ act,
+                                 const double *__restrict__ X, const double *__restrict__ bcval, double *__restrict__ u)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[i] = eq[i] > 0 ? X[(int64_t)act[i / nd] * nd + i % nd] : bcval[i];
+}
+
+// Per instance and DOF id: sum_free rhs^2, sum_free RT^2 (nodes of the instance)
+// and eNorm (element force entries of the instance). Grid (GX, ninst); the last
+// block of an instance sums its GX partials in order.
+template <int ND>
+__global__ void __launch_bounds__(NTHREADS) k_nrb_sums(const int *__restrict__ node_start,
+                                                       const int *__restrict__ elem_start, int nnpe,
+                                                       const int *__restrict__ eq, const double *__restrict__ load,
+                                                       const double *__restrict__ fint, const double *__restrict__ fe,
+                                                       double *part, unsigned int *cnt, double *out)
+{
+    const int inst = blockIdx.y;
+    double v[3 * ND];
+#pragma unroll
+    for (int k = 0; k < 3 * ND; ++k) v[k] = 0.0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int A = node_start[inst] + blockIdx.x * blockDim.x + threadIdx.x; A < node_start[inst + 1]; A += stride) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const int i = A * ND + d;
+            if (eq[i] > 0) {
+                const double rt = load ? load[i] : 0.0;
+                const double r = rt - fint[i];
+                v[d] += r * r;
+                v[ND + d] += rt * rt;
+            }
+        }
+    }
+    const int64_t k0 = (int64_t)elem_start[inst] * nnpe, k1 = (int64_t)elem_start[inst + 1] * nnpe;
+    for (int64_t k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += stride) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double f = fe[k * ND + d];
+            v[2 * ND + d] += f * f;
+        }
+    }
+    block_sum<3 * ND>(v);
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 3 * ND; ++k) part[((size_t)inst * gridDim.x + blockIdx.x) * 3 * ND + k] = v[k];
+        __threadfence();
+        s_last = atomicAdd(cnt + inst, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return;
+    __threadfence();
+    double t[3 * ND];
+#pragma unroll
+    for (int k = 0; k < 3 * ND; ++k) t[k] = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b)
+#pragma unroll
+        for (int k = 0; k < 3 * ND; ++k) t[k] += __ldcg(part + ((size_t)inst * gridDim.x + b) * 3 * ND + k);
+#pragma unroll
+    for (int k = 0; k < 3 * ND; ++k) out[(size_t)inst * 3 * ND + k] = t[k];
+    cnt[inst] = 0;
+}
+
+// Node-space right-hand side: b = RT - F at free DOFs of running instances
+// (scale -1 and no load: b = -F, for the initial guess), 0 elsewhere.
+__global__ void k_nrb_rhs(int n, int nd, const int *__restrict__ eq, const int *__restrict__ act,
+                          const int *__restrict__ node_inst, const int *__restrict__ active,
+                          const double *__restrict__ load, const double *__restrict__ f, double *__restrict__ b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || eq[i] <= 0) return;
+    const int A = i / nd;
+    b[(int64_t)act[A] * nd + i % nd] = active[node_inst[A]] ? (load ? load[i] : 0.0) - f[i] : 0.0;
+}
+
+__global__ void k_nrb_add(int64_t n, double *__restrict__ X, const double *__restrict__ dX)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) X[i] += dX[i];
+}
+
 }  // namespace
 
 int nr_ensure(ogb_model *md)
@@ -287,6 +371,160 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
     OGB_CUDA(cudaGetLastError());
     if (iterations) *iterations = nite;
     if (lin_info) *lin_info = last;
+    return OGB_OK;
+}
+
+// NonLinearStatic steps of independent instances advanced together (a batch of
+// separate runs): one internal-force evaluation, one tangent assembly and one
+// batched PCG per Newton iteration for all instances, while every instance
+// keeps its own NRSolver convergence test (DOF-grouped, as nonlinear_step) and
+// stops iterating -- zero right-hand side, zero increment -- once converged.
+// iterations[i]: Newton iterations of instance i. Returns OGB_OK when every
+// instance converged; the state is committed only then.
+int nonlinear_step_batch(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,
+                         int maxiter, double lin_rtol, int precision, double *u_node, double *reac, int *iterations,
+                         int (*assemble)(ogb_model *, ogb_mtrx *), int (*forces)(ogb_model *, const double *, double *))
+{
+    ogb_ctx *ctx = md->ctx;
+    cudaStream_t s = ctx->stream;
+    const int nd = md->ndofpn, nn = md->nnodes, n = nn * nd;
+    const int ninst = (int)md->inst_start.size() - 1;
+    if (!m->has_sell || m->sell.ninst != ninst) return fail(OGB_E_STATE, "matrix not built from this batch");
+    if ((int)md->inst_elem_start.size() != ninst + 1)
+        return fail(OGB_E_STATE, "batched Newton needs each instance's elements contiguous and in instance order");
+    OGB_CHECK(nr_ensure(md));
+    OGB_CHECK(md->v_fnode.alloc(n));
+    const int64_t nv = m->sell.nns();
+    if (!md->nrb_X.p) {
+        OGB_CHECK(md->nrb_X.alloc(nv));
+        OGB_CUDA(cudaMemsetAsync(md->nrb_X.p, 0, nv * sizeof(double), s));
+    }
+    OGB_CHECK(md->nrb_b.alloc(nv));
+    OGB_CHECK(md->nrb_x.alloc(nv));
+    OGB_CHECK(md->nrb_out.alloc((size_t)ninst * 3 * nd));
+    constexpr int GX = 16;
+    OGB_CHECK(md->nr_part.alloc((size_t)ninst * GX * 3 * nd));
+    if (!md->nrb_cnt.p) {
+        OGB_CHECK(md->nrb_cnt.alloc(ninst));
+        OGB_CUDA(cudaMemsetAsync(md->nrb_cnt.p, 0, ninst * sizeof(unsigned int), s));
+    }
+    OGB_CHECK(md->nrb_active.alloc(ninst));
+    if (!md->d_node_inst.p) {
+        std::vector<int> ni(nn);
+        for (int i = 0; i < ninst; ++i)
+            for (int A = md->inst_start[i]; A < md->inst_start[i + 1]; ++A) ni[A] = i;
+        OGB_CHECK(md->d_node_inst.alloc(nn));
+        OGB_CHECK(md->d_inst_start.alloc(ninst + 1));
+        OGB_CHECK(md->d_inst_elem_start.alloc(ninst + 1));
+        OGB_CUDA(cudaMemcpyAsync(md->d_node_inst.p, ni.data(), nn * sizeof(int), cudaMemcpyHostToDevice, s));
+        OGB_CUDA(cudaMemcpyAsync(md->d_inst_start.p, md->inst_start.data(), (ninst + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
+        OGB_CUDA(cudaMemcpyAsync(md->d_inst_elem_start.p, md->inst_elem_start.data(), (ninst + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
+        OGB_CUDA(cudaStreamSynchronize(s));
+    }
+    // free DOFs per (instance, DOF id): which groups enter the test
+    std::vector<int> nfree((size_t)ninst * nd, 0);
+    for (int i = 0; i < ninst; ++i)
+        for (int A = md->inst_start[i]; A < md->inst_start[i + 1]; ++A)
+            for (int d = 0; d < nd; ++d)
+                if (md->h_eq[(size_t)A * nd + d] > 0) nfree[(size_t)i * nd + d]++;
+    std::vector<int> active(ninst, 1), nite(ninst, 0);
+    std::vector<double> h((size_t)ninst * 3 * nd);
+    std::vector<int> pit(ninst), pst(ninst);
+    std::vector<double> pac(ninst);
+    auto solve_batch = [&]() -> int {
+        OGB_CUDA(cudaMemsetAsync(md->nrb_x.p, 0, nv * sizeof(double), s));
+        int r = batch_pcg(m, 1, md->nrb_b.p, md->nrb_x.p, lin_rtol, 1000000, precision, pit.data(), pac.data(),
+                          pst.data());
+        if (r != OGB_OK) return r;
+        k_nrb_add<<<nblk(nv), NTHREADS, 0, s>>>(nv, md->nrb_X.p, md->nrb_x.p);
+        count_launch(ctx);
+        return OGB_OK;
+    };
+    auto upload_active = [&]() -> int {
+        OGB_CUDA(cudaMemcpyAsync(md->nrb_active.p, active.data(), ninst * sizeof(int), cudaMemcpyHostToDevice, s));
+        return OGB_OK;
+    };
+    OGB_CHECK(assemble(md, m));   // tangent at the start of the step
+    if (md->initial_guess == 1) {
+        k_nr_prescribed_increment<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, bcval, md->nr_bcprev.p, md->nr_du.p);
+        const int64_t nt = (int64_t)md->nelem * md->nnpe;
+        if (nd == 3)
+            k_nr_ke_times<3><<<nblk(nt), NTHREADS, 0, s>>>(md->nelem, md->nnpe, md->ke.p, md->conn.p, md->nr_du.p,
+                                                           md->fe.p);
+        else
+            k_nr_ke_times<2><<<nblk(nt), NTHREADS, 0, s>>>(md->nelem, md->nnpe, md->ke.p, md->conn.p, md->nr_du.p,
+                                                           md->fe.p);
+        count_launch(ctx, 2);
+        OGB_CHECK(launch_gather_vector(md, md->v_fnode.p));
+        OGB_CHECK(upload_active());
+        OGB_CUDA(cudaMemsetAsync(md->nrb_b.p, 0, nv * sizeof(double), s));
+        k_nrb_rhs<<<nblk(n), NTHREADS, 0, s>>>(n, nd, md->eq.p, md->act.p, md->d_node_inst.p, md->nrb_active.p,
+                                               nullptr, md->v_fnode.p, md->nrb_b.p);
+        count_launch(ctx);
+        OGB_CHECK(solve_batch());
+    }
+    int status = OGB_OK;
+    for (int it = 0;; ++it) {
+        k_nrb_assemble_u<<<nblk(n), NTHREADS, 0, s>>>(n, nd, md->eq.p, md->act.p, md->nrb_X.p, bcval, u_node);
+        count_launch(ctx);
+        OGB_CHECK(forces(md, u_node, md->v_fnode.p));
+        dim3 grid(GX, ninst);
+        if (nd == 3)
+            k_nrb_sums<3><<<grid, NTHREADS, 0, s>>>(md->d_inst_start.p, md->d_inst_elem_start.p, md->nnpe, md->eq.p,
+                                                    load, md->v_fnode.p, md->fe.p, md->nr_part.p, md->nrb_cnt.p,
+                                                    md->nrb_out.p);
+        else
+            k_nrb_sums<2><<<grid, NTHREADS, 0, s>>>(md->d_inst_start.p, md->d_inst_elem_start.p, md->nnpe, md->eq.p,
+                                                    load, md->v_fnode.p, md->fe.p, md->nr_part.p, md->nrb_cnt.p,
+                                                    md->nrb_out.p);
+        count_launch(ctx);
+        OGB_CUDA(cudaGetLastError());
+        OGB_CUDA(cudaMemcpyAsync(h.data(), md->nrb_out.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        OGB_CUDA(cudaStreamSynchronize(s));
+        OGB_CHECK(check_device_status(ctx, "batched nonlinear step"));
+        bool any = false;
+        for (int i = 0; i < ninst; ++i) {
+            if (!active[i]) continue;
+            bool conv = true;
+            for (int d = 0; d < nd; ++d) {
+                if (!nfree[(size_t)i * nd + d]) continue;
+                const double *hi = h.data() + (size_t)i * 3 * nd;
+                const double den = hi[nd + d] + hi[2 * nd + d];
+                const double err = den >= 1e-6 ? sqrt(hi[d] / den) : sqrt(hi[d]);
+                if (!isfinite(err) || err > rtolf * 1e20) {
+                    for (int k = 0; k < ninst; ++k)
+                        if (iterations) iterations[k] = nite[k];
+                    return fail(OGB_E_BREAKDOWN, "NRSolver divergence in instance " + std::to_string(i));
+                }
+                if (err > rtolf || (err > 0.0 && nite[i] == 0)) conv = false;
+            }
+            if (conv) active[i] = 0;
+            else if (nite[i] >= maxiter) status = OGB_E_NOTCONV;
+            else any = true;
+        }
+        if (status != OGB_OK || !any) break;
+        if (it > 0) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
+        OGB_CHECK(upload_active());
+        OGB_CUDA(cudaMemsetAsync(md->nrb_b.p, 0, nv * sizeof(double), s));
+        k_nrb_rhs<<<nblk(n), NTHREADS, 0, s>>>(n, nd, md->eq.p, md->act.p, md->d_node_inst.p, md->nrb_active.p, load,
+                                               md->v_fnode.p, md->nrb_b.p);
+        count_launch(ctx);
+        OGB_CHECK(solve_batch());
+        for (int i = 0; i < ninst; ++i)
+            if (active[i]) ++nite[i];
+    }
+    if (iterations)
+        for (int i = 0; i < ninst; ++i) iterations[i] = nite[i];
+    if (status != OGB_OK) return fail(status, "NRSolver: maximum number of iterations reached without convergence");
+    OGB_CHECK(ogb_model_commit_state(md));
+    OGB_CUDA(cudaMemcpyAsync(md->nr_bcprev.p, bcval, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (reac) {
+        k_nr_reactions<<<nblk(n), NTHREADS, 0, s>>>(n, md->eq.p, md->v_fnode.p, load, reac);
+        count_launch(ctx);
+    }
+    OGB_CUDA(cudaGetLastError());
     return OGB_OK;
 }
 

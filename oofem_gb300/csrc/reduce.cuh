@@ -106,8 +106,12 @@ __device__ __forceinline__ void final_sums(const double *part, double (&out)[NV]
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         double s = 0;
-        const volatile double *pp = part + (size_t)k * gridDim.x;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += NTHREADS) s += pp[b];
+        const double *pp = part + (size_t)k * gridDim.x;
+        // L2 loads (the partials were written by other blocks before their
+        // fence and count increment); independent, so a thread's loads are in
+        // flight together instead of one L2 round trip per partial
+#pragma unroll 8
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += NTHREADS) s += __ldcg(pp + b);
         out[k] = s;
     }
     block_sum<NV>(out);

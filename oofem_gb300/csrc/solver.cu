@@ -110,11 +110,12 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
                                                         PcgScal *sc)
 {
     if (DOT && halted(sc)) return;
-    // Blocks are taken in groups of G: the G block columns of the next group are
-    // loaded while the current group's gathers and products run, so the
-    // column -> x dependency does not stall every block (an FP32 stream reaches
-    // ~0.99 of the copy rate with G = 4, against ~0.9 for a plain unrolled loop).
-    // G is picked per matrix and value type by timing (sell_autotune).
+    // G = 0: a plain loop over the blocks of the row, unrolled by four.
+    // G > 0: blocks are taken in groups of G and the G block columns of the next
+    // group are loaded while the current group's gathers and products run, so
+    // the column -> x dependency does not stall every block. Which is faster
+    // depends on the matrix (its width, the locality of its gathers, its size
+    // against L2): sell_autotune times them per matrix and value type.
     const int s = blockIdx.x * (NTHREADS / 32) + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
     double dot = 0.0;
@@ -130,32 +131,50 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
         }
         const V *vp = val + base * (ND * ND) + r;
         const int *cp = col + base + r;   // values and columns are streamed once: evict first
-        int cn[G];
-#pragma unroll
-        for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
-        for (int k0 = 0; k0 < w; k0 += G) {
-            int cc[G];
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                cc[g] = cn[g];
-                cn[g] = k0 + G + g < w ? __ldcs(cp + 32 * (k0 + G + g)) : arow;
-            }
-            ACC xb[G][ND];
-#pragma unroll
-            for (int g = 0; g < G; ++g)
+        if constexpr (G == 0) {
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const int c = __ldcs(cp + 32 * k);
+                ACC xb[ND];
 #pragma unroll
                 for (int j = 0; j < ND; ++j) {
-                    xb[g][j] = (ACC)__ldg(x + (int64_t)cc[g] * ND + j);
-                    if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
+                    xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
+                    if (DIFF && c != arow) xb[j] -= xa[j];
                 }
+                const V *vk = vp + (int64_t)k * (32 * ND * ND);
 #pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (k0 + g < w) {
-                    const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+                for (int i = 0; i < ND; ++i)
 #pragma unroll
-                    for (int i = 0; i < ND; ++i)
+                    for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
+            }
+        } else {
+            int cn[G];
 #pragma unroll
-                        for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[g][j];
+            for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
+            for (int k0 = 0; k0 < w; k0 += G) {
+                int cc[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    cc[g] = cn[g];
+                    cn[g] = k0 + G + g < w ? __ldcs(cp + 32 * (k0 + G + g)) : arow;
+                }
+                ACC xb[G][ND];
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) {
+                        xb[g][j] = (ACC)__ldg(x + (int64_t)cc[g] * ND + j);
+                        if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
+                    }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (k0 + g < w) {
+                        const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[g][j];
+                    }
                 }
             }
         }
@@ -634,13 +653,30 @@ struct Op {
     // SELL
     const SellMat *S = nullptr;
     int nchunks() const { return (int)(n / CHUNK); }
-    int spmv_grid() const { return sell ? (int)ceil_div(S->nslices, NTHREADS / 32) : vec_grid(nchunks()); }
+    int spmv_grid() const;
 };
+
+// Warps per slice: four for small matrices (fewer than 16 slices per SM, where
+// one warp per slice leaves most warp slots empty), else one -- measured on
+// GB300 over 1.3k, 10.5k and 31.7k slices of 27-block rows.
+inline int sell_split(const SellMat &S)
+{
+    if (S.force_split) return S.force_split;
+    return S.nslices < NUM_SMS * 16 ? 4 : 1;
+}
+
+inline int sell_grid(const SellMat &S)
+{
+    return (int)ceil_div((int64_t)S.nslices * sell_split(S), NTHREADS / 32);
+}
+
+int Op::spmv_grid() const { return sell ? sell_grid(*S) : vec_grid(nchunks()); }
 
 Op make_op(ogb_mtrx *m, bool use_sell)
 {
     Op op;
     if (use_sell) {
+        m->sell.force_split = m->ctx->spmv_split;
         op.sell = true;
         op.S = &m->sell;
         op.n = m->sell.nns();
@@ -656,66 +692,169 @@ Op make_op(ogb_mtrx *m, bool use_sell)
     return op;
 }
 
-template <class V, class X, class ACC, bool DOT, bool DIFF, int ND>
-void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int G, const V *val, const X *x, X *y, double *part,
-                    unsigned int *count, PcgScal *sc)
+// Split form for matrices with few slices per resident warp: SPLIT warps share
+// one slice, warp `part` taking blocks k = part, part + SPLIT, ... (each load
+// still a coalesced 128-byte warp load); the parts are added in part order
+// through shared memory by the slice's first warp. More, shorter work units
+// keep every SM busy to the end instead of a nearly empty last wave. The sum
+// order differs from the one-warp forms, so the split is chosen by a fixed
+// rule on the slice count (never by timing) and results stay reproducible.
+template <int ND, class V, class X, class ACC, bool DOT, bool DIFF, int SPLIT>
+__global__ void __launch_bounds__(NTHREADS) k_sell_spmv_split(int nslices, const int64_t *__restrict__ sl_ptr,
+                                                              const int *__restrict__ sl_width,
+                                                              const int *__restrict__ col, const V *__restrict__ val,
+                                                              const X *__restrict__ x, X *__restrict__ y,
+                                                              double *part, unsigned int *count, PcgScal *sc)
 {
-    switch (G) {
-    case 1:
-        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 1><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
-                                                                        val, x, y, part, count, sc);
-        break;
-    case 2:
-        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 2><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
-                                                                        val, x, y, part, count, sc);
-        break;
-    default:
-        k_sell_spmv<ND, V, X, ACC, DOT, DIFF, 4><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p,
-                                                                        val, x, y, part, count, sc);
-        break;
+    if (DOT && halted(sc)) return;
+    constexpr int WARPS = NTHREADS / 32, SPB = WARPS / SPLIT;
+    __shared__ ACC red[WARPS][ND][32];
+    const int warp = threadIdx.x >> 5, r = threadIdx.x & 31;
+    const int q = warp % SPLIT;
+    const int s = blockIdx.x * SPB + warp / SPLIT;
+    ACC yy[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) yy[i] = 0;
+    if (s < nslices) {
+        const int64_t base = sl_ptr[s];
+        const int w = sl_width[s];
+        const int arow = s * 32 + r;
+        ACC xa[ND];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) xa[i] = DIFF ? (ACC)x[(int64_t)arow * ND + i] : (ACC)0;
+        const V *vp = val + base * (ND * ND) + r;
+        const int *cp = col + base + r;
+#pragma unroll 2
+        for (int k = q; k < w; k += SPLIT) {
+            const int c = __ldcs(cp + 32 * k);
+            ACC xb[ND];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+                xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
+                if (DIFF && c != arow) xb[j] -= xa[j];
+            }
+            const V *vk = vp + (int64_t)k * (32 * ND * ND);
+#pragma unroll
+            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
+        }
     }
+#pragma unroll
+    for (int i = 0; i < ND; ++i) red[warp][i][r] = yy[i];
+    __syncthreads();
+    double dot = 0.0;
+    if (q == 0 && s < nslices) {
+        const int64_t a = (int64_t)s * 32 + r;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            ACC t = red[warp][i][r];
+#pragma unroll
+            for (int p = 1; p < SPLIT; ++p) t += red[warp + p][i][r];
+            y[a * ND + i] = (X)t;
+            if (DOT) dot += (double)x[a * ND + i] * (double)t;
+        }
+    }
+    if (!DOT) return;
+    double acc[1] = {dot};
+    block_sum<1>(acc);
+    if (publish_partials<1>(acc, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], count, sc);
+    }
+}
+
+// SELL SpMV loop variants (one warp per slice, the same sum order): 1 = plain
+// unrolled loop, 2 / 3 = block columns prefetched in groups of 1 / 4. (Groups of
+// two ran at half the speed of both on GB300 and are not offered.)
+constexpr int SPMV_VARIANTS = 3;
+template <class V, class X, class ACC, bool DOT, bool DIFF, int ND>
+void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int variant, const V *val, const X *x, X *y,
+                    double *part, unsigned int *count, PcgScal *sc)
+{
+#define OGB_SELL(G_)                                                                                              \
+    k_sell_spmv<ND, V, X, ACC, DOT, DIFF, G_><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, \
+                                                                     val, x, y, part, count, sc)
+    switch (variant) {
+    case 1: OGB_SELL(0); break;
+    case 2: OGB_SELL(1); break;
+    default: OGB_SELL(4); break;
+    }
+#undef OGB_SELL
 }
 
 template <class V, class X, class ACC, bool DOT, bool DIFF>
 void launch_sell(cudaStream_t s, int g, const SellMat &S, int G, const V *val, const X *x, X *y, double *part,
                  unsigned int *count, PcgScal *sc)
 {
-    if (S.nd == 3) launch_sell_nd<V, X, ACC, DOT, DIFF, 3>(s, g, S, G, val, x, y, part, count, sc);
-    else launch_sell_nd<V, X, ACC, DOT, DIFF, 2>(s, g, S, G, val, x, y, part, count, sc);
+    (void)g;
+    const int split = sell_split(S), grid = sell_grid(S);
+#define OGB_SPLIT(ND_, SP_)                                                                                     \
+    k_sell_spmv_split<ND_, V, X, ACC, DOT, DIFF, SP_><<<grid, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, \
+                                                                                S.col.p, val, x, y, part, count, sc)
+    if (split == 2) {
+        if (S.nd == 3) OGB_SPLIT(3, 2);
+        else OGB_SPLIT(2, 2);
+        return;
+    }
+    if (split == 4) {
+        if (S.nd == 3) OGB_SPLIT(3, 4);
+        else OGB_SPLIT(2, 4);
+        return;
+    }
+#undef OGB_SPLIT
+    if (S.nd == 3) launch_sell_nd<V, X, ACC, DOT, DIFF, 3>(s, grid, S, G, val, x, y, part, count, sc);
+    else launch_sell_nd<V, X, ACC, DOT, DIFF, 2>(s, grid, S, G, val, x, y, part, count, sc);
 }
 
-// Prefetch group of the SELL SpMV for value type V: the context's forced
-// choice, else the matrix's tuned one (4 until tuned).
+// SELL SpMV variant for value type V: the context's forced choice, else the
+// matrix's tuned one (the plain loop until tuned).
 template <class V>
 int sell_group(const ogb_ctx *ctx, const SellMat &S)
 {
     if (ctx->spmv_group) return ctx->spmv_group;
-    const int g = S.group[sizeof(V) == 4 ? 1 : 0];
-    return g ? g : 4;
+    const int v = S.group[sizeof(V) == 4 ? 1 : 0];
+    return v ? v : 1;
 }
 
-// Autotuner: times the SpMV of this matrix and value type with prefetch groups
-// 1, 2 and 4 (three launches each after one warm-up, CUDA events on the
-// context stream) and keeps the fastest. Runs once per matrix structure and
+// Autotuner: times every SELL SpMV variant of this matrix and value type in the
+// form the solve launches (fused p.q, on scratch scalars `sc`, whose `done`
+// must be 0) -- one warm-up and three timed launches each, CUDA events on the
+// context stream -- and keeps the fastest. Runs once per matrix structure and
 // value type, outside graph capture; x and y are scratch vectors.
 template <class V, class X, class ACC, bool DIFF>
-int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y)
+int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double *part, unsigned int *count,
+                  PcgScal *sc)
 {
     if (!op.sell || ctx->spmv_group) return OGB_OK;
     SellMat &S = const_cast<SellMat &>(*op.S);
     int &slot = S.group[sizeof(V) == 4 ? 1 : 0];
     if (slot) return OGB_OK;
+    if (sell_split(S) > 1) {   // the split form has one loop variant
+        slot = 1;
+        return OGB_OK;
+    }
     cudaStream_t s = ctx->stream;
     const int g = op.spmv_grid();
+    OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
     cudaEvent_t e0, e1;
     OGB_CUDA(cudaEventCreate(&e0));
     OGB_CUDA(cudaEventCreate(&e1));
     float best = 0.f;
-    int best_g = 4;
-    for (int G : {1, 2, 4}) {
-        launch_sell<V, X, ACC, false, DIFF>(s, g, S, G, val, x, y, nullptr, nullptr, nullptr);
+    int best_v = 1;
+    for (int v = 1; v <= SPMV_VARIANTS; ++v) {
+        // the scratch scalars are cleared before every launch: an epilogue that
+        // met p.q <= 0 on the scratch vectors would otherwise mark them done and
+        // turn the following launches into no-ops
+        cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
+        launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc);
         cudaEventRecord(e0, s);
-        for (int k = 0; k < 3; ++k) launch_sell<V, X, ACC, false, DIFF>(s, g, S, G, val, x, y, nullptr, nullptr, nullptr);
+        for (int k = 0; k < 3; ++k) {
+            cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
+            launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc);
+        }
         cudaEventRecord(e1, s);
         count_launch(ctx, 4);
         cudaError_t e = cudaEventSynchronize(e1);
@@ -726,14 +865,14 @@ int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y)
             cudaEventDestroy(e1);
             return cuda_fail(e, "SpMV autotune");
         }
-        if (G == 1 || ms < best) {
+        if (v == 1 || ms < best) {
             best = ms;
-            best_g = G;
+            best_v = v;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    slot = best_g;
+    slot = best_v;
     return OGB_OK;
 }
 
@@ -899,7 +1038,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
     PcgScal *sc = m->w_scal.p;
     double *r = m->w_r.p, *z = m->w_z.p, *p = m->w_p.p, *q = m->w_q.p, *dinv = m->w_dinv.p;
     OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
-    OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, val, p, q)));
+    OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc + 1)));
     OGB_CHECK((launch_diag_inv<double, double>(ctx, op, val, dinv, sc)));
     OGB_CHECK((apply_op<double, double, false>(ctx, op, val, x, q, nullptr, nullptr, nullptr)));
     k_pcg_init<double><<<g, NTHREADS, 0, s>>>(nch, b, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol);
@@ -970,9 +1109,8 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
     OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
     const bool diff = op.sell && ctx->mixed_diff;
-    if (diff) OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q)));
-    else OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q)));
-    OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, v64, x, q64)));
+    if (diff) OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+    else OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
     int iters = 0, replacements = 0, status = OGB_E_NOTCONV;
     double achieved = 0.0;
     bool first = true;

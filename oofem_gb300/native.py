@@ -32,7 +32,7 @@ OPT_MIXED_ORTH = 3
 OPT_MIXED_DROP_PPM = 4
 OPT_MIXED_P32 = 5
 OPT_MIXED_X64 = 6
-OPT_SPMV_GROUP = 7
+OPT_SPMV_VARIANT = 7
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
@@ -94,6 +94,8 @@ SIGNATURES = {
     "ogb_model_gp_state": (_i, [_vp, _vp]),
     "ogb_model_reset_state": (_i, [_vp]),
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
+    "ogb_batch_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
+    "ogb_batch_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
@@ -447,6 +449,21 @@ class GpuModel:
                                            C.byref(it))
         _check(code)
         return u, reac, it.value
+
+    def batch_nonlinear_step(self, A: GpuCsrMtrx, bc_value, nodal_load=None, rtolf=1e-8, maxiter=50,
+                             lin_rtol=1e-12, precision=PREC_FP64):
+        """One NonLinearStatic step of every instance; returns (u_node, reactions,
+        newton_iterations per instance)."""
+        bcv = np.ascontiguousarray(bc_value, dtype=np.float64)
+        ld = None if nodal_load is None else np.ascontiguousarray(nodal_load, dtype=np.float64)
+        u = np.zeros_like(bcv)
+        reac = np.zeros_like(bcv)
+        its = np.zeros(getattr(self, "_ninst", 1), np.int32)
+        code = self.lib.ogb_batch_nonlinear_step(self.h, A.h, _ptr(bcv), _ptr(ld) if ld is not None else None,
+                                                 rtolf, maxiter, lin_rtol, precision, _ptr(u), _ptr(reac),
+                                                 _ptr(its))
+        _check(code)
+        return u, reac, its
 
     def close(self):
         if self.h:
