@@ -144,8 +144,10 @@ def cpu_sample(iters_full: int, nfree_full: int, nelem_full: int, nnz_full: int)
     t_elem = t_asm / sm.nelem
     t_nnz_it = t_cg / (n_it * ci.size)
     t_full = t_elem * nelem_full + t_nnz_it * nnz_full * iters_full
-    return {"value": nfree_full / t_full, "unit": "DOF/s", "cores": 1, "kind": "port",
-            "sample": (f"oracle (serial C restatement) on a 58x12x12 cantilever ({neq} DOFs): "
+    nth = O.threads()
+    return {"value": nfree_full / t_full, "unit": "DOF/s", "cores": nth, "kind": "port",
+            "sample": (f"oracle (C restatement; element loop on {nth} OpenMP threads, CG single-threaded as "
+                       f"the reference's IML CG) on a 58x12x12 cantilever ({neq} DOFs): "
                        f"pattern+assembly {t_elem * 1e6:.1f} us/element, CG {t_nnz_it * 1e9:.3f} ns/nnz/iteration "
                        f"({n_it} iterations); scaled to {nelem_full} elements, {nnz_full} nnz and the "
                        f"{iters_full} FP64 PCG iterations the full workload needs to 1e-8"),
@@ -558,6 +560,75 @@ def run_gpu_newton(args):
     print(json.dumps(out))
 
 
+def run_gpu_idm1_batch(args):
+    """Damage on tets, a batch of seeds: unit cube of n^3 cells x 6 LTRSpace tets
+    per seed (nodes jittered +-0.15h, seed-dependent), IsotropicDamageMaterial1
+    (E 30e9, nu 0.2, e0 1e-4, gf 100), z = 0 fixed, z = 1 pulled to 4 e0 over 20
+    increments; the batch takes the first `--idm-steps` increments (the pre-peak
+    part, before the softening steps that need hundreds of Newton iterations) as
+    batched NonLinearStatic steps, each seed with its own NRSolver test (rtolf
+    1e-6), linear systems by mixed-precision batched PCG to 1e-8.
+    value = free DOFs of all seeds x steps / time."""
+    import torch
+    from oofem_gb300 import meshgen as mg, native
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    n, nseed, nsteps, run = args.cube_n, args.seeds, 20, args.idm_steps
+    mat = mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=100.0)
+    meshes = [mg.tet_cube(n, jitter=0.15, seed=100 * rank + k, material=mat, end_disp=4e-4) for k in range(nseed)]
+    big, ns = mg.concat_meshes(meshes)
+    nfree = big.nfree
+    ctx = native.Context(local)
+    model = native.GpuModel(ctx, big)
+    model.set_instances(ns)
+    A = native.GpuCsrMtrx(ctx)
+    model.build_matrix(A)
+
+    def analysis():
+        model.reset_state()
+        its = []
+        for k in range(1, run + 1):
+            _, _, it = model.batch_nonlinear_step(A, big.bc_value * (k / nsteps), None, rtolf=1e-6, maxiter=400,
+                                                  lin_rtol=1e-8, precision=native.PREC_MIXED)
+            its.append(it.tolist())
+        return its
+
+    model.batch_nonlinear_step(A, big.bc_value * (1.0 / nsteps), None, rtolf=1e-6, maxiter=400, lin_rtol=1e-8,
+                               precision=native.PREC_MIXED)   # warm-up
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = ctx.kernel_launches()
+    t0 = time.perf_counter()
+    its = analysis()
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = ctx.kernel_launches() - l0
+    cb = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        sm = mg.tet_cube(4, jitter=0.15, seed=1, material=mat, end_disp=4e-4)
+        t0 = time.perf_counter()
+        O.nonlinear_static(O.mesh_dict(sm), [float(k) for k in range(1, run + 1)], float(nsteps), 1e-6, 400)
+        tc = time.perf_counter() - t0
+        cb = {"value": sm.nfree * run / tc, "unit": "DOF/s", "cores": 1, "kind": "port",
+              "sample": f"oracle NonLinearStatic/NRSolver (serial C + numpy, direct solves) on one 4^3-cell cube "
+                        f"({sm.nfree} DOFs), same material and the same {run} increments"}
+    out = {
+        "metric": METRIC, "value": nfree * run / secs, "unit": "DOF/s", "n_gpus": 1, "steps": run,
+        "warmup": 1, "ms_per_step": 1e3 * secs / run, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "config": {"workload": f"idm1_tet_cube_{n}_x{nseed}_seeds_first_{run}_of_{nsteps}_increments",
+                   "free_dofs": nfree, "elements": big.nelem, "rtolf": 1e-6, "lin_rtol": 1e-8,
+                   "precision": "FP64 damage update and residual, mixed FP32 batched PCG"},
+        "newton_iterations_per_seed": its, "clocks": clk, "gpu_launches": int(launches),
+        "timing": "host wall clock around the analysis (device synchronized)", "cpu_baseline": cb,
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -569,7 +640,11 @@ def main():
     ap.add_argument("--nx", type=int, default=0, help="profiling only: smaller cantilever")
     ap.add_argument("--ny", type=int, default=0)
     ap.add_argument("--nz", type=int, default=0)
-    ap.add_argument("--workload", default="cantilever", choices=["cantilever", "rve_batch", "mises_block"])
+    ap.add_argument("--workload", default="cantilever",
+                    choices=["cantilever", "rve_batch", "mises_block", "idm1_batch"])
+    ap.add_argument("--cube-n", type=int, default=40)
+    ap.add_argument("--seeds", type=int, default=8)
+    ap.add_argument("--idm-steps", type=int, default=16)
     ap.add_argument("--rve-count", type=int, default=256)
     ap.add_argument("--spmv-variant", type=int, default=0,
                     help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
@@ -582,6 +657,8 @@ def main():
         run_gpu_batch(args)
     elif args.workload == "mises_block":
         run_gpu_newton(args)
+    elif args.workload == "idm1_batch":
+        run_gpu_idm1_batch(args)
     else:
         run_gpu(args)
 

@@ -10,6 +10,10 @@
  */
 #include "oofem_oracle.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -795,29 +799,55 @@ void oro_internal_forces(int etype, int ndim, int nnodes, const double *coords, 
     (void)nl;
 }
 
+/* Threads of the element loop (the reference runs its element loops with OpenMP,
+ * engngm.C:900-929, and adds every element matrix inside a critical section). */
+int oro_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 void oro_assemble_tangent(int etype, int ndim, int nnodes, const double *coords, int nelem,
                           const int *conn, const int *elem_mat, const double *mats,
                           double thickness, const double *state, int nloc, const int *loc,
                           int neq, const int64_t *rowptr, const int *colind, double *val)
 {
     (void)nnodes;
-    int ng = oro_ngp(etype), ns = oro_nstress(etype);
-    double xe[24], D[8 * 36], Ke[576];
+    const int ng = oro_ngp(etype), ns = oro_nstress(etype);
+    /* element matrices of a chunk in parallel, then added in element order: the
+     * result does not depend on the thread count */
+    enum { CH = 2048 };
+    double *kb = (double *)malloc((size_t)CH * 576 * sizeof(double));
     memset(val, 0, (size_t)rowptr[neq] * sizeof(double));
-    for (int e = 0; e < nelem; ++e) {
-        oro_gather_element(etype, ndim, coords, conn, e, xe);
-        const double *mat = mats + 8 * elem_mat[e];
-        for (int g = 0; g < ng; ++g) {
-            const double *st = state ? state + ((size_t)e * ng + g) * ORO_NSTATE : NULL;
-            double zero[ORO_NSTATE] = {0};
-            oro_material_tangent(etype, mat, st ? st : zero, D + (size_t)g * ns * ns);
+    for (int e0 = 0; e0 < nelem; e0 += CH) {
+        const int ne = nelem - e0 < CH ? nelem - e0 : CH;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int k = 0; k < ne; ++k) {
+            const int e = e0 + k;
+            double xe[24], D[8 * 36];
+            oro_gather_element(etype, ndim, coords, conn, e, xe);
+            const double *mat = mats + 8 * elem_mat[e];
+            for (int g = 0; g < ng; ++g) {
+                const double *st = state ? state + ((size_t)e * ng + g) * ORO_NSTATE : NULL;
+                double zero[ORO_NSTATE] = {0};
+                oro_material_tangent(etype, mat, st ? st : zero, D + (size_t)g * ns * ns);
+            }
+            oro_elem_stiffness(etype, xe, D, 1, thickness, 1, kb + (size_t)k * 576);
         }
-        oro_elem_stiffness(etype, xe, D, 1, thickness, 1, Ke);
-        const int *l = loc + (size_t)e * nloc;
-        for (int j = 0; j < nloc; ++j) {
-            if (!l[j]) continue;
-            for (int i = 0; i < nloc; ++i)
-                if (l[i]) csr_add(rowptr, colind, val, l[i] - 1, l[j] - 1, Ke[i * nloc + j]);
+        for (int k = 0; k < ne; ++k) {
+            const double *Ke = kb + (size_t)k * 576;
+            const int *l = loc + (size_t)(e0 + k) * nloc;
+            for (int j = 0; j < nloc; ++j) {
+                if (!l[j]) continue;
+                for (int i = 0; i < nloc; ++i)
+                    if (l[i]) csr_add(rowptr, colind, val, l[i] - 1, l[j] - 1, Ke[i * nloc + j]);
+            }
         }
     }
+    free(kb);
 }

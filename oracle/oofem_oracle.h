@@ -28,6 +28,7 @@
 extern "C" {
 #endif
 
+int  oro_threads(void);
 int  oro_nnpe(int etype);
 int  oro_ndofpn(int etype);
 int  oro_ngp(int etype);

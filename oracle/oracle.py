@@ -36,6 +36,11 @@ def lib():
     return _lib
 
 
+def threads() -> int:
+    """OpenMP threads of the oracle's element loops (1 when built without OpenMP)."""
+    return int(lib().oro_threads())
+
+
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 

@@ -8,7 +8,8 @@ from conftest import ROOT
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "oofem_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "oofem_gb300.h")) as fh:
+        src = fh.read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(ogb_[a-z0-9_]+)\s*\(", src)))
 

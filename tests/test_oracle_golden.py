@@ -57,7 +57,8 @@ def test_linear_static(case, oracle):
 
 def test_patch300_reference_deck(oracle):
     """LTRSpace compression patch test, exact solution from tests/sm/patch300.in."""
-    rules = json.load(open(os.path.join(GOLDEN, "patch300.json")))
+    with open(os.path.join(GOLDEN, "patch300.json")) as fh:
+        rules = json.load(fh)
     coords = np.array([[0, 0, 0], [3, 0, 0], [0, 3, 0], [0, 0, 6], [3, 0, 6], [0, 3, 6]], float)
     conn = np.array([[1, 2, 3, 4], [4, 5, 2, 3], [4, 6, 5, 3]], np.int32) - 1
     bc = np.zeros((6, 3), np.uint8)

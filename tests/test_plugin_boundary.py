@@ -29,8 +29,10 @@ def test_plugin_registers_through_the_class_factory(tmp_path, native_lib):
     assert r.returncode == 0, r.stderr
     deck = str(tmp_path / "gpu.in")
     write_deck(mg.hex_cantilever(4, 2, 2), deck, "LinearStatic nsteps 1 smtype 11 lstype 9 lstol 1e-10 lsiter 1000")
-    text = open(deck).read().replace("nmodules 1", "nmodules 0").replace("refdump tstep_all\n", "")
-    open(deck, "w").write(text)
+    with open(deck) as fh:
+        text = fh.read().replace("nmodules 1", "nmodules 0").replace("refdump tstep_all\n", "")
+    with open(deck, "w") as fh:
+        fh.write(text)
     env = dict(os.environ)
     env["LD_PRELOAD"] = os.path.join(ROOT, "oracle", "_ref", "liboofem_gb300_plugin.so")
     env["LD_LIBRARY_PATH"] = REF_BUILD + ":" + os.path.join(ROOT, "oofem_gb300")

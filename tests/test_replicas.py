@@ -33,7 +33,7 @@ def test_two_gloo_ranks_combine_max_time_and_total_work():
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
     world = 2
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:   # no fork of this (threaded) process
         out = mgr.dict()
         mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
