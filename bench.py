@@ -516,7 +516,7 @@ def run_gpu_newton(args):
             _, _, nite = model.nonlinear_step(A, mesh.bc_value * (k / nsteps), None, rtolf=1e-8, maxiter=50,
                                               lin_rtol=1e-8, precision=prec)
             nites.append(nite)
-        return nites
+        return nites, model.solver_stats()
 
     analysis(native.PREC_MIXED)   # warm-up: autotuning, graph capture, allocations
     torch.cuda.synchronize()
@@ -524,13 +524,13 @@ def run_gpu_newton(args):
     clocks.start()
     l0 = ctx.kernel_launches()
     t0 = time.perf_counter()
-    nites = analysis(native.PREC_MIXED)
+    nites, lin = analysis(native.PREC_MIXED)
     torch.cuda.synchronize()
     secs = time.perf_counter() - t0
     launches = ctx.kernel_launches() - l0
     clk = clocks.stop()
     t0 = time.perf_counter()
-    nites64 = analysis(native.PREC_FP64)
+    nites64, lin64 = analysis(native.PREC_FP64)
     torch.cuda.synchronize()
     secs64 = time.perf_counter() - t0
     cb = None
@@ -551,8 +551,9 @@ def run_gpu_newton(args):
         "config": {"workload": f"mises_block_{nx}x{ny}x{nz}_10_increments", "free_dofs": nfree,
                    "elements": mesh.nelem, "rtolf": 1e-8, "lin_rtol": 1e-8,
                    "precision": "FP64 radial return and residual, mixed FP32 PCG + FP64 refinement"},
-        "newton_iterations": nites, "fp64": {"value": nfree * nsteps / secs64, "seconds": secs64,
-                                             "newton_iterations": nites64},
+        "newton_iterations": nites, "linear_solves": lin[0], "pcg_iterations": lin[1],
+        "fp64": {"value": nfree * nsteps / secs64, "seconds": secs64, "newton_iterations": nites64,
+                 "linear_solves": lin64[0], "pcg_iterations": lin64[1]},
         "mixed_over_fp64": secs64 / secs, "clocks": clk, "gpu_launches": int(launches),
         "timing": "host wall clock around the 10-step analysis (device synchronized)",
         "cpu_baseline": cb,

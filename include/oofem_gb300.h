@@ -237,6 +237,10 @@ OGB_API int ogb_model_reset_state(ogb_model *md);
  * prescribed values since the last converged step through the tangent of that
  * state (EngngModel::assemblePrescribedExtrapolatedForces, engngm.C:1614-1666). */
 OGB_API int ogb_model_set_initial_guess(ogb_model *md, int type);
+/* Linear solves of the Newton drivers since the model was created or reset, and
+ * their PCG iterations (summed over instances for batched steps). Instrumentation,
+ * no reference counterpart. */
+OGB_API int ogb_model_solver_stats(ogb_model *md, int64_t *solves, int64_t *iterations);
 /* One NonLinearStatic step with NRSolver in full Newton mode
  * (NonLinearStatic::proceedStep nlinearstatic.C:453-565 with controlmode 1,
  * stiffmode 0, no initial guess; NRSolver::solve nrsolver.C:204-402 with

@@ -881,8 +881,17 @@ int ogb_model_reset_state(ogb_model *md)
     if (md->nr_X.p) OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, md->nr_X.n * sizeof(double), s));
     if (md->nr_bcprev.p) OGB_CUDA(cudaMemsetAsync(md->nr_bcprev.p, 0, md->nr_bcprev.n * sizeof(double), s));
     if (md->nrb_X.p) OGB_CUDA(cudaMemsetAsync(md->nrb_X.p, 0, md->nrb_X.n * sizeof(double), s));
+    md->lin_solves = md->lin_iters = 0;
     if (md->state.p) OGB_CUDA(cudaMemsetAsync(md->state.p, 0, md->state.n * sizeof(double), s));
     OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_model_solver_stats(ogb_model *md, int64_t *solves, int64_t *iterations)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (solves) *solves = md->lin_solves;
+    if (iterations) *iterations = md->lin_iters;
     return OGB_OK;
 }
 

@@ -250,6 +250,7 @@ struct ogb_model {
     ogb::DBuf<double> nr_X, nr_part, nr_out;
     ogb::DBuf<double> nr_bcprev, nr_du;   // prescribed values of the last converged step; increment
     int initial_guess = 0;                 // NonLinearStatic initialGuess: 0 IG_None, 1 IG_Tangent
+    int64_t lin_solves = 0, lin_iters = 0;  // linear solves of the Newton drivers and their PCG iterations
     ogb::DBuf<unsigned int> nr_count;
     ogb::HBuf<double> h_nr_out;
 };

@@ -302,6 +302,8 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
         count_launch(ctx);
         OGB_CUDA(cudaGetLastError());
         int r = solve(m, lin_rtol, 1000000, precision, &last);
+        md->lin_solves++;
+        md->lin_iters += last.iterations;
         if (r != OGB_OK) {
             if (iterations) *iterations = 0;
             return r;
@@ -354,6 +356,8 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
         if (nite > 0) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
         OGB_CUDA(cudaMemsetAsync(m->w_x.p, 0, (size_t)m->npad * sizeof(double), s));
         int r = solve(m, lin_rtol, 1000000, precision, &last);
+        md->lin_solves++;
+        md->lin_iters += last.iterations;
         if (r != OGB_OK) {
             if (iterations) *iterations = nite;
             return r;
@@ -437,6 +441,8 @@ int nonlinear_step_batch(ogb_model *md, ogb_mtrx *m, const double *bcval, const 
         OGB_CUDA(cudaMemsetAsync(md->nrb_x.p, 0, nv * sizeof(double), s));
         int r = batch_pcg(m, 1, md->nrb_b.p, md->nrb_x.p, lin_rtol, 1000000, precision, pit.data(), pac.data(),
                           pst.data());
+        md->lin_solves++;
+        for (int i = 0; i < ninst; ++i) md->lin_iters += pit[i];
         if (r != OGB_OK) return r;
         k_nrb_add<<<nblk(nv), NTHREADS, 0, s>>>(nv, md->nrb_X.p, md->nrb_x.p);
         count_launch(ctx);

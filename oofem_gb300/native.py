@@ -94,6 +94,7 @@ SIGNATURES = {
     "ogb_model_gp_state": (_i, [_vp, _vp]),
     "ogb_model_reset_state": (_i, [_vp]),
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
+    "ogb_model_solver_stats": (_i, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ogb_batch_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_batch_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
@@ -431,6 +432,12 @@ class GpuModel:
 
     def reset_state(self):
         _check(self.lib.ogb_model_reset_state(self.h))
+
+    def solver_stats(self):
+        """(linear solves, PCG iterations) of the Newton drivers since creation / reset."""
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib.ogb_model_solver_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_initial_guess(self, kind: int):
         """NonLinearStatic initialguess: 0 IG_None, 1 IG_Tangent."""
