@@ -130,9 +130,6 @@ struct SellMat {
     DBuf<int64_t> sl_ptr;   // nslices+1
     DBuf<int> sl_width;     // blocks per row of each slice
     DBuf<int> col;          // nslots
-    DBuf<short> col16;      // nslots: column - first row of the slice, for compact slices
-    DBuf<unsigned char> sl_wide;   // 1: the slice's columns need 32 bits (col), 0: col16
-    double col_bytes = 4.0; // mean column bytes per block the SpMV reads
     DBuf<int64_t> diag;     // slot of the diagonal block of each row (nslices*32)
     DBuf<double> v64;       // nslots * ND*ND
     DBuf<float> v32;

@@ -656,35 +656,6 @@ __global__ void k_fill_sell(int nrows_pad, int nact, const int *rownode, const i
     for (; kk < w; ++kk) col[base + (int64_t)kk * 32 + r] = a < nact ? a : a;   // zero-valued padding slots
 }
 
-// 16-bit column offsets: one warp per slice; the slice is compact when every
-// block column lies within +-32767 rows of its first row (padding slots hold the
-// row itself). Counts compact slots for the byte accounting.
-__global__ void k_compact_cols(int nslices, const int64_t *sl_ptr, const int *sl_width, const int *col, short *col16,
-                               unsigned char *sl_wide, unsigned long long *compact_slots)
-{
-    const int s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    const int r = threadIdx.x & 31;
-    if (s >= nslices) return;
-    const int64_t base = sl_ptr[s];
-    const int w = sl_width[s];
-    const int first = s * 32;
-    bool fits = true;
-    for (int k = 0; k < w; ++k) {
-        const int d = col[base + (int64_t)k * 32 + r] - first;
-        fits = fits && d >= -32767 && d <= 32767;
-    }
-    const bool compact = __all_sync(0xffffffffu, fits);
-    if (compact)
-        for (int k = 0; k < w; ++k) {
-            const int64_t slot = base + (int64_t)k * 32 + r;
-            col16[slot] = (short)(col[slot] - first);
-        }
-    if (r == 0) {
-        sl_wide[s] = compact ? 0 : 1;
-        if (compact) atomicAdd(compact_slots, (unsigned long long)w * 32ull);
-    }
-}
-
 __global__ void k_ns_of_eq(int nnodes, int ndofpn, const int *eq, const int *act, int *ns_of_eq)
 {
     int A = blockIdx.x * blockDim.x + threadIdx.x;
@@ -768,22 +739,11 @@ int build_sell(ogb_model *md, ogb_mtrx *m)
         k_fill_sell<2><<<nblk(nrows_pad), NTHREADS, 0, st>>>(nrows_pad, S.nact, rownode.p, md->nb_ptr.p, md->nb_col.p,
                                                              md->act.p, S.sl_ptr.p, S.sl_width.p, S.col.p, S.diag.p,
                                                              md->blk_slot.p, S.v64.p, S.v32.p);
-    OGB_CHECK(S.col16.alloc(nslots));
-    OGB_CHECK(S.sl_wide.alloc(nslices));
-    DBuf<unsigned long long> ncompact;
-    OGB_CHECK(ncompact.alloc(1));
-    OGB_CUDA(cudaMemsetAsync(ncompact.p, 0, sizeof(unsigned long long), st));
-    k_compact_cols<<<(unsigned)ceil_div(nslices, NTHREADS / 32), NTHREADS, 0, st>>>(
-        nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.col16.p, S.sl_wide.p, ncompact.p);
     OGB_CHECK(S.ns_of_eq.alloc(md->neq > 0 ? md->neq : 1));
     k_ns_of_eq<<<nblk(nn), NTHREADS, 0, st>>>(nn, nd, md->eq.p, md->act.p, S.ns_of_eq.p);
-    count_launch(ctx, 3);
-    unsigned long long h_compact = 0;
-    OGB_CUDA(cudaMemcpyAsync(&h_compact, ncompact.p, sizeof(h_compact), cudaMemcpyDeviceToHost, st));
+    count_launch(ctx, 2);
     OGB_CUDA(cudaGetLastError());
     OGB_CUDA(cudaStreamSynchronize(st));   // the temporaries above are freed on return
-    S.col_bytes = nslots ? (2.0 * (double)h_compact + 4.0 * (double)(nslots - (int64_t)h_compact)) / (double)nslots
-                         : 4.0;
     S.v32_version = -1;
     m->has_sell = true;
     return OGB_OK;

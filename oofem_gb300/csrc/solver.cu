@@ -102,76 +102,9 @@ __global__ void __launch_bounds__(NTHREADS) k_spmv(int nchunks, const int64_t *_
 // and the product is (K x)_A = sum_{B != A} K_AB (x_B - x_A) + S_A x_A, which is
 // K x exactly but keeps the products small for smooth fields, so FP32 storage
 // loses far less on the near-rigid modes that decide CG convergence.
-// Block columns of a slice: 32-bit node rows, or (compact slices, every
-// neighbour within +-32767 rows of the slice's first row) 16-bit offsets from
-// that row -- half the column bytes of the stream.
-template <class C>
-__device__ __forceinline__ int sell_col(const C *cp, int k, int cbase)
-{
-    return cbase + (int)__ldcs(cp + 32 * k);
-}
-
-// Products of one lane's row over blocks k = k0, k0 + step, ... (G = 0: plain
-// loop unrolled by four; G > 0: block columns of the next G blocks loaded while
-// the current group's gathers and products run).
-template <int ND, class V, class X, class ACC, bool DIFF, int G, class C>
-__device__ __forceinline__ void sell_row(const C *__restrict__ cp, int cbase, int w, const V *__restrict__ vp,
-                                         const X *__restrict__ x, int arow, const ACC (&xa)[ND], ACC (&yy)[ND])
-{
-    if constexpr (G == 0) {
-#pragma unroll 4
-        for (int k = 0; k < w; ++k) {
-            const int c = sell_col(cp, k, cbase);
-            ACC xb[ND];
-#pragma unroll
-            for (int j = 0; j < ND; ++j) {
-                xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
-                if (DIFF && c != arow) xb[j] -= xa[j];
-            }
-            const V *vk = vp + (int64_t)k * (32 * ND * ND);
-#pragma unroll
-            for (int i = 0; i < ND; ++i)
-#pragma unroll
-                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
-        }
-    } else {
-        int cn[G];
-#pragma unroll
-        for (int g = 0; g < G; ++g) cn[g] = g < w ? sell_col(cp, g, cbase) : arow;
-        for (int k0 = 0; k0 < w; k0 += G) {
-            int cc[G];
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                cc[g] = cn[g];
-                cn[g] = k0 + G + g < w ? sell_col(cp, k0 + G + g, cbase) : arow;
-            }
-            ACC xb[G][ND];
-#pragma unroll
-            for (int g = 0; g < G; ++g)
-#pragma unroll
-                for (int j = 0; j < ND; ++j) {
-                    xb[g][j] = (ACC)__ldg(x + (int64_t)cc[g] * ND + j);
-                    if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
-                }
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (k0 + g < w) {
-                    const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
-#pragma unroll
-                    for (int i = 0; i < ND; ++i)
-#pragma unroll
-                        for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[g][j];
-                }
-            }
-        }
-    }
-}
-
 template <int ND, class V, class X, class ACC, bool DOT, bool DIFF, int G>
 __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64_t *__restrict__ sl_ptr,
                                                         const int *__restrict__ sl_width, const int *__restrict__ col,
-                                                        const short *__restrict__ col16,
-                                                        const unsigned char *__restrict__ sl_wide,
                                                         const V *__restrict__ val, const X *__restrict__ x,
                                                         X *__restrict__ y, double *part, unsigned int *count,
                                                         PcgScal *sc)
@@ -196,11 +129,55 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
             yy[i] = 0;
             xa[i] = DIFF ? (ACC)x[(int64_t)arow * ND + i] : (ACC)0;
         }
-        const V *vp = val + base * (ND * ND) + r;   // values and columns are streamed once: evict first
-        if (sl_wide[s])
-            sell_row<ND, V, X, ACC, DIFF, G>(col + base + r, 0, w, vp, x, arow, xa, yy);
-        else
-            sell_row<ND, V, X, ACC, DIFF, G>(col16 + base + r, s * 32, w, vp, x, arow, xa, yy);
+        const V *vp = val + base * (ND * ND) + r;
+        const int *cp = col + base + r;   // values and columns are streamed once: evict first
+        if constexpr (G == 0) {
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const int c = __ldcs(cp + 32 * k);
+                ACC xb[ND];
+#pragma unroll
+                for (int j = 0; j < ND; ++j) {
+                    xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
+                    if (DIFF && c != arow) xb[j] -= xa[j];
+                }
+                const V *vk = vp + (int64_t)k * (32 * ND * ND);
+#pragma unroll
+                for (int i = 0; i < ND; ++i)
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
+            }
+        } else {
+            int cn[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
+            for (int k0 = 0; k0 < w; k0 += G) {
+                int cc[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    cc[g] = cn[g];
+                    cn[g] = k0 + G + g < w ? __ldcs(cp + 32 * (k0 + G + g)) : arow;
+                }
+                ACC xb[G][ND];
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) {
+                        xb[g][j] = (ACC)__ldg(x + (int64_t)cc[g] * ND + j);
+                        if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
+                    }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (k0 + g < w) {
+                        const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[g][j];
+                    }
+                }
+            }
+        }
         const int64_t a = (int64_t)s * 32 + r;
 #pragma unroll
         for (int i = 0; i < ND; ++i) {
@@ -722,34 +699,10 @@ Op make_op(ogb_mtrx *m, bool use_sell)
 // keep every SM busy to the end instead of a nearly empty last wave. The sum
 // order differs from the one-warp forms, so the split is chosen by a fixed
 // rule on the slice count (never by timing) and results stay reproducible.
-template <int ND, class V, class X, class ACC, bool DIFF, int SPLIT, class C>
-__device__ __forceinline__ void sell_part(const C *__restrict__ cp, int cbase, int q, int w, const V *__restrict__ vp,
-                                          const X *__restrict__ x, int arow, const ACC (&xa)[ND], ACC (&yy)[ND])
-{
-#pragma unroll 2
-    for (int k = q; k < w; k += SPLIT) {
-        const int c = sell_col(cp, k, cbase);
-        ACC xb[ND];
-#pragma unroll
-        for (int j = 0; j < ND; ++j) {
-            xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
-            if (DIFF && c != arow) xb[j] -= xa[j];
-        }
-        const V *vk = vp + (int64_t)k * (32 * ND * ND);
-#pragma unroll
-        for (int i = 0; i < ND; ++i)
-#pragma unroll
-            for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
-    }
-}
-
 template <int ND, class V, class X, class ACC, bool DOT, bool DIFF, int SPLIT>
 __global__ void __launch_bounds__(NTHREADS) k_sell_spmv_split(int nslices, const int64_t *__restrict__ sl_ptr,
                                                               const int *__restrict__ sl_width,
-                                                              const int *__restrict__ col,
-                                                              const short *__restrict__ col16,
-                                                              const unsigned char *__restrict__ sl_wide,
-                                                              const V *__restrict__ val,
+                                                              const int *__restrict__ col, const V *__restrict__ val,
                                                               const X *__restrict__ x, X *__restrict__ y,
                                                               double *part, unsigned int *count, PcgScal *sc)
 {
@@ -770,10 +723,22 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv_split(int nslices, const
 #pragma unroll
         for (int i = 0; i < ND; ++i) xa[i] = DIFF ? (ACC)x[(int64_t)arow * ND + i] : (ACC)0;
         const V *vp = val + base * (ND * ND) + r;
-        if (sl_wide[s])
-            sell_part<ND, V, X, ACC, DIFF, SPLIT>(col + base + r, 0, q, w, vp, x, arow, xa, yy);
-        else
-            sell_part<ND, V, X, ACC, DIFF, SPLIT>(col16 + base + r, s * 32, q, w, vp, x, arow, xa, yy);
+        const int *cp = col + base + r;
+#pragma unroll 2
+        for (int k = q; k < w; k += SPLIT) {
+            const int c = __ldcs(cp + 32 * k);
+            ACC xb[ND];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+                xb[j] = (ACC)__ldg(x + (int64_t)c * ND + j);
+                if (DIFF && c != arow) xb[j] -= xa[j];
+            }
+            const V *vk = vp + (int64_t)k * (32 * ND * ND);
+#pragma unroll
+            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) yy[i] += (ACC)__ldcs(vk + 32 * (i * ND + j)) * xb[j];
+        }
     }
 #pragma unroll
     for (int i = 0; i < ND; ++i) red[warp][i][r] = yy[i];
@@ -811,7 +776,7 @@ void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int variant, const 
 {
 #define OGB_SELL(G_)                                                                                              \
     k_sell_spmv<ND, V, X, ACC, DOT, DIFF, G_><<<g, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, \
-                                                                     S.col16.p, S.sl_wide.p, val, x, y, part, count, sc)
+                                                                     val, x, y, part, count, sc)
     switch (variant) {
     case 1: OGB_SELL(0); break;
     case 2: OGB_SELL(1); break;
@@ -828,8 +793,7 @@ void launch_sell(cudaStream_t s, int g, const SellMat &S, int G, const V *val, c
     const int split = sell_split(S), grid = sell_grid(S);
 #define OGB_SPLIT(ND_, SP_)                                                                                     \
     k_sell_spmv_split<ND_, V, X, ACC, DOT, DIFF, SP_><<<grid, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, \
-                                                                                S.col.p, S.col16.p, S.sl_wide.p, val, x, y, \
-                                                                                part, count, sc)
+                                                                                S.col.p, val, x, y, part, count, sc)
     if (split == 2) {
         if (S.nd == 3) OGB_SPLIT(3, 2);
         else OGB_SPLIT(2, 2);
@@ -925,7 +889,7 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
         launch_sell<V, X, ACC, DOT, DIFF>(s, g, S, sell_group<V>(ctx, S), val, x, y, part, count, sc);
         // algorithmic bytes: every stored value and block column once (the SELL
         // padding slots are not counted), x once and y once
-        bytes = (double)op.nzt * sizeof(V) + (double)op.nzt / (S.nd * S.nd) * S.col_bytes +
+        bytes = (double)op.nzt * sizeof(V) + (double)op.nzt / (S.nd * S.nd) * sizeof(int) +
                 (double)op.n * sizeof(X) * 2;
     } else {
         const int nch = op.nchunks();
