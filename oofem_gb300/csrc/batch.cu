@@ -30,10 +30,11 @@ namespace {
 
 struct BatchScal {
     double bnorm2, rho, pq, rnorm2, alpha, beta;
-    int done;    // 0 running, 1 converged, 2 breakdown, 3 zero pivot, 4 iteration limit
+    double mark;   // mixed precision: FP64 residual^2 at the last halving
+    int done;      // 0 running, 1 converged, 2 breakdown, 3 zero pivot, 4 iteration limit, 5 stalled (mixed)
     int iters;
-    int pause;   // mixed precision: waits for the next FP64 residual replacement
-    int pad_;
+    int pause;     // mixed precision: waits for the next FP64 residual replacement
+    int since;     // mixed precision: replacements since the FP64 residual last halved
 };
 
 constexpr int UNIT = NTHREADS;               // scalar rows per vector block
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
         BatchScal &q = sc[inst * NR + c];
         if (!pair_running<NR>(q)) continue;
         q.pq = t[c];
-        if (!(t[c] > 0.0) || !isfinite(t[c])) q.done = 2;
+        if (!(t[c] > 0.0) || !isfinite(t[c])) q.done = sizeof(V) == 4 ? 5 : 2;   // FP32: the FP64 pass takes over
         else q.alpha = q.rho / t[c];
     }
 }
@@ -394,14 +395,27 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
         if (init) {
             s.bnorm2 = t[c];
             s.iters = 0;
+            s.mark = t[NR + c];
+            s.since = 0;
         }
         double normb = sqrt(s.bnorm2);
         if (normb == 0.0) normb = 1.0;
         s.rnorm2 = t[NR + c];
         const double rz = t[2 * NR + c];
+        // stagnation: six replacements without halving the FP64 residual, or an
+        // FP32 breakdown, hand the pair to the FP64 pass
+        if (!init) {
+            if (t[NR + c] < 0.25 * s.mark) {
+                s.mark = t[NR + c];
+                s.since = 0;
+            } else {
+                ++s.since;
+            }
+        }
         if (sqrt(t[NR + c]) / normb <= rtol) s.done = 1;
-        else if (!isfinite(t[NR + c]) || !isfinite(rz) || !(rz > 0.0)) s.done = 2;
+        else if (!isfinite(t[NR + c])) s.done = 2;
         else if (s.iters >= maxit) s.done = 4;
+        else if (!isfinite(rz) || !(rz > 0.0) || s.since >= 6) s.done = 5;
         else {
             s.rho = rz;
             s.pause = 0;
@@ -459,7 +473,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
         double normb = sqrt(s.bnorm2);
         if (normb == 0.0) normb = 1.0;
         const double half = 0.5 * rtol * normb;
-        if (!isfinite(t[c]) || !isfinite(t[NR + c])) s.done = 2;
+        if (!isfinite(t[c]) || !isfinite(t[NR + c])) s.done = 5;
         else if (t[c] <= half * half || !(t[NR + c] > 0.0) || s.iters >= maxit) s.pause = 1;
         else {
             s.beta = t[NR + c] / s.rho;
@@ -723,20 +737,42 @@ int batch_pcg(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, in
     int r = OGB_E_ARG;
     const int nd = m->sell.nd;
 #define OGB_BATCH_CASE(ND_, NR_) \
-    if (nd == ND_ && nrhs == NR_) r = run_batch<ND_, NR_>(m, b, x, rtol, maxit, mixed, res);
-    OGB_BATCH_CASE(3, 1) OGB_BATCH_CASE(3, 2) OGB_BATCH_CASE(3, 3) OGB_BATCH_CASE(3, 4)
-    OGB_BATCH_CASE(2, 1) OGB_BATCH_CASE(2, 2) OGB_BATCH_CASE(2, 3) OGB_BATCH_CASE(2, 4)
+    if (nd == ND_ && nrhs == NR_) r = run_batch<ND_, NR_>(m, b, x, rtol, maxit, mx, out);
+    auto run = [&](bool mx, std::vector<BatchScal> &out) {
+        OGB_BATCH_CASE(3, 1) OGB_BATCH_CASE(3, 2) OGB_BATCH_CASE(3, 3) OGB_BATCH_CASE(3, 4)
+        OGB_BATCH_CASE(2, 1) OGB_BATCH_CASE(2, 2) OGB_BATCH_CASE(2, 3) OGB_BATCH_CASE(2, 4)
+    };
 #undef OGB_BATCH_CASE
+    run(mixed, res);
     if (r != OGB_OK) return r;
+    bool stalled = false;
+    int used = 0;
+    for (const auto &q : res) {
+        stalled = stalled || q.done == 5;
+        used = q.iters > used ? q.iters : used;
+    }
+    if (stalled && used < maxit) {
+        // pairs the FP32 operator cannot bring to the tolerance continue from their
+        // current solution in an FP64 pass; converged pairs stop at its first test
+        std::vector<BatchScal> res64;
+        run(false, res64);
+        if (r != OGB_OK) return r;
+        for (size_t k = 0; k < res.size(); ++k)
+            if (res[k].done == 5) {
+                const int it = res[k].iters;
+                res[k] = res64[k];
+                res[k].iters += it;
+            }
+    }
     int worst = OGB_OK;
     for (size_t k = 0; k < res.size(); ++k) {
         const BatchScal &s = res[k];
         double normb = sqrt(s.bnorm2);
         if (normb == 0.0) normb = 1.0;
-        const int code = s.done == 1   ? OGB_OK
-                         : s.done == 2 ? OGB_E_BREAKDOWN
-                         : s.done == 3 ? OGB_E_ZERODIAG
-                                       : OGB_E_NOTCONV;
+        const int code = s.done == 1                 ? OGB_OK
+                         : s.done == 2 || s.done == 5 ? OGB_E_BREAKDOWN
+                         : s.done == 3               ? OGB_E_ZERODIAG
+                                                     : OGB_E_NOTCONV;
         if (iters) iters[k] = s.iters;
         if (achieved) achieved[k] = sqrt(s.rnorm2) / normb;
         if (status) status[k] = code;

@@ -114,7 +114,7 @@ struct PcgScal {
     int done;         // 1 converged, 2 breakdown, 3 zero diagonal, 4 max iterations
     int iters;
     int reliable;     // mixed: an FP64 residual replacement is due
-    int pad_;
+    int cycle_end;    // mixed: iteration count at which the current cycle ends at the latest
 };
 
 // Node-block SELL-32 storage: rows = active nodes (>= 1 free DOF) in node

@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__res
         if (!isfinite(t[0]) || !isfinite(t[1])) {
             sc->done = 2;
         } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 ||
-                   !(t[1] > 0.0) || sc->iters >= maxit) {
+                   !(t[1] > 0.0) || sc->iters >= maxit || sc->iters >= sc->cycle_end) {
             sc->reliable = 1;
         } else {
             sc->beta = t[1] / sc->rho;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const d
                                                             X *__restrict__ r, X *__restrict__ z,
                                                             const P *__restrict__ p, const X *__restrict__ dinv,
                                                             double *part, unsigned int *count, PcgScal *sc, int first,
-                                                            int orth)
+                                                            int orth, int cycle_cap)
 {
     double v[3] = {0, 0, 0};
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
@@ -371,6 +371,9 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const d
             sc->rho = t[1];
         }
         sc->reliable = 0;
+        // a cycle whose recursive residual no longer falls tenfold still ends
+        // after cycle_cap iterations, so the FP64 residual is looked at again
+        sc->cycle_end = sc->iters + cycle_cap;
     }
 }
 
@@ -424,7 +427,8 @@ __global__ void __launch_bounds__(NTHREADS) k_update4(int64_t n, double *__restr
         if (MIXED) {
             if (!isfinite(t[0]) || !isfinite(t[1])) {
                 sc->done = 2;
-            } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit) {
+            } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
+                       sc->iters >= sc->cycle_end) {
                 sc->reliable = 1;
                 return;
             }
@@ -520,7 +524,8 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
         sc->iters += 1;
         if (!isfinite(t[0]) || !isfinite(t[1])) {
             sc->done = 2;
-        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit) {
+        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
+                       sc->iters >= sc->cycle_end) {
             sc->reliable = 1;
         } else {
             sc->beta = t[1] / sc->rho;
@@ -1082,7 +1087,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
 // FP32 and the SpMV multiplies and accumulates in FP32.
 template <class X, class P>
 int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v32, const double *b, double *x,
-                   double rtol, int maxit, ogb_solve_info *info)
+                   double rtol, int maxit, ogb_solve_info *info, bool *stalled)
 {
     ogb_ctx *ctx = m->ctx;
     cudaStream_t s = ctx->stream;
@@ -1111,7 +1116,9 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     const bool diff = op.sell && ctx->mixed_diff;
     if (diff) OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
     else OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
-    int iters = 0, replacements = 0, status = OGB_E_NOTCONV;
+    int iters = 0, replacements = 0, status = OGB_E_NOTCONV, since_mark = 0, longest = 0;
+    double mark = INFINITY;
+    *stalled = false;
     double achieved = 0.0;
     bool first = true;
     PcgScal res{};
@@ -1159,6 +1166,18 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
         if (achieved <= rtol) { status = OGB_OK; break; }
         if (!isfinite(achieved)) { status = OGB_E_BREAKDOWN; break; }
         if (iters >= maxit) break;
+        // stagnation: the FP32 operator no longer brings the FP64 residual down
+        // (six replacement cycles without halving it, or a breakdown of the
+        // FP32 recurrences); the caller finishes the solve in FP64
+        if (!(achieved < 0.5 * mark)) {
+            if (++since_mark >= 6 || replacements > 400) {
+                *stalled = true;
+                break;
+            }
+        } else {
+            mark = achieved;
+            since_mark = 0;
+        }
         if (first) {
             // the recursive residual below half the target asks for an FP64 check
             double th[2] = {0.25 * rtol * rtol * normb * normb, ctx->mixed_drop * ctx->mixed_drop};
@@ -1166,8 +1185,10 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             OGB_CUDA(cudaStreamSynchronize(s));
         }
         // replacement: r = r64, z = D^-1 r, beta; then p = z + beta p
+        // cycle cap: unbounded for the first cycle, then twice the longest cycle so far (at least 512)
+        const int cap = first ? (maxit < (1 << 29) ? maxit : (1 << 29)) : (2 * longest > 512 ? 2 * longest : 512);
         k_mixed_replace<X, P><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
-                                                     first ? 1 : 0, ctx->mixed_orth ? 1 : 0);
+                                                     first ? 1 : 0, ctx->mixed_orth ? 1 : 0, cap);
         k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
         count_launch(ctx, 2);
         first = false;
@@ -1184,9 +1205,13 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
                 OGB_CHECK(batch());
             }
         }
+        longest = res.iters - iters > longest ? res.iters - iters : longest;
         iters = res.iters;
         if (res.done == 3) { status = OGB_E_ZERODIAG; break; }
-        if (res.done == 2) { status = OGB_E_BREAKDOWN; break; }
+        if (res.done == 2) {   // FP32 recurrences broke down: finish in FP64
+            *stalled = true;
+            break;
+        }
         if constexpr (F32) {
             if (!ctx->mixed_x64) {
                 // fold the FP32 increment into the FP64 solution
@@ -1194,7 +1219,6 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
                 count_launch(ctx);
             }
         }
-        if (replacements > 400) break;
     }
     if (info) {
         info->iterations = iters;
@@ -1315,12 +1339,26 @@ int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, o
     const double *bo;
     double *xo;
     OGB_CHECK(to_op_space(m, op, b, x, &bo, &xo));
+    ogb_solve_info mi{};
+    bool stalled = false;
     if (m->ctx->mixed_vec32)
-        OGB_CHECK((pcg_mixed_core<float, float>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
+        OGB_CHECK((pcg_mixed_core<float, float>(m, op, v64, v32, bo, xo, rtol, maxit, &mi, &stalled)));
     else if (m->ctx->mixed_p32)
-        OGB_CHECK((pcg_mixed_core<double, float>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
+        OGB_CHECK((pcg_mixed_core<double, float>(m, op, v64, v32, bo, xo, rtol, maxit, &mi, &stalled)));
     else
-        OGB_CHECK((pcg_mixed_core<double, double>(m, op, v64, v32, bo, xo, rtol, maxit, info)));
+        OGB_CHECK((pcg_mixed_core<double, double>(m, op, v64, v32, bo, xo, rtol, maxit, &mi, &stalled)));
+    if (stalled && mi.status != OGB_OK && mi.iterations < maxit) {
+        // the FP32 operator cannot reach this tolerance on this matrix: continue
+        // from the current solution with the FP64 drop-in PCG (same test on ||b||)
+        PcgScal res{};
+        OGB_CHECK(pcg64_core(m, op, v64, bo, xo, rtol, maxit - mi.iterations, res));
+        double normb = sqrt(res.bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        mi.iterations += res.iters;
+        mi.achieved = sqrt(res.rnorm2) / normb;
+        mi.status = map_status(res.done);
+    }
+    if (info) *info = mi;
     OGB_CHECK(from_op_space(m, op, x));
     return OGB_OK;
 }

@@ -197,3 +197,22 @@ def test_solve_multi_matches_single_solves(ctx, native_lib, oracle):
     assert mixed.solve_multi(A, B, X3) == 0
     assert (mixed.last_multi[1] <= 1e-10).all()
     assert rel(X3, X) < 1e-6
+
+
+def test_batch_mixed_below_fp32_reach_finishes_in_fp64(ctx, native_lib):
+    """Mixed batch at 1e-13: pairs whose FP64 residual stops falling under the
+    FP32 operator finish in an FP64 pass from their current solution; every pair
+    converges and agrees with the FP64 batch."""
+    from oofem_gb300 import meshgen as mg
+    meshes = mg.rve_batch(3, seed=9, side_min=10, side_max=30)
+    big, ns = mg.concat_meshes(meshes)
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
+    out = {}
+    for prec in (native_lib.PREC_FP64, native_lib.PREC_MIXED):
+        model = native_lib.GpuModel(ctx, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(ctx)
+        u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-13, precision=prec)
+        assert (st == 0).all(), (prec, st)
+        out[prec] = u
+    assert rel(out[native_lib.PREC_MIXED], out[native_lib.PREC_FP64]) < 1e-9

@@ -241,3 +241,18 @@ def test_sell_and_csr_operators_agree(ctx, native_lib, oracle):
     assert s.solve(A, b, x2) == 0
     assert abs(s.last.iterations - it1) <= 2
     assert rel(x1, x2) < 1e-9
+
+
+def test_mixed_precision_below_fp32_reach_finishes_in_fp64(ctx, native_lib):
+    """A tolerance the FP32 operator cannot reach (1e-13): the mixed solve detects
+    that the FP64 residual stopped falling and finishes with the FP64 PCG from its
+    current solution; the result converges and matches the FP64 solve."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(24, 5, 5, jitter=0.2, seed=2)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    u64, r64, i64 = model.linear_static(A, rtol=1e-13, precision=native_lib.PREC_FP64)
+    um, rm, im = model.linear_static(A, rtol=1e-13, precision=native_lib.PREC_MIXED)
+    assert i64.status == 0 and im.status == 0
+    assert im.achieved <= 1e-13
+    assert rel(um, u64) < 1e-9
