@@ -96,9 +96,11 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
 #define OGB_OPT_MIXED_X64 6
 /*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
- *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 / 5 = each slice shared by
- *   2 / 4 warps; 0 (default) = warps per slice from the slice count, loop form
- *   timed once per matrix and value type by the built-in autotuner. */
+ *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 = values and columns
+ *   staged through shared memory by bulk asynchronous copies (FP32 values; FP64
+ *   uses form 3), 5 / 6 = each slice shared by 2 / 4 warps; 0 (default) = warps
+ *   per slice from the slice count, loop form timed once per matrix and value
+ *   type by the built-in autotuner. */
 #define OGB_OPT_SPMV_VARIANT 7
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)

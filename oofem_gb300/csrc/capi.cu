@@ -48,6 +48,7 @@ int check_device_status(ogb_ctx *ctx, const char *where)
     case DS_LIMIT: return fail(OGB_E_LIMIT, w + ": a per-node/per-row capacity was exceeded");
     case DS_PATTERN: return fail(OGB_E_PATTERN, w + ": location outside the sparsity pattern");
     case DS_NEGVOL: return fail(OGB_E_MESH, w + ": negative volume (tetrahedron with detJ <= 0)");
+    case DS_TIMEOUT: return fail(OGB_E_CUDA, w + ": a bulk copy into shared memory did not complete in time");
     }
     return fail(OGB_E_STATE, w + ": device error");
 }
@@ -354,9 +355,9 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
     case OGB_OPT_MIXED_P32: ctx->mixed_p32 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_X64: ctx->mixed_x64 = value != 0; return OGB_OK;
     case OGB_OPT_SPMV_VARIANT:
-        if (value < 0 || value > 5) return fail(OGB_E_ARG, "SpMV variant must be 0 (tuned) or 1..5");
-        ctx->spmv_group = value >= 4 ? 1 : (int)value;
-        ctx->spmv_split = value == 0 ? 0 : value == 4 ? 2 : value == 5 ? 4 : 1;
+        if (value < 0 || value > 6) return fail(OGB_E_ARG, "SpMV variant must be 0 (tuned) or 1..6");
+        ctx->spmv_group = value >= 5 ? 1 : (int)value;
+        ctx->spmv_split = value == 0 ? 0 : value == 5 ? 2 : value == 6 ? 4 : 1;
         return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");

@@ -97,6 +97,7 @@ enum DevStatus : int {
     DS_LIMIT = 1,      // a fixed per-row / per-node capacity was exceeded
     DS_PATTERN = 2,    // an assembled location is missing from the pattern
     DS_NEGVOL = 3,     // tetrahedron with detJ <= 0 (fei3dtetlin.C:146)
+    DS_TIMEOUT = 4,    // an asynchronous copy did not complete within the wait limit
 };
 
 // Per-system PCG scalars (one record per right-hand side / instance).

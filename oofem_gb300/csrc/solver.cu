@@ -771,10 +771,165 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv_split(int nslices, const
     }
 }
 
+// ---- SELL SpMV with the value and column stream staged by the Tensor Memory
+// Accelerator: every warp owns one slice and a TMA_NS-stage shared-memory ring;
+// lane 0 issues one bulk copy (cp.async.bulk) of the next TMA_KC blocks' values
+// and one of their block columns into a free stage, completing on that stage's
+// mbarrier, while the warp computes from the stage that has landed. The copies
+// keep many bytes in flight without registers; the products are those of the
+// one-warp loop forms, in the same order (identical results). Waits are bounded:
+// a stage that does not land sets DS_TIMEOUT, the warp writes NaN (the solve then
+// stops on a breakdown) and leaves after a bounded wait for its other copies.
+constexpr int TMA_KC = 4, TMA_NS = 2;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bulk global -> shared copy: both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Wait for the phase of `parity` to complete; false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    for (int i = 0; i < (1 << 20); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <int ND>
+__host__ __device__ constexpr int tma_stage_bytes() { return TMA_KC * 32 * (ND * ND * 4 + 4); }
+template <int ND>
+__host__ __device__ constexpr int tma_smem_bytes() { return (NTHREADS / 32) * TMA_NS * (tma_stage_bytes<ND>() + 8); }
+
+template <int ND, class X, bool DOT, bool DIFF>
+__global__ void __launch_bounds__(NTHREADS) k_sell_spmv_tma(int nslices, const int64_t *__restrict__ sl_ptr,
+                                                            const int *__restrict__ sl_width,
+                                                            const int *__restrict__ col,
+                                                            const float *__restrict__ val, const X *__restrict__ x,
+                                                            X *__restrict__ y, double *part, unsigned int *count,
+                                                            PcgScal *sc, int *status)
+{
+    if (DOT && halted(sc)) return;
+    constexpr int VB = TMA_KC * 32 * ND * ND * 4, STAGE = tma_stage_bytes<ND>();
+    extern __shared__ __align__(128) unsigned char tma_smem[];
+    const int warp = threadIdx.x >> 5, r = threadIdx.x & 31;
+    const int s = blockIdx.x * (NTHREADS / 32) + warp;
+    unsigned char *wb = tma_smem + warp * (TMA_NS * STAGE);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(tma_smem + (NTHREADS / 32) * TMA_NS * STAGE) + warp * TMA_NS;
+    double dot = 0.0;
+    if (s < nslices) {
+        const int64_t base = sl_ptr[s];
+        const int w = sl_width[s];
+        const int nch = (w + TMA_KC - 1) / TMA_KC;
+        if (r == 0) {
+            for (int i = 0; i < TMA_NS; ++i) mbar_init(&bars[i], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncwarp();
+        // chunk c: blocks c*KC .. of the slice = one contiguous run of values
+        // (slot groups of 32 x ND*ND floats) and of block columns
+        auto issue = [&](int c) {
+            const int st = c % TMA_NS, kb = min(TMA_KC, w - c * TMA_KC);
+            const int64_t slot0 = base + (int64_t)c * TMA_KC * 32;
+            mbar_expect_tx(&bars[st], (uint32_t)(kb * 32 * (ND * ND * 4 + 4)));
+            bulk_g2s(wb + st * STAGE, val + slot0 * (ND * ND), (uint32_t)(kb * 32 * ND * ND * 4), &bars[st]);
+            bulk_g2s(wb + st * STAGE + VB, col + slot0, (uint32_t)(kb * 32 * 4), &bars[st]);
+        };
+        if (r == 0)
+            for (int c = 0; c < TMA_NS && c < nch; ++c) issue(c);
+        const int arow = s * 32 + r;
+        float yy[ND], xa[ND];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            yy[i] = 0.f;
+            xa[i] = DIFF ? (float)x[(int64_t)arow * ND + i] : 0.f;
+        }
+        uint32_t par = 0;
+        bool ok = true;
+        for (int c = 0; c < nch; ++c) {
+            const int st = c % TMA_NS, kb = min(TMA_KC, w - c * TMA_KC);
+            if (!mbar_wait(&bars[st], (par >> st) & 1u)) {
+                ok = false;
+                break;
+            }
+            par ^= 1u << st;
+            const float *sv = reinterpret_cast<const float *>(wb + st * STAGE);
+            const int *scol = reinterpret_cast<const int *>(wb + st * STAGE + VB);
+#pragma unroll 4
+            for (int kk = 0; kk < kb; ++kk) {
+                const int cc = scol[kk * 32 + r];
+                float xb[ND];
+#pragma unroll
+                for (int j = 0; j < ND; ++j) {
+                    xb[j] = (float)__ldg(x + (int64_t)cc * ND + j);
+                    if (DIFF && cc != arow) xb[j] -= xa[j];
+                }
+#pragma unroll
+                for (int i = 0; i < ND; ++i)
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) yy[i] += sv[kk * 32 * ND * ND + (i * ND + j) * 32 + r] * xb[j];
+            }
+            __syncwarp();
+            if (r == 0 && c + TMA_NS < nch) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(c + TMA_NS);
+            }
+        }
+        if (!ok) {
+            if (r == 0) {
+                atomicCAS(status, DS_OK, DS_TIMEOUT);
+                for (int st = 0; st < TMA_NS; ++st) mbar_wait(&bars[st], (par >> st) & 1u);
+            }
+#pragma unroll
+            for (int i = 0; i < ND; ++i) yy[i] = __int_as_float(0x7fc00000);   // NaN: the solve stops
+        }
+        const int64_t a = (int64_t)s * 32 + r;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            y[a * ND + i] = (X)yy[i];
+            if (DOT) dot += (double)x[a * ND + i] * (double)yy[i];
+        }
+    }
+    if (!DOT) return;
+    double acc[1] = {dot};
+    block_sum<1>(acc);
+    if (publish_partials<1>(acc, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], count, sc);
+    }
+}
+
 // SELL SpMV loop variants (one warp per slice, the same sum order): 1 = plain
 // unrolled loop, 2 / 3 = block columns prefetched in groups of 1 / 4. (Groups of
 // two ran at half the speed of both on GB300 and are not offered.)
-constexpr int SPMV_VARIANTS = 3;
+constexpr int SPMV_VARIANTS = 4;   // 4 = TMA-staged (FP32 values only)
 template <class V, class X, class ACC, bool DOT, bool DIFF, int ND>
 void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int variant, const V *val, const X *x, X *y,
                     double *part, unsigned int *count, PcgScal *sc)
@@ -790,12 +945,34 @@ void launch_sell_nd(cudaStream_t s, int g, const SellMat &S, int variant, const 
 #undef OGB_SELL
 }
 
+template <int ND, class X, bool DOT, bool DIFF>
+void launch_sell_tma(cudaStream_t s, int grid, const SellMat &S, const float *val, const X *x, X *y, double *part,
+                     unsigned int *count, PcgScal *sc, int *status)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sell_spmv_tma<ND, X, DOT, DIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tma_smem_bytes<ND>());
+        attr = true;
+    }
+    k_sell_spmv_tma<ND, X, DOT, DIFF><<<grid, NTHREADS, tma_smem_bytes<ND>(), s>>>(
+        S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y, part, count, sc, status);
+}
+
 template <class V, class X, class ACC, bool DOT, bool DIFF>
 void launch_sell(cudaStream_t s, int g, const SellMat &S, int G, const V *val, const X *x, X *y, double *part,
-                 unsigned int *count, PcgScal *sc)
+                 unsigned int *count, PcgScal *sc, int *status = nullptr)
 {
     (void)g;
     const int split = sell_split(S), grid = sell_grid(S);
+    if constexpr (sizeof(V) == 4 && sizeof(ACC) == 4) {
+        if (G == 4 && split == 1 && status) {
+            if (S.nd == 3) launch_sell_tma<3, X, DOT, DIFF>(s, grid, S, val, x, y, part, count, sc, status);
+            else launch_sell_tma<2, X, DOT, DIFF>(s, grid, S, val, x, y, part, count, sc, status);
+            return;
+        }
+    }
+    if (G == 4) G = 3;   // no TMA form for FP64 values
 #define OGB_SPLIT(ND_, SP_)                                                                                     \
     k_sell_spmv_split<ND_, V, X, ACC, DOT, DIFF, SP_><<<grid, NTHREADS, 0, s>>>(S.nslices, S.sl_ptr.p, S.sl_width.p, \
                                                                                 S.col.p, val, x, y, part, count, sc)
@@ -854,11 +1031,12 @@ int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, do
         // met p.q <= 0 on the scratch vectors would otherwise mark them done and
         // turn the following launches into no-ops
         cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
-        launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc);
+        if (v == 4 && sizeof(V) != 4) break;   // the TMA form exists for FP32 values only
+        launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc, ctx->status.p);
         cudaEventRecord(e0, s);
         for (int k = 0; k < 3; ++k) {
             cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
-            launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc);
+            launch_sell<V, X, ACC, true, DIFF>(s, g, S, v, val, x, y, part, count, sc, ctx->status.p);
         }
         cudaEventRecord(e1, s);
         count_launch(ctx, 4);
@@ -891,7 +1069,7 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
     prof_begin(ctx);
     if (op.sell) {
         const SellMat &S = *op.S;
-        launch_sell<V, X, ACC, DOT, DIFF>(s, g, S, sell_group<V>(ctx, S), val, x, y, part, count, sc);
+        launch_sell<V, X, ACC, DOT, DIFF>(s, g, S, sell_group<V>(ctx, S), val, x, y, part, count, sc, ctx->status.p);
         // algorithmic bytes: every stored value and block column once (the SELL
         // padding slots are not counted), x once and y once
         bytes = (double)op.nzt * sizeof(V) + (double)op.nzt / (S.nd * S.nd) * sizeof(int) +

@@ -3,7 +3,7 @@
     python -m oofem_gb300.spmv_sweep [--sizes 100x20x20,200x40x40,290x58x58]
 
 For each mesh and precision it runs one LinearStatic solve to 1e-8 per form
-(OGB_OPT_SPMV_VARIANT 1..5, and 0 = the library's own choice) after a warm-up
+(OGB_OPT_SPMV_VARIANT 1..6, and 0 = the library's own choice) after a warm-up
 solve, with kernel timing on, and prints one JSON line per run: the step time,
 the PCG iterations and the mean device time and bandwidth of the sampled SpMV
 launches. This is how the split rule and the autotuner's candidate forms in
@@ -17,8 +17,8 @@ import time
 from . import meshgen as mg
 from . import native
 
-FORMS = {1: "plain loop", 2: "prefetch 1", 3: "prefetch 4", 4: "2 warps per slice", 5: "4 warps per slice",
-         0: "library choice"}
+FORMS = {1: "plain loop", 2: "prefetch 1", 3: "prefetch 4", 4: "TMA-staged", 5: "2 warps per slice",
+         6: "4 warps per slice", 0: "library choice"}
 
 
 def sweep(sizes, device=0):
@@ -29,7 +29,7 @@ def sweep(sizes, device=0):
         A = native.GpuCsrMtrx(ctx)
         model.build_matrix(A)
         for prec in (native.PREC_MIXED, native.PREC_FP64):
-            for v in (1, 2, 3, 4, 5, 0):
+            for v in (1, 2, 3, 4, 5, 6, 0):
                 ctx.set_option(native.OPT_SPMV_VARIANT, v)
                 model.linear_static(A, rtol=1e-8, maxit=200000, precision=prec)
                 ctx.profile(True)

@@ -256,3 +256,24 @@ def test_mixed_precision_below_fp32_reach_finishes_in_fp64(ctx, native_lib):
     assert i64.status == 0 and im.status == 0
     assert im.achieved <= 1e-13
     assert rel(um, u64) < 1e-9
+
+
+def test_spmv_forms_give_identical_results(native_lib):
+    """The one-warp SpMV forms (plain loop, prefetching, TMA-staged) compute the
+    same products in the same order: mixed and FP64 solves through each of them
+    give bit-identical displacements and iteration counts."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(30, 6, 6, jitter=0.2, seed=4)
+    out = {}
+    for v in (1, 2, 3, 4):
+        c = native_lib.Context(0)
+        c.set_option(native_lib.OPT_SPMV_VARIANT, v)
+        model = native_lib.GpuModel(c, mesh)
+        A = native_lib.GpuCsrMtrx(c)
+        um, _, im = model.linear_static(A, rtol=1e-10, precision=native_lib.PREC_MIXED)
+        u6, _, i6 = model.linear_static(A, rtol=1e-10, precision=native_lib.PREC_FP64)
+        assert im.status == 0 and i6.status == 0
+        out[v] = (um, im.iterations, u6, i6.iterations)
+    for v in (2, 3, 4):
+        assert np.array_equal(out[v][0], out[1][0]) and out[v][1] == out[1][1], v
+        assert np.array_equal(out[v][2], out[1][2]) and out[v][3] == out[1][3], v
