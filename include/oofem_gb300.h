@@ -105,7 +105,7 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
- * graphs, the first of each replayed 16-iteration batch inside them; ogb_ctx_profile_read
+ * graphs, the ninth of each replayed 16-iteration batch inside them; ogb_ctx_profile_read
  * returns the summed device time (ms), the launch count and the algorithmic
  * bytes of those launches (values + column indices + row pointers + x + y),
  * and resets the counters. No reference counterpart (instrumentation). */
