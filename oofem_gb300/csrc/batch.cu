@@ -37,7 +37,8 @@ struct BatchScal {
     int since;     // mixed precision: replacements since the FP64 residual last halved
 };
 
-constexpr int UNIT = NTHREADS;               // scalar rows per vector block
+constexpr int RPT = 4;                       // scalar rows per thread in the vector kernels
+constexpr int UNIT = RPT * NTHREADS;         // scalar rows per vector block (1024)
 constexpr int SPMV_SLICES = NTHREADS / 32;   // slices (of 32 node rows) per SpMV block
 constexpr int MAXNR = 4;
 constexpr int BBATCH = 16;                   // iterations per captured graph
@@ -203,21 +204,26 @@ __global__ void __launch_bounds__(NTHREADS) k_binit(const double *__restrict__ b
                                                     const int *__restrict__ unit_inst,
                                                     const int64_t *__restrict__ unit_ptr, double rtol)
 {
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
     double v[3 * NR];
-    const double di = dinv[row];
 #pragma unroll
-    for (int c = 0; c < NR; ++c) {
-        const int64_t k = row * NR + c;
-        const double bb = b[k];
-        const double rr = bb - q[k];
-        const double zz = rr * di;
-        r[k] = rr;
-        z[k] = zz;
-        p[k] = zz;
-        v[c] = bb * bb;
-        v[NR + c] = rr * rr;
-        v[2 * NR + c] = rr * zz;
+    for (int k = 0; k < 3 * NR; ++k) v[k] = 0.0;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+        const double di = dinv[row];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            const int64_t k = row * NR + c;
+            const double bb = b[k];
+            const double rr = bb - q[k];
+            const double zz = rr * di;
+            r[k] = rr;
+            z[k] = zz;
+            p[k] = zz;
+            v[c] += bb * bb;
+            v[NR + c] += rr * rr;
+            v[2 * NR + c] += rr * zz;
+        }
     }
     const int inst = unit_inst[blockIdx.x];
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
@@ -255,24 +261,31 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate(double *__restrict__ x, do
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 1)) return;
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
-    const double di = dinv[row];
-    double v[2 * NR];
+    bool run[NR];
+    double alpha[NR], v[2 * NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
+        run[c] = sc[inst * NR + c].done == 0;   // converged pairs keep their solution
+        alpha[c] = sc[inst * NR + c].alpha;
         v[c] = 0.0;
         v[NR + c] = 0.0;
-        const int done = sc[inst * NR + c].done;
-        const double alpha = sc[inst * NR + c].alpha;
-        if (done) continue;   // converged pairs keep their solution
-        const int64_t k = row * NR + c;
-        x[k] = fma(alpha, p[k], x[k]);
-        const double rr = fma(-alpha, q[k], r[k]);
-        const double zz = rr * di;
-        r[k] = rr;
-        z[k] = zz;
-        v[c] = rr * rr;
-        v[NR + c] = rr * zz;
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+        const double di = dinv[row];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            if (!run[c]) continue;
+            const int64_t k = row * NR + c;
+            x[k] = fma(alpha[c], p[k], x[k]);
+            const double rr = fma(-alpha[c], q[k], r[k]);
+            const double zz = rr * di;
+            r[k] = rr;
+            z[k] = zz;
+            v[c] += rr * rr;
+            v[NR + c] += rr * zz;
+        }
     }
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
     block_sum<2 * NR>(v);
@@ -305,14 +318,22 @@ __global__ void __launch_bounds__(NTHREADS) k_bpupdate(const double *__restrict_
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 1)) return;
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
+    bool run[NR];
+    double beta[NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
-        const int done = sc[inst * NR + c].done;
-        const double beta = sc[inst * NR + c].beta;
-        if (done) continue;
-        const int64_t k = row * NR + c;
-        p[k] = fma(beta, p[k], z[k]);
+        run[c] = sc[inst * NR + c].done == 0;
+        beta[c] = sc[inst * NR + c].beta;
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            if (!run[c]) continue;
+            const int64_t k = row * NR + c;
+            p[k] = fma(beta[c], p[k], z[k]);
+        }
     }
 }
 
@@ -359,27 +380,36 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 2)) return;
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
-    const float di = dinv[row];
+    bool live[NR], restart[NR];
     double v[3 * NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
+        const BatchScal &s = sc[inst * NR + c];
+        live[c] = s.done == 0;
+        restart[c] = init || s.pause;
         v[c] = 0.0;
         v[NR + c] = 0.0;
         v[2 * NR + c] = 0.0;
-        const BatchScal &s = sc[inst * NR + c];
-        if (s.done) continue;
-        const int64_t k = row * NR + c;
-        const double bb = b[k];
-        const double r6 = bb - q64[k];
-        const float rf = (float)r6;
-        const float zf = rf * di;
-        r[k] = rf;
-        z[k] = zf;
-        if (init || s.pause) p[k] = zf;
-        v[c] = bb * bb;
-        v[NR + c] = r6 * r6;
-        v[2 * NR + c] = (double)(rf * zf);
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+        const float di = dinv[row];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            if (!live[c]) continue;
+            const int64_t k = row * NR + c;
+            const double bb = b[k];
+            const double r6 = bb - q64[k];
+            const float rf = (float)r6;
+            const float zf = rf * di;
+            r[k] = rf;
+            z[k] = zf;
+            if (restart[c]) p[k] = zf;
+            v[c] += bb * bb;
+            v[NR + c] += r6 * r6;
+            v[2 * NR + c] += (double)(rf * zf);
+        }
     }
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
     block_sum<3 * NR>(v);
@@ -436,25 +466,34 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 1)) return;
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
-    const float di = dinv[row];
+    bool run[NR];
+    double alpha[NR];
     float v[2 * NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
+        const BatchScal &s = sc[inst * NR + c];
+        run[c] = pair_running<NR>(s);
+        alpha[c] = s.alpha;
         v[c] = 0.f;
         v[NR + c] = 0.f;
-        const BatchScal &s = sc[inst * NR + c];
-        if (!pair_running<NR>(s)) continue;
-        const double alpha = s.alpha;
-        const int64_t k = row * NR + c;
-        const float pp = p[k];
-        x[k] = fma(alpha, (double)pp, x[k]);
-        const float rr = fmaf(-(float)alpha, q[k], r[k]);
-        const float zz = rr * di;
-        r[k] = rr;
-        z[k] = zz;
-        v[c] = rr * rr;
-        v[NR + c] = rr * zz;
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+        const float di = dinv[row];
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            if (!run[c]) continue;
+            const int64_t k = row * NR + c;
+            const float pp = p[k];
+            x[k] = fma(alpha[c], (double)pp, x[k]);
+            const float rr = fmaf(-(float)alpha[c], q[k], r[k]);
+            const float zz = rr * di;
+            r[k] = rr;
+            z[k] = zz;
+            v[c] = fmaf(rr, rr, v[c]);
+            v[NR + c] = fmaf(rr, zz, v[NR + c]);
+        }
     }
     const int64_t u0 = unit_ptr[inst], u1 = unit_ptr[inst + 1];
     double bs[2 * NR];
@@ -488,13 +527,23 @@ __global__ void __launch_bounds__(NTHREADS) k_bpupdate32(const float *__restrict
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 1)) return;
-    const int64_t row = (int64_t)blockIdx.x * UNIT + threadIdx.x;
+    bool run[NR];
+    float beta[NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         const BatchScal &s = sc[inst * NR + c];
-        if (!pair_running<NR>(s)) continue;
-        const int64_t k = row * NR + c;
-        p[k] = fmaf((float)s.beta, p[k], z[k]);
+        run[c] = pair_running<NR>(s);
+        beta[c] = (float)s.beta;
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+            if (!run[c]) continue;
+            const int64_t k = row * NR + c;
+            p[k] = fmaf(beta[c], p[k], z[k]);
+        }
     }
 }
 
@@ -547,7 +596,7 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
     std::vector<int> vinst(nvu), sinst(nsu);
     std::vector<int64_t> vptr(ninst + 1), sptr(ninst + 1);
     for (int i = 0; i <= ninst; ++i) {
-        vptr[i] = S.inst_row_base[i] * ND / UNIT;            // 1024 * ND / 256: exact
+        vptr[i] = S.inst_row_base[i] * ND / UNIT;            // 1024 * ND / 1024: exact
         sptr[i] = S.inst_row_base[i] / (32 * SPMV_SLICES);   // 1024 / 256: exact
     }
     for (int i = 0; i < ninst; ++i) {
