@@ -97,6 +97,46 @@ __device__ __forceinline__ bool pair_running(const BatchScal &q)
     return q.done == 0 && q.pause == 0;
 }
 
+// The W entries of one node row of an interleaved vector (W = ND x NR values,
+// the row starting at a multiple of W): 16-byte loads when W is a multiple of 4
+// floats, 8-byte loads when even (the row start is then aligned to them), else
+// single loads -- fewer gather instructions per block.
+template <int W>
+__device__ __forceinline__ void gather_row(const float *__restrict__ src, float (&dst)[W])
+{
+    if constexpr (W % 4 == 0) {
+#pragma unroll
+        for (int j = 0; j < W; j += 4) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(src + j));
+            dst[j] = v.x; dst[j + 1] = v.y; dst[j + 2] = v.z; dst[j + 3] = v.w;
+        }
+    } else if constexpr (W % 2 == 0) {
+#pragma unroll
+        for (int j = 0; j < W; j += 2) {
+            const float2 v = __ldg(reinterpret_cast<const float2 *>(src + j));
+            dst[j] = v.x; dst[j + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < W; ++j) dst[j] = __ldg(src + j);
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void gather_row(const double *__restrict__ src, double (&dst)[W])
+{
+    if constexpr (W % 2 == 0) {
+#pragma unroll
+        for (int j = 0; j < W; j += 2) {
+            const double2 v = __ldg(reinterpret_cast<const double2 *>(src + j));
+            dst[j] = v.x; dst[j + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < W; ++j) dst[j] = __ldg(src + j);
+    }
+}
+
 // q = K p for all right-hand sides: matrix values V, vectors X, products and
 // sums in V. DOT: also p.q per pair (block sums in V per warp, FP64 above) and
 // alpha for running pairs. DIFF: the FP32 difference form (the diagonal slot
@@ -145,12 +185,12 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
             }
             V xb[G][W];
 #pragma unroll
-            for (int g = 0; g < G; ++g)
+            for (int g = 0; g < G; ++g) {
+                gather_row<W>(x + (int64_t)cc[g] * W, xb[g]);
+                if (DIFF && cc[g] != arow)
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                    xb[g][j] = (V)__ldg(x + (int64_t)cc[g] * W + j);
-                    if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
-                }
+                    for (int j = 0; j < W; ++j) xb[g][j] -= xa[j];
+            }
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 if (k0 + g < w) {
