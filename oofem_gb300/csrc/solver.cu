@@ -1048,7 +1048,9 @@ int sell_autotune(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, do
             cudaEventDestroy(e1);
             return cuda_fail(e, "SpMV autotune");
         }
-        if (v == 1 || ms < best) {
+        // a later form must win by 2 % to replace an earlier one: near-ties keep
+        // the simpler form, and the choice does not flip with timing noise
+        if (v == 1 || ms < 0.98f * best) {
             best = ms;
             best_v = v;
         }
