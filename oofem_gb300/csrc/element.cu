@@ -709,12 +709,8 @@ static int run_stiffness(ogb_model *md)
 {
     ogb_ctx *ctx = md->ctx;
     constexpr size_t smem = stiff_smem<ET>(PERGP);
-    static bool attr_set = false;
-    if (!attr_set) {
-        OGB_CUDA(cudaFuncSetAttribute(k_elem_stiffness<ET, PERGP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        attr_set = true;
-    }
+    static bool attr_set[64] = {};
+    OGB_CUDA(set_smem_limit_once((const void *)k_elem_stiffness<ET, PERGP>, (int)smem, attr_set));
     int nb = (int)ceil_div(md->nelem, NTHREADS / ET_<ET>::NPE);
     k_elem_stiffness<ET, PERGP><<<nb, NTHREADS, smem, ctx->stream>>>(
         md->nelem, md->coords.p, md->conn.p, md->emat.p, md->mats.p, md->Dmat.p, md->state.p, md->thickness,
@@ -729,12 +725,8 @@ static int run_forces(ogb_model *md, const double *u_node)
 {
     ogb_ctx *ctx = md->ctx;
     constexpr size_t smem = force_smem<ET>();
-    static bool attr_set = false;
-    if (!attr_set) {
-        OGB_CUDA(cudaFuncSetAttribute(k_elem_internal_forces<ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        attr_set = true;
-    }
+    static bool attr_set[64] = {};
+    OGB_CUDA(set_smem_limit_once((const void *)k_elem_internal_forces<ET>, (int)smem, attr_set));
     double *st = md->nonlinear ? md->state.p : nullptr;
     int nb = (int)ceil_div(md->nelem, NTHREADS / ET_<ET>::NPE);
     k_elem_internal_forces<ET><<<nb, NTHREADS, smem, ctx->stream>>>(

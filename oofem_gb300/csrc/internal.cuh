@@ -260,6 +260,20 @@ namespace ogb {
 
 constexpr int NSTATE = 24;
 
+// Raise a kernel's dynamic shared-memory limit once per device (the attribute
+// belongs to the device the call is made on). `done` is the caller's flag table.
+inline cudaError_t set_smem_limit_once(const void *kernel, int bytes, bool (&done)[64])
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
+}
+
 // --------------------------------------------------------------- launchers
 // scan.cu
 int exclusive_scan_i64(ogb_ctx *ctx, const int64_t *in, int64_t *out, int64_t n, int64_t *total_host);

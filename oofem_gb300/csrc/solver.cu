@@ -949,12 +949,8 @@ template <int ND, class X, bool DOT, bool DIFF>
 void launch_sell_tma(cudaStream_t s, int grid, const SellMat &S, const float *val, const X *x, X *y, double *part,
                      unsigned int *count, PcgScal *sc, int *status)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sell_spmv_tma<ND, X, DOT, DIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tma_smem_bytes<ND>());
-        attr = true;
-    }
+    static bool attr[64] = {};
+    set_smem_limit_once((const void *)k_sell_spmv_tma<ND, X, DOT, DIFF>, tma_smem_bytes<ND>(), attr);
     k_sell_spmv_tma<ND, X, DOT, DIFF><<<grid, NTHREADS, tma_smem_bytes<ND>(), s>>>(
         S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, val, x, y, part, count, sc, status);
 }
