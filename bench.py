@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
+SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -359,7 +360,8 @@ def run_gpu(args):
         "fp64": {"value": nfree / (ms64 * 1e-3), "ms_per_step": ms64, "iterations": infos64[-1].iterations,
                  "achieved": infos64[-1].achieved},
         "mixed_over_fp64": ms64 / ms,
-        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv (node-block SELL-32, FP32 values, difference form, fused p.q)",
+        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv (node-block SELL-32, FP32 values, difference form, fused p.q; "
+                               "form %s)" % SPMV_FORMS.get(A.spmv_forms()[1], "?"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind,

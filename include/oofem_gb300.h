@@ -146,6 +146,10 @@ OGB_API int ogb_mtrx_times_dev(ogb_mtrx *m, const double *x_dev, double *y_dev);
  * (NRSolver::applyConstraintsToStiffness does at(i,i) *= 1e6, nrsolver.C:501-503). */
 OGB_API int ogb_mtrx_at(ogb_mtrx *m, int i, int j, double *value);
 OGB_API int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value);
+/* Node-block SpMV forms in use for this matrix (0 = not tuned yet, or no
+ * node-block copy): the OGB_OPT_SPMV_VARIANT numbers 1..4 chosen for FP64 and
+ * FP32 values, and the warps per slice. Instrumentation, no reference counterpart. */
+OGB_API int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_per_slice);
 /* SparseMtrx::giveVersion (sparsemtrx.h:82): bumped on every mutation. */
 OGB_API int ogb_mtrx_version(ogb_mtrx *m, int64_t *version);
 

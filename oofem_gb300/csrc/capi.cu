@@ -571,6 +571,17 @@ int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value)
     return OGB_OK;
 }
 
+int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_per_slice)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    const bool sell = m->has_sell;
+    if (fp64_form) *fp64_form = sell ? m->sell.group[0] : 0;
+    if (fp32_form) *fp32_form = sell ? m->sell.group[1] : 0;
+    if (warps_per_slice) *warps_per_slice = sell ? (m->sell.force_split ? m->sell.force_split
+                                                    : (m->sell.nslices < NUM_SMS * 16 ? 4 : 1)) : 0;
+    return OGB_OK;
+}
+
 int ogb_mtrx_version(ogb_mtrx *m, int64_t *version)
 {
     if (!m || !version) return fail(OGB_E_ARG, "null argument");

@@ -102,6 +102,7 @@ SIGNATURES = {
     "ogb_linear_static": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_linear_static_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp, C.POINTER(SolveInfo)]),
     "ogb_model_set_instances": (_i, [_vp, _i, _vp]),
+    "ogb_mtrx_spmv_forms": (_i, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ogb_pcg_solve_multi": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp]),
     "ogb_pcg_solve_multi_dev": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp]),
     "ogb_batch_linear_static": (_i, [_vp, _vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _vp, _vp]),
@@ -238,6 +239,12 @@ class GpuCsrMtrx:
 
     def zero(self):
         _check(self.lib.ogb_mtrx_zero(self.h))
+
+    def spmv_forms(self):
+        """(FP64 form, FP32 form, warps per slice) of the node-block SpMV."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.ogb_mtrx_spmv_forms(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def assemble_begin(self):
         _check(self.lib.ogb_mtrx_assemble_begin(self.h))
