@@ -38,3 +38,30 @@ def test_rve_boundary_strain():
     assert np.allclose(m.bc_value[bnd, 0], 5e-4 * m.coords[bnd, 1])
     assert np.allclose(m.bc_value[bnd, 1], 5e-4 * m.coords[bnd, 0])
     assert set(np.unique(m.elem_mat)) <= {0, 1}
+
+
+def test_concat_meshes_offsets_and_materials():
+    from oofem_gb300 import meshgen as mg
+    a = mg.quad_rve(3, seed=1)
+    b = mg.quad_rve(5, seed=2)
+    big, ns = mg.concat_meshes([a, b])
+    assert list(ns) == [0, a.nnodes, a.nnodes + b.nnodes]
+    assert big.nelem == a.nelem + b.nelem
+    assert (big.conn[:a.nelem] == a.conn).all()
+    assert (big.conn[a.nelem:] == b.conn + a.nnodes).all()
+    # materials concatenated, element indices shifted by the first mesh's table
+    assert len(big.materials) == len(a.materials) + len(b.materials)
+    assert (big.elem_mat[a.nelem:] == b.elem_mat + len(a.materials)).all()
+    assert (big.bc_mask[ns[1]:] == b.bc_mask).all()
+    # every element's nodes lie in one instance
+    inst = np.searchsorted(ns, big.conn, side="right") - 1
+    assert (inst == inst[:, :1]).all()
+
+
+def test_rve_batch_is_seeded_and_in_range():
+    from oofem_gb300 import meshgen as mg
+    r1 = mg.rve_batch(6, seed=4, side_min=5, side_max=9)
+    r2 = mg.rve_batch(6, seed=4, side_min=5, side_max=9)
+    sides = [int(round(np.sqrt(m.nelem))) for m in r1]
+    assert all(5 <= n <= 9 for n in sides)
+    assert all((x.coords == y.coords).all() and (x.elem_mat == y.elem_mat).all() for x, y in zip(r1, r2))
