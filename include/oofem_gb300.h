@@ -243,14 +243,39 @@ OGB_API int ogb_model_reset_state(ogb_model *md);
  * prescribed values since the last converged step through the tangent of that
  * state (EngngModel::assemblePrescribedExtrapolatedForces, engngm.C:1614-1666). */
 OGB_API int ogb_model_set_initial_guess(ogb_model *md, int type);
+/* NRSolver's `manrmsteps` (nrsolver.C:120-126 and the re-assembly test at
+ * nrsolver.C:285-290): the tangent is always assembled at the start of a step;
+ * with manrmsteps = k > 0 (accelerated Newton; k = 1 is full Newton, the
+ * default here) it is re-assembled from the current state before the linear
+ * solve of every iteration nite > 0 with nite % k == 0; with 0 (modified Newton,
+ * the reference's default when the key is absent) the start-of-step tangent
+ * serves every iteration of the step. Applies to ogb_nonlinear_step and
+ * ogb_batch_nonlinear_step. */
+OGB_API int ogb_model_set_nr_mode(ogb_model *md, int manrmsteps);
+/* Checkpoint of the analysis state, the device-resident counterpart of the
+ * reference's context files (EngngModel::saveStepContext engngm.C:768-777,
+ * saveContext / restoreContext engngm.C:1755-1850; each material status's saveContext / restoreContext, e.g.
+ * misesmat.C:758-790): the committed Gauss-point state of every element (plastic
+ * strain, kappa, damage, Le, crack direction), the Newton solution of the free
+ * DOFs, the prescribed values of the last converged step (the IG_Tangent
+ * increment starts from them) and the batched Newton solution. A self-describing
+ * byte blob: ogb_model_state_bytes gives its size; ogb_model_save_state writes it
+ * (call between steps: the temp state is not saved); ogb_model_restore_state
+ * loads it into a model of the same mesh and element type (OGB_E_ARG on any
+ * mismatch of the header: element type, node, element, Gauss-point, DOF and
+ * equation counts). Restoring and continuing gives bit-identical steps. */
+OGB_API int ogb_model_state_bytes(ogb_model *md, size_t *bytes);
+OGB_API int ogb_model_save_state(ogb_model *md, void *buf, size_t bytes);
+OGB_API int ogb_model_restore_state(ogb_model *md, const void *buf, size_t bytes);
 /* Linear solves of the Newton drivers since the model was created or reset, and
  * their PCG iterations (summed over instances for batched steps). Instrumentation,
  * no reference counterpart. */
 OGB_API int ogb_model_solver_stats(ogb_model *md, int64_t *solves, int64_t *iterations);
-/* One NonLinearStatic step with NRSolver in full Newton mode
+/* One NonLinearStatic / StaticStructural step with NRSolver
  * (NonLinearStatic::proceedStep nlinearstatic.C:453-565 with controlmode 1,
- * stiffmode 0, no initial guess; NRSolver::solve nrsolver.C:204-402 with
- * manrmsteps 1; NRSolver::checkConvergence nrsolver.C:593-790 with rtolf and DOF
+ * stiffmode 0; StaticStructural::solveYourselfAt staticstructural.C:235-356;
+ * NRSolver::solve nrsolver.C:204-402 in the mode set by ogb_model_set_nr_mode,
+ * the initial guess set by ogb_model_set_initial_guess; NRSolver::checkConvergence nrsolver.C:593-790 with rtolf and DOF
  * grouping). bc_value / nodal_load: this step's total prescribed values and
  * nodal loads (nnodes x ndofpn). The model keeps the free-DOF solution between
  * steps. The linear systems are solved by PCG to lin_rtol in `precision`. On

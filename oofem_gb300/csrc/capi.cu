@@ -899,6 +899,107 @@ int ogb_model_reset_state(ogb_model *md)
     return OGB_OK;
 }
 
+namespace {
+// Header of a state checkpoint; the arrays follow it in this order: GP state,
+// free-DOF Newton solution (neq), last prescribed values (nnodes x ndofpn),
+// batched Newton solution (nrb_len). All doubles.
+struct StateHeader {
+    char magic[8];
+    int32_t format, etype, nnodes, nelem, ngp, ndofpn, neq, nstate;
+    int64_t state_len, nrb_len;
+};
+constexpr char STATE_MAGIC[8] = {'O', 'G', 'B', 'S', 'T', 'A', 'T', 'E'};
+constexpr int32_t STATE_FORMAT = 1;
+
+StateHeader state_header(const ogb_model *md)
+{
+    StateHeader h{};
+    memcpy(h.magic, STATE_MAGIC, 8);
+    h.format = STATE_FORMAT;
+    h.etype = md->etype;
+    h.nnodes = md->nnodes;
+    h.nelem = md->nelem;
+    h.ngp = md->ngp;
+    h.ndofpn = md->ndofpn;
+    h.neq = md->neq;
+    h.nstate = NSTATE;
+    h.state_len = md->state.p ? (int64_t)md->nelem * md->ngp * NSTATE : 0;
+    h.nrb_len = md->nrb_X.p ? (int64_t)md->nrb_X.n : 0;
+    return h;
+}
+
+size_t state_bytes(const StateHeader &h)
+{
+    return sizeof(StateHeader) +
+           sizeof(double) * (size_t)(h.state_len + h.neq + (int64_t)h.nnodes * h.ndofpn + h.nrb_len);
+}
+}  // namespace
+
+int ogb_model_state_bytes(ogb_model *md, size_t *bytes)
+{
+    if (!md || !bytes) return fail(OGB_E_ARG, "null argument");
+    *bytes = state_bytes(state_header(md));
+    return OGB_OK;
+}
+
+int ogb_model_save_state(ogb_model *md, void *buf, size_t bytes)
+{
+    if (!md || !buf) return fail(OGB_E_ARG, "null argument");
+    const StateHeader h = state_header(md);
+    if (bytes < state_bytes(h)) return fail(OGB_E_ARG, "state buffer too small");
+    cudaStream_t s = md->ctx->stream;
+    char *p = static_cast<char *>(buf);
+    memcpy(p, &h, sizeof h);
+    double *d = reinterpret_cast<double *>(p + sizeof h);
+    auto put = [&](const DBuf<double> &src, size_t n) -> int {
+        if (n == 0) return OGB_OK;
+        if (src.p) OGB_CUDA(cudaMemcpyAsync(d, src.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        else memset(d, 0, n * sizeof(double));
+        d += n;
+        return OGB_OK;
+    };
+    OGB_CHECK(put(md->state, (size_t)h.state_len));
+    OGB_CHECK(put(md->nr_X, (size_t)h.neq));
+    OGB_CHECK(put(md->nr_bcprev, (size_t)h.nnodes * h.ndofpn));
+    OGB_CHECK(put(md->nrb_X, (size_t)h.nrb_len));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int ogb_model_restore_state(ogb_model *md, const void *buf, size_t bytes)
+{
+    if (!md || !buf) return fail(OGB_E_ARG, "null argument");
+    if (bytes < sizeof(StateHeader)) return fail(OGB_E_ARG, "state blob shorter than its header");
+    StateHeader h;
+    memcpy(&h, buf, sizeof h);
+    const StateHeader mine = state_header(md);
+    if (memcmp(h.magic, STATE_MAGIC, 8) != 0 || h.format != STATE_FORMAT)
+        return fail(OGB_E_ARG, "not a state checkpoint of this library");
+    if (h.etype != mine.etype || h.nnodes != mine.nnodes || h.nelem != mine.nelem || h.ngp != mine.ngp ||
+        h.ndofpn != mine.ndofpn || h.neq != mine.neq || h.nstate != mine.nstate || h.state_len != mine.state_len)
+        return fail(OGB_E_ARG, "state checkpoint of another mesh or material model");
+    if (h.nrb_len < 0 || bytes < state_bytes(h)) return fail(OGB_E_ARG, "state blob truncated");
+    cudaStream_t s = md->ctx->stream;
+    OGB_CHECK(nr_ensure(md));
+    const double *d = reinterpret_cast<const double *>(static_cast<const char *>(buf) + sizeof h);
+    auto get = [&](DBuf<double> &dst, size_t n) -> int {
+        if (n == 0) return OGB_OK;
+        OGB_CHECK(dst.alloc(n));
+        OGB_CUDA(cudaMemcpyAsync(dst.p, d, n * sizeof(double), cudaMemcpyHostToDevice, s));
+        d += n;
+        return OGB_OK;
+    };
+    OGB_CHECK(get(md->state, (size_t)h.state_len));
+    OGB_CHECK(get(md->nr_X, (size_t)h.neq));
+    OGB_CHECK(get(md->nr_bcprev, (size_t)h.nnodes * h.ndofpn));
+    if (h.nrb_len > 0) {
+        if (md->nrb_X.p && md->nrb_X.n != (size_t)h.nrb_len) md->nrb_X.release();
+        OGB_CHECK(get(md->nrb_X, (size_t)h.nrb_len));
+    }
+    OGB_CUDA(cudaStreamSynchronize(s));   // the blob is the caller's: copies done before return
+    return OGB_OK;
+}
+
 int ogb_model_solver_stats(ogb_model *md, int64_t *solves, int64_t *iterations)
 {
     if (!md) return fail(OGB_E_ARG, "null argument");
@@ -912,6 +1013,14 @@ int ogb_model_set_initial_guess(ogb_model *md, int type)
     if (!md) return fail(OGB_E_ARG, "null argument");
     if (type != 0 && type != 1) return fail(OGB_E_ARG, "initial guess must be 0 (IG_None) or 1 (IG_Tangent)");
     md->initial_guess = type;
+    return OGB_OK;
+}
+
+int ogb_model_set_nr_mode(ogb_model *md, int manrmsteps)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (manrmsteps < 0) return fail(OGB_E_ARG, "manrmsteps < 0");
+    md->nr_manrm = manrmsteps;
     return OGB_OK;
 }
 

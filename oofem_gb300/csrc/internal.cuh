@@ -251,6 +251,7 @@ struct ogb_model {
     ogb::DBuf<double> nr_X, nr_part, nr_out;
     ogb::DBuf<double> nr_bcprev, nr_du;   // prescribed values of the last converged step; increment
     int initial_guess = 0;                 // NonLinearStatic initialGuess: 0 IG_None, 1 IG_Tangent
+    int nr_manrm = 1;                      // NRSolver manrmsteps: 0 modified Newton, k re-assembles when nite % k == 0
     int64_t lin_solves = 0, lin_iters = 0;  // linear solves of the Newton drivers and their PCG iterations
     ogb::DBuf<unsigned int> nr_count;
     ogb::HBuf<double> h_nr_out;
@@ -304,6 +305,7 @@ int extract_diag(ogb_mtrx *m);
 int pick_tpr(const ogb_mtrx *m);
 
 // newton.cu
+int nr_ensure(ogb_model *md);   // Newton work buffers; nr_X and nr_bcprev zeroed on first allocation
 int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf, int maxiter,
                    double lin_rtol, int precision, double *u_node, double *reac, int *iterations,
                    ogb_solve_info *lin_info, int (*assemble)(ogb_model *, ogb_mtrx *),

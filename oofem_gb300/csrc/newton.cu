@@ -261,6 +261,15 @@ int nr_ensure(ogb_model *md)
     return OGB_OK;
 }
 
+// NRSolver's re-assembly test before the linear solve of iteration nite
+// (nrsolver.C:285-290, mCalcStiffBeforeRes on): never at nite 0 (the tangent of
+// the start of the step serves), then every manrmsteps-th iteration; modified
+// Newton (manrmsteps 0) keeps the start-of-step tangent.
+static bool nr_reassemble(const ogb_model *md, int nite)
+{
+    return nite > 0 && md->nr_manrm > 0 && nite % md->nr_manrm == 0;
+}
+
 // One NonLinearStatic step. bcval/load: this step's total prescribed values and
 // nodal loads (device, nnodes*ndofpn). On success the material state is
 // committed; u_node and reac (device, optional) receive the converged field.
@@ -353,7 +362,7 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
             if (iterations) *iterations = nite;
             return fail(OGB_E_NOTCONV, "NRSolver: maximum number of iterations reached without convergence");
         }
-        if (nite > 0) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
+        if (nr_reassemble(md, nite)) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
         OGB_CUDA(cudaMemsetAsync(m->w_x.p, 0, (size_t)m->npad * sizeof(double), s));
         int r = solve(m, lin_rtol, 1000000, precision, &last);
         md->lin_solves++;
@@ -399,6 +408,8 @@ int nonlinear_step_batch(ogb_model *md, ogb_mtrx *m, const double *bcval, const 
     OGB_CHECK(nr_ensure(md));
     OGB_CHECK(md->v_fnode.alloc(n));
     const int64_t nv = m->sell.nns();
+    if (md->nrb_X.p && md->nrb_X.n != (size_t)nv)
+        return fail(OGB_E_STATE, "restored batched Newton solution does not fit this matrix");
     if (!md->nrb_X.p) {
         OGB_CHECK(md->nrb_X.alloc(nv));
         OGB_CUDA(cudaMemsetAsync(md->nrb_X.p, 0, nv * sizeof(double), s));
@@ -511,7 +522,7 @@ int nonlinear_step_batch(ogb_model *md, ogb_mtrx *m, const double *bcval, const 
             else any = true;
         }
         if (status != OGB_OK || !any) break;
-        if (it > 0) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
+        if (nr_reassemble(md, it)) OGB_CHECK(assemble(md, m));   // tangent from the current temp state
         OGB_CHECK(upload_active());
         OGB_CUDA(cudaMemsetAsync(md->nrb_b.p, 0, nv * sizeof(double), s));
         k_nrb_rhs<<<nblk(n), NTHREADS, 0, s>>>(n, nd, md->eq.p, md->act.p, md->d_node_inst.p, md->nrb_active.p, load,

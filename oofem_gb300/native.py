@@ -94,6 +94,10 @@ SIGNATURES = {
     "ogb_model_gp_state": (_i, [_vp, _vp]),
     "ogb_model_reset_state": (_i, [_vp]),
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
+    "ogb_model_set_nr_mode": (_i, [_vp, _i]),
+    "ogb_model_state_bytes": (_i, [_vp, C.POINTER(C.c_size_t)]),
+    "ogb_model_save_state": (_i, [_vp, _vp, C.c_size_t]),
+    "ogb_model_restore_state": (_i, [_vp, _vp, C.c_size_t]),
     "ogb_model_solver_stats": (_i, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ogb_batch_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_batch_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
@@ -449,6 +453,24 @@ class GpuModel:
     def set_initial_guess(self, kind: int):
         """NonLinearStatic initialguess: 0 IG_None, 1 IG_Tangent."""
         _check(self.lib.ogb_model_set_initial_guess(self.h, int(kind)))
+
+    def save_state(self) -> bytes:
+        """Checkpoint of the committed analysis state (GP state, Newton solution,
+        last prescribed values) as bytes; restore_state loads it."""
+        n = C.c_size_t()
+        _check(self.lib.ogb_model_state_bytes(self.h, C.byref(n)))
+        buf = (C.c_char * n.value)()
+        _check(self.lib.ogb_model_save_state(self.h, buf, n.value))
+        return bytes(buf)
+
+    def restore_state(self, blob: bytes):
+        buf = C.create_string_buffer(blob, len(blob))
+        _check(self.lib.ogb_model_restore_state(self.h, buf, len(blob)))
+
+    def set_nr_mode(self, manrmsteps: int):
+        """NRSolver manrmsteps: 0 modified Newton, k > 0 re-assembles the tangent
+        every k-th iteration (1 = full Newton, the default)."""
+        _check(self.lib.ogb_model_set_nr_mode(self.h, int(manrmsteps)))
 
     def nonlinear_step(self, A: GpuCsrMtrx, bc_value, nodal_load=None, rtolf=1e-8, maxiter=50,
                        lin_rtol=1e-12, precision=PREC_FP64):

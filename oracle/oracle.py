@@ -235,10 +235,14 @@ def check_convergence(rhs_node, RT_node, eq, enorm, rtolf, nite):
     return ok, errs
 
 
-def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: int, initial_guess: int = 0):
-    """NonLinearStatic (controlmode 1, tangent stiffness) with NRSolver in full
-    Newton mode (manrmsteps 1: tangent re-assembled every iteration after the
-    first, nrsolver.C:204-402). Prescribed values and loads follow
+def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: int, initial_guess: int = 0,
+                     manrmsteps: int = 1):
+    """NonLinearStatic (controlmode 1, tangent stiffness) with NRSolver
+    (nrsolver.C:204-402). The tangent is assembled at the start of each step and,
+    with manrmsteps k > 0, re-assembled before the solve of every iteration
+    nite > 0 with nite % k == 0 (k = 1: full Newton); manrmsteps 0 is modified
+    Newton, the start-of-step tangent throughout (nrsolver.C:120-126, 285-290).
+    Prescribed values and loads follow
     PiecewiseLinFunction t:[0, ramp_steps] -> f:[0, 1]. initial_guess 1 is
     IG_Tangent (nlinearstatic.C:532-544): before the Newton loop the free DOFs
     take K^-1 (-sum_e K_e du_prescribed), the prescribed increment since the last
@@ -291,7 +295,7 @@ def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: i
                 break
             if nite >= maxiter:
                 raise RuntimeError("NRSolver: maximum number of iterations reached")
-            if nite > 0:
+            if nite > 0 and manrmsteps > 0 and nite % manrmsteps == 0:
                 val = assemble_tangent(m, loc, neq, rowptr, colind, state)
             K = sp.csr_matrix((val, colind, rowptr), shape=(neq, neq))
             b = np.zeros(neq)
@@ -302,3 +306,27 @@ def nonlinear_static(m: dict, times, ramp_steps: float, rtolf: float, maxiter: i
         reac = np.where(bc_mask == 1, F - np.asarray(m["nodal_load"]) * fac, 0.0)
         out.append(dict(u=u_node, reac=reac, stress=sig, strain=eps, nite=nite, state=state.copy()))
     return out
+
+
+def static_structural(m: dict, nsteps: int, ramp_time: float, deltat: float = 1.0, prescribed_times=None,
+                      rtolf: float = 1e-3, maxiter: int = 100000000, manrmsteps: int = 0,
+                      initial_guess: int = 1):
+    """StaticStructural (staticstructural.C:235-356): step n at time
+    t_{n-1} + deltat (or prescribedtimes[n-1]); IG_Tangent by default, the free DOFs starting from
+    the converged solution pushed by K(previous state)^-1 (-sum_e K_e du), du the
+    element's total displacement at this step minus that of the last one
+    (EngngModel::assembleExtrapolatedForces engngm.C:1536-1610; after
+    DofDistributedPrimaryField::advanceSolution only the prescribed DOFs differ);
+    NRSolver's defaults: modified Newton (no manrmsteps), rtolf 1e-3, nsmax 1e8
+    (nrsolver.C:103-140). Prescribed values and loads follow the ramp
+    t:[0, ramp_time] -> [0, 1]."""
+    if prescribed_times is not None:
+        times = [float(t) for t in prescribed_times]
+    else:
+        # t_n = t_{n-1} + deltat, accumulated (TimeStepController::giveNextStep)
+        times, t = [], 0.0
+        for _ in range(nsteps):
+            t += deltat
+            times.append(t)
+    return nonlinear_static(m, times, ramp_time, rtolf, maxiter, initial_guess=initial_guess,
+                            manrmsteps=manrmsteps)

@@ -182,6 +182,18 @@ def main():
                                                  maxiter=np.int32(maxiter),
                                                  initial_guess=np.int32(initial_guess)))
 
+    def static_structural(name, mesh, nsteps, deltat=1.0, rtolf=1e-8, maxiter=400, manrmsteps=None):
+        # StaticStructural with the reference's defaults: nrsolver, IG_Tangent,
+        # modified Newton unless manrmsteps is given
+        analysis = (f"StaticStructural nsteps {nsteps} deltat {deltat!r} rtolf {rtolf!r} maxiter {maxiter}"
+                    + (f" manrmsteps {manrmsteps}" if manrmsteps is not None else ""))
+        tend = nsteps * deltat
+        ramp = f"PiecewiseLinFunction 2 nPoints 2 t 2 0.0 {float(tend)!r} f(t) 2 0.0 1.0"
+        run_case(name, mesh, args.work, analysis=analysis, dumpK=False, bc_ltf=2, load_ltf=2,
+                 extra_funcs=(ramp,), extra=dict(rtolf=np.float64(rtolf), ramp_time=np.float64(tend),
+                                                 deltat=np.float64(deltat), maxiter=np.int32(maxiter),
+                                                 manrmsteps=np.int32(-1 if manrmsteps is None else manrmsteps)))
+
     ey = 250e6 / 210e9
     cases = {
         "hex_cantilever_20x4x4": lambda: run_case(
@@ -205,6 +217,16 @@ def main():
                                                      material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6,
                                                                           H=2e9),
                                                      end_disp=3 * ey * 0.5), 10, initial_guess=1),
+        "ss_mises_hex_6x3x3": lambda: static_structural(
+            "ss_mises_hex_6x3x3", mg.hex_block_pull(6, 3, 3, h=0.05, jitter=0.2, seed=12,
+                                                    material=mg.Material(mg.MAT_MISES, 210e9, 0.3, sig0=250e6,
+                                                                         H=2e9),
+                                                    end_disp=3 * ey * 0.3), 5, deltat=0.5),
+        "ss_mises_hex_5x2x2_accel": lambda: static_structural(
+            "ss_mises_hex_5x2x2_accel", mg.hex_block_pull(5, 2, 2, h=0.05, jitter=0.2, seed=13,
+                                                          material=mg.Material(mg.MAT_MISES, 210e9, 0.3,
+                                                                               sig0=250e6, H=2e9),
+                                                          end_disp=3 * ey * 0.25), 8, manrmsteps=2),
         "idm1_tet_3": lambda: nonlinear(
             "idm1_tet_3", mg.tet_cube(3, jitter=0.15, seed=5,
                                       material=mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=1000.0),

@@ -116,3 +116,26 @@ def test_nonlinear_static_newton(case, oracle):
             dam = le > 0
             if dam.any():
                 assert rel(r["state"][dam, 2], le[dam]) < 1e-9
+
+
+SS_CASES = ["ss_mises_hex_6x3x3", "ss_mises_hex_5x2x2_accel"]
+
+
+@pytest.mark.parametrize("case", SS_CASES)
+def test_static_structural(case, oracle):
+    """StaticStructural with the reference's defaults (nrsolver, IG_Tangent
+    initial guess, modified Newton unless manrmsteps is given; deltat time
+    stepping) and MisesMat against the reference run: same Newton iterations per
+    step, same displacements, reactions, GP stresses and kappa."""
+    g = load_golden(case)
+    ns = int(g["nsteps"])
+    mr = int(g["manrmsteps"])
+    res = oracle.static_structural(g, ns, float(g["ramp_time"]), deltat=float(g["deltat"]),
+                                   rtolf=float(g["rtolf"]), maxiter=int(g["maxiter"]),
+                                   manrmsteps=0 if mr < 0 else mr)
+    for k, r in enumerate(res, 1):
+        assert r["nite"] == int(g[f"s{k}_nite"]), (k, r["nite"], int(g[f"s{k}_nite"]))
+        assert rel(r["u"], g[f"s{k}_u"]) < 1e-8
+        assert rel(r["reac"], g[f"s{k}_reac"]) < 1e-8
+        assert rel(r["stress"], g[f"s{k}_stress"]) < 1e-8
+        assert rel(r["state"][:, 6], g[f"s{k}_kappa"].ravel()) < 1e-8
