@@ -36,7 +36,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
-SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged"}
+SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged",
+              8: "half-stored: upper blocks streamed, lower blocks applied as transposes"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -107,9 +108,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per SpMV launch from the committed ncu summary (if any)."""
-    p = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+def profile_traffic(form: int):
+    """DRAM bytes per SpMV launch of this form from the committed ncu summary (if any)."""
+    p = os.path.join(ROOT, "profiles", "spmv_half_traffic.json" if form == 8 else "spmv_traffic.json")
     if os.path.exists(p):
         try:
             return json.load(open(p))
@@ -223,6 +224,7 @@ def run_gpu(args):
     ctx = native.Context(local)
     if args.spmv_variant:
         ctx.set_option(native.OPT_SPMV_VARIANT, args.spmv_variant)
+    ctx.set_option(native.OPT_SPMV_HALF, args.spmv_half)
     model = native.GpuModel(ctx, mesh)
     A = native.GpuCsrMtrx(ctx)
     model.build_matrix(A)
@@ -340,7 +342,8 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     sp_ms, sp_n, sp_bytes = prof
     achieved = (sp_bytes / sp_n) / (sp_ms / sp_n * 1e-3) / 1e9 if sp_n else None
-    traffic = profile_traffic()
+    f32_form = A.spmv_forms()[1]
+    traffic = profile_traffic(f32_form)
     info = infos[-1]
     cb = None
     if ws == 1 and not args.no_cpu:
@@ -360,8 +363,9 @@ def run_gpu(args):
         "fp64": {"value": nfree / (ms64 * 1e-3), "ms_per_step": ms64, "iterations": infos64[-1].iterations,
                  "achieved": infos64[-1].achieved},
         "mixed_over_fp64": ms64 / ms,
-        "roofline": {"bound": "hbm", "kernel": "k_sell_spmv (node-block SELL-32, FP32 values, difference form, fused p.q; "
-                               "form %s)" % SPMV_FORMS.get(A.spmv_forms()[1], "?"),
+        "roofline": {"bound": "hbm", "kernel": ("k_half_spmv" if f32_form == 8 else "k_sell_spmv") +
+                     " (node-block SELL-32, FP32 values, difference form, fused p.q; form %s)" %
+                     SPMV_FORMS.get(f32_form, "?"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind,
@@ -651,6 +655,8 @@ def main():
     ap.add_argument("--rve-count", type=int, default=256)
     ap.add_argument("--spmv-variant", type=int, default=0,
                     help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
+    ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
+                    help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -102,6 +102,15 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   per slice from the slice count, loop form timed once per matrix and value
  *   type by the built-in autotuner. */
 #define OGB_OPT_SPMV_VARIANT 7
+/*   OGB_OPT_SPMV_HALF (0/1/2, default 1): mixed solves keep the FP32 operator
+ *   of a node-block matrix half-stored: the diagonal and upper blocks of each
+ *   row, the lower blocks read as transposes of the upper blocks of earlier rows
+ *   (the matrix is symmetric), which halves the matrix stream of every FP32
+ *   SpMV. 1 = for matrices large enough for one warp per slice, 2 = for every
+ *   node-block matrix, 0 = never. A forced OGB_OPT_SPMV_VARIANT uses the full
+ *   copy. The sum order differs from the full copy's (results agree to FP32
+ *   rounding of the operator, not bitwise). */
+#define OGB_OPT_SPMV_HALF 8
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
@@ -148,7 +157,9 @@ OGB_API int ogb_mtrx_at(ogb_mtrx *m, int i, int j, double *value);
 OGB_API int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value);
 /* Node-block SpMV forms in use for this matrix (0 = not tuned yet, or no
  * node-block copy): the OGB_OPT_SPMV_VARIANT numbers 1..4 chosen for FP64 and
- * FP32 values, and the warps per slice. Instrumentation, no reference counterpart. */
+ * FP32 values, and the warps per slice; fp32_form is 8 when the last mixed solve
+ * used the half-stored copy (OGB_OPT_SPMV_HALF). Instrumentation, no reference
+ * counterpart. */
 OGB_API int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_per_slice);
 /* SparseMtrx::giveVersion (sparsemtrx.h:82): bumped on every mutation. */
 OGB_API int ogb_mtrx_version(ogb_mtrx *m, int64_t *version);

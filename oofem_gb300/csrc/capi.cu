@@ -359,6 +359,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->spmv_group = value >= 5 ? 1 : (int)value;
         ctx->spmv_split = value == 0 ? 0 : value == 5 ? 2 : value == 6 ? 4 : 1;
         return OGB_OK;
+    case OGB_OPT_SPMV_HALF:
+        if (value < 0 || value > 2) return fail(OGB_E_ARG, "half-stored SpMV option must be 0, 1 or 2");
+        ctx->spmv_half = (int)value;
+        return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
         ctx->mixed_drop = value * 1e-6;
@@ -576,7 +580,7 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
     if (!m) return fail(OGB_E_ARG, "null argument");
     const bool sell = m->has_sell;
     if (fp64_form) *fp64_form = sell ? m->sell.group[0] : 0;
-    if (fp32_form) *fp32_form = sell ? m->sell.group[1] : 0;
+    if (fp32_form) *fp32_form = sell ? (m->last_half ? 8 : m->sell.group[1]) : 0;
     if (warps_per_slice) *warps_per_slice = sell ? (m->sell.force_split ? m->sell.force_split
                                                     : (m->sell.nslices < NUM_SMS * 16 ? 4 : 1)) : 0;
     return OGB_OK;

@@ -123,6 +123,33 @@ struct PcgScal {
 // that lane r of a warp reads row r's k-th block with coalesced loads.
 //   slot(s, k, r)   = sl_ptr[s] + 32 k + r                (column index array)
 //   value(slot, e)  = (slot - r) * ND*ND + 32 e + r        (e = i*ND + j)
+// Half-stored FP32 copy of a symmetric node-block SELL matrix. Row a keeps its
+// diagonal block and the blocks of its columns b > a as a SELL-32 of its own
+// (the upper part); for its columns c < a it keeps a list entry (c << 6 | k),
+// k the position of a in row c's upper list, and reads K_ac as the transpose of
+// the block K_ca stored there. The upper values stream from HBM once; the
+// transposed reads come back to the same blocks shortly after (on structured
+// meshes a warp's lanes read neighbouring blocks together) and hit L2. Slots
+// are laid out as in the full copy: slot = sl_ptr[s] + 32 k + r, values at
+// (slot - r) * ND*ND + 32 e + r.
+struct HalfSell {
+    bool ok = false;
+    bool tried = false;          // built or found unsuitable for this structure
+    int64_t nslotsU = 0, nslotsL = 0;
+    DBuf<int64_t> sl_ptrU, sl_ptrL;   // nslices + 1
+    DBuf<int> sl_widthU, sl_widthL;   // nslices
+    DBuf<int> colU;                   // nslotsU (padding: the row itself)
+    DBuf<int64_t> srcU;               // slot of the same block in the full copy (-1: padding)
+    DBuf<int> low;                    // nslotsL: c << 6 | k (-1: padding)
+    DBuf<float> v32;                  // nslotsU * ND*ND
+    int64_t version = -1;             // full-copy v32_version these values were taken from
+    void reset()
+    {
+        ok = tried = false;
+        version = -1;
+    }
+};
+
 struct SellMat {
     int nd = 0;
     int nact = 0;           // active node rows
@@ -140,6 +167,7 @@ struct SellMat {
     int group[2] = {0, 0};  // tuned SpMV variant for FP64 / FP32 values (0 = not yet)
     int force_split = 0;    // warps per slice forced by OGB_OPT_SPMV_VARIANT 5 / 6 (0 = rule)
     std::vector<int64_t> inst_row_base;   // first node-space row of each instance (+ total)
+    HalfSell half;                        // half-stored FP32 copy (built on first use)
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
 
@@ -171,6 +199,7 @@ struct ogb_ctx {
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)
     bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
     int spmv_group = 0;         // SELL SpMV loop variant forced (1..4) or 0 = tuned per matrix
+    int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     ogb::DBuf<int> status;           // device status word
@@ -207,6 +236,7 @@ struct ogb_mtrx {
     ogb::SellMat sell;
     ogb::DBuf<double> n_b, n_x, n_r64, n_q64;   // node-space FP64 vectors
     ogb::DBuf<float> n_d32;                      // mixed: solution increment since the last replacement
+    bool last_half = false;                      // the last mixed solve used the half-stored FP32 copy
 };
 
 struct ogb_model {
@@ -287,6 +317,11 @@ int build_loc_pattern(ogb_mtrx *m, int neq, int nelem, const int64_t *loc_ptr_h,
 int staged_assemble(ogb_mtrx *m);
 int pad_matrix_rows(ogb_mtrx *m);
 int build_sell(ogb_model *md, ogb_mtrx *m);
+// halfsell.cu: the half-stored FP32 copy of m->sell (half.ok stays false when the
+// matrix does not fit its index packing); refresh_half copies the current FP32
+// values into it.
+int build_half(ogb_ctx *ctx, SellMat &S);
+int refresh_half(ogb_ctx *ctx, SellMat &S);
 
 // element.cu
 int launch_elem_stiffness(ogb_model *md);

@@ -197,6 +197,126 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
     }
 }
 
+// q = K p from the half-stored FP32 copy (halfsell.cu), fused p.q and alpha.
+// Upper pass: the row's diagonal block and its blocks of columns b > a, streamed
+// like k_sell_spmv (block columns prefetched G ahead). Lower pass: for every
+// column c < a, the block K_ca that row c stored (slot ptrU[c / 32] + 32 k +
+// c % 32) applied transposed, K_ac = K_ca^T; its list entries are prefetched G
+// ahead. The upper values are loaded with the default cache policy, not
+// streamed: the lower passes of later rows read them again from L2. DIFF: the
+// diagonal slot holds the block row sum and the off-diagonal blocks act on
+// x_c - x_a. The sum order is fixed (upper list, then lower list).
+template <int ND, class X, bool DIFF, int G>
+__global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
+                                                        const int *__restrict__ wU, const int *__restrict__ colU,
+                                                        const float *__restrict__ val, const int64_t *__restrict__ ptrL,
+                                                        const int *__restrict__ wL, const int *__restrict__ low,
+                                                        const X *__restrict__ x, X *__restrict__ y, double *part,
+                                                        unsigned int *count, PcgScal *sc)
+{
+    if (halted(sc)) return;
+    const int s = blockIdx.x * (NTHREADS / 32) + (threadIdx.x >> 5);
+    const int r = threadIdx.x & 31;
+    double dot = 0.0;
+    if (s < nslices) {
+        const int arow = s * 32 + r;
+        float yy[ND], xa[ND];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            yy[i] = 0.f;
+            xa[i] = (float)x[(int64_t)arow * ND + i];
+        }
+        {   // upper pass
+            const int64_t base = ptrU[s];
+            const int w = wU[s];
+            const float *vp = val + base * (ND * ND) + r;
+            const int *cp = colU + base + r;
+            int cn[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
+            for (int k0 = 0; k0 < w; k0 += G) {
+                int cc[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    cc[g] = cn[g];
+                    cn[g] = k0 + G + g < w ? __ldcs(cp + 32 * (k0 + G + g)) : arow;
+                }
+                float xb[G][ND];
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) {
+                        xb[g][j] = (float)__ldg(x + (int64_t)cc[g] * ND + j);
+                        if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
+                    }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (k0 + g < w) {
+                        const float *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j) yy[i] += __ldg(vk + 32 * (i * ND + j)) * xb[g][j];
+                    }
+                }
+            }
+        }
+        {   // lower pass
+            const int64_t base = ptrL[s];
+            const int w = wL[s];
+            const int *lp = low + base + r;
+            int en[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) en[g] = g < w ? __ldcs(lp + 32 * g) : -1;
+            for (int k0 = 0; k0 < w; k0 += G) {
+                int e[G];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    e[g] = en[g];
+                    en[g] = k0 + G + g < w ? __ldcs(lp + 32 * (k0 + G + g)) : -1;
+                }
+                const float *vk[G];
+                float xb[G][ND];
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int c = e[g] >= 0 ? (e[g] >> 6) : arow;
+                    const int kk = e[g] >= 0 ? (e[g] & 63) : 0;
+                    const int rc = c & 31;
+                    vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + rc;
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) {
+                        xb[g][j] = (float)__ldg(x + (int64_t)c * ND + j);
+                        if (DIFF) xb[g][j] -= xa[j];
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (e[g] >= 0) {
+#pragma unroll
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j) yy[i] += __ldg(vk[g] + 32 * (j * ND + i)) * xb[g][j];
+                    }
+                }
+            }
+        }
+        const int64_t a = (int64_t)s * 32 + r;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            y[a * ND + i] = (X)yy[i];
+            dot += (double)x[a * ND + i] * (double)yy[i];   // exact in FP64
+        }
+    }
+    double acc[1] = {dot};
+    block_sum<1>(acc);
+    if (publish_partials<1>(acc, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        finish_pq(t[0], count, sc);
+    }
+}
+
 // ---------------------------------------------------------------- vector kernels
 // r = b - Ax (Ax in q), z = D^-1 r, p = z; ||b||^2, ||r||^2, r.z.
 template <class X>
@@ -1090,6 +1210,34 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
     return OGB_OK;
 }
 
+// q = K p through the half-stored FP32 copy, fused p.q (mixed solves).
+template <class X, bool DIFF>
+int apply_half(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, unsigned int *count, PcgScal *sc)
+{
+    const SellMat &S = *op.S;
+    const HalfSell &H = S.half;
+    const int grid = (int)ceil_div(S.nslices, NTHREADS / 32);
+    cudaStream_t s = ctx->stream;
+    prof_begin(ctx);
+    if (S.nd == 3)
+        k_half_spmv<3, X, DIFF, 4><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
+                                                             H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
+                                                             sc);
+    else
+        k_half_spmv<2, X, DIFF, 4><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
+                                                             H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
+                                                             sc);
+    // algorithmic bytes: the upper values (the diagonal blocks and half of the
+    // off-diagonal ones) with their block columns, one 4-byte entry per lower
+    // block, x once and y once; padding slots not counted
+    const double nd2 = (double)S.nd * S.nd, blocks = (double)op.nzt / nd2, rows = (double)S.nact;
+    const double up = 0.5 * (blocks + rows), lo = 0.5 * (blocks - rows);
+    prof_end(ctx, up * nd2 * sizeof(float) + up * sizeof(int) + lo * sizeof(int) + (double)op.n * sizeof(X) * 2);
+    count_launch(ctx);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
 template <class X, class V>
 int launch_diag_inv(ogb_ctx *ctx, const Op &op, const V *val, X *dinv, PcgScal *sc)
 {
@@ -1290,8 +1438,27 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
     OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
     const bool diff = op.sell && ctx->mixed_diff;
-    if (diff) OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
-    else OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+    // the half-stored FP32 copy for large node-block matrices (one warp per slice)
+    bool half = false;
+    if constexpr (sizeof(P) == 4) {
+        if (op.sell && !ctx->spmv_group &&
+            (ctx->spmv_half == 2 || (ctx->spmv_half == 1 && sell_split(*op.S) == 1))) {
+            SellMat &S = const_cast<SellMat &>(*op.S);
+            if (!S.half.tried) OGB_CHECK(build_half(ctx, S));
+            if (S.half.ok) {
+                OGB_CHECK(refresh_half(ctx, S));
+                half = true;
+            }
+        }
+    }
+    m->last_half = half;
+    if (half) {
+        // no loop variants to tune
+    } else if (diff) {
+        OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+    } else {
+        OGB_CHECK((sell_autotune<float, P, float, false>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+    }
     int iters = 0, replacements = 0, status = OGB_E_NOTCONV, since_mark = 0, longest = 0;
     double mark = INFINITY;
     *stalled = false;
@@ -1301,10 +1468,16 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     auto batch = [&]() -> int {
         for (int k = 0; k < BATCH; ++k) {
             ctx->prof_sample = k == BATCH / 2 || !ctx->capture_events;   // time one mid-batch SpMV per replay
-            if (diff)
+            if (half) {
+                if constexpr (sizeof(P) == 4) {
+                    if (diff) OGB_CHECK((apply_half<P, true>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc)));
+                    else OGB_CHECK((apply_half<P, false>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc)));
+                }
+            } else if (diff) {
                 OGB_CHECK((apply_op<float, P, true, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
-            else
+            } else {
                 OGB_CHECK((apply_op<float, P, true, float>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc)));
+            }
             ctx->prof_sample = true;
             if constexpr (F32) {
                 if (ctx->mixed_x64) {

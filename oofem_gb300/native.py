@@ -33,6 +33,7 @@ OPT_MIXED_DROP_PPM = 4
 OPT_MIXED_P32 = 5
 OPT_MIXED_X64 = 6
 OPT_SPMV_VARIANT = 7
+OPT_SPMV_HALF = 8
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
