@@ -5,7 +5,7 @@
 // the row's other columns, zero padding slots whose column is a itself):
 //   upper list  = [diagonal] + [entries with column b > a, in full-row order]
 //   lower list  = [(c, k) for entries with column c < a, in full-row order],
-//                 k = position of a in row c's upper list.
+//                 k = position of a in row c's upper list, packed c << 6 | k.
 // The lower entries of a row are exactly the transposes of upper entries of
 // earlier rows (the pattern is symmetric), so every stored block is used twice
 // per SpMV and the matrix stream from HBM halves. The SpMV kernel lives with

@@ -201,11 +201,12 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // Upper pass: the row's diagonal block and its blocks of columns b > a, streamed
 // like k_sell_spmv (block columns prefetched G ahead). Lower pass: for every
 // column c < a, the block K_ca that row c stored (slot ptrU[c / 32] + 32 k +
-// c % 32) applied transposed, K_ac = K_ca^T; its list entries are prefetched G
-// ahead. The upper values are loaded with the default cache policy, not
-// streamed: the lower passes of later rows read them again from L2. DIFF: the
-// diagonal slot holds the block row sum and the off-diagonal blocks act on
-// x_c - x_a. The sum order is fixed (upper list, then lower list).
+// c % 32 of its upper list, the entry packing c << 6 | k) applied transposed,
+// K_ac = K_ca^T; the entries are prefetched G ahead.
+// The upper values bypass L1 (no reuse within the block) and stay in L2, where
+// the lower passes of later rows read them a second and last time (evict-first).
+// DIFF: the diagonal slot holds the block row sum and the off-diagonal blocks
+// act on x_c - x_a. The sum order is fixed (upper list, then lower list).
 template <int ND, class X, bool DIFF, int G>
 __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
 #pragma unroll
                         for (int i = 0; i < ND; ++i)
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldg(vk + 32 * (i * ND + j)) * xb[g][j];
+                            for (int j = 0; j < ND; ++j) yy[i] += __ldcg(vk + 32 * (i * ND + j)) * xb[g][j];
                     }
                 }
             }
@@ -281,8 +282,7 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
                 for (int g = 0; g < G; ++g) {
                     const int c = e[g] >= 0 ? (e[g] >> 6) : arow;
                     const int kk = e[g] >= 0 ? (e[g] & 63) : 0;
-                    const int rc = c & 31;
-                    vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + rc;
+                    vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + (c & 31);
 #pragma unroll
                     for (int j = 0; j < ND; ++j) {
                         xb[g][j] = (float)__ldg(x + (int64_t)c * ND + j);
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
 #pragma unroll
                         for (int i = 0; i < ND; ++i)
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldg(vk[g] + 32 * (j * ND + i)) * xb[g][j];
+                            for (int j = 0; j < ND; ++j) yy[i] += __ldcs(vk[g] + 32 * (j * ND + i)) * xb[g][j];
                     }
                 }
             }
@@ -1220,11 +1220,11 @@ int apply_half(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, unsig
     cudaStream_t s = ctx->stream;
     prof_begin(ctx);
     if (S.nd == 3)
-        k_half_spmv<3, X, DIFF, 4><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
+        k_half_spmv<3, X, DIFF, 8><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
                                                              H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
                                                              sc);
     else
-        k_half_spmv<2, X, DIFF, 4><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
+        k_half_spmv<2, X, DIFF, 8><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
                                                              H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
                                                              sc);
     // algorithmic bytes: the upper values (the diagonal blocks and half of the
