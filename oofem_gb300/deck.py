@@ -1,0 +1,513 @@
+"""Reader for OOFEM text input decks, limited to what this library runs, and a
+runner that executes a deck on the GPU path.
+
+Accepted (anything else raises DeckError naming the record):
+  analysis   LinearStatic, NonLinearStatic (controlmode 1), StaticStructural
+             (solvertype nrsolver) with their step, NRSolver and linear-solver keys
+  nodes      Node (coords; old-style `bc` / `load` references)
+  elements   LSpace, PlaneStress2d, LTRSpace (one type per deck)
+  sections   SimpleCS (thick, material, set; or the element's crossSect / mat)
+  materials  IsoLE, MisesMat (htype 0, no damage), idm1 (Mazars, exponential
+             cohesive law)
+  loads      BoundaryCondition (dofs / values / set, or prescribedvalue with node
+             `bc` references), NodalLoad (dofs / components / set, or node `load`)
+  functions  ConstantFunction, PiecewiseLinFunction
+  sets       nodes, noderanges, elements, elementranges, allelements
+
+Record syntax follows the reference's reader (src/core/oofemtxtdatareader.C,
+oofemtxtinputrecord.C, src/core/tokenizer.C): one record per line, `#` starts a
+comment line, keywords are matched without regard to case, an array field is a
+count followed by that many values, a range field is `{(a b) c ...}`. Component
+order after the counts record: dof managers, elements, cross sections,
+materials, boundary conditions and loads, initial conditions, functions, sets
+(Domain::instanciateYourself, src/core/domain.C:485-700).
+"""
+from __future__ import annotations
+
+import builtins
+import dataclasses
+import re
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import meshgen as mg
+from .engng import ConstantFunction, PiecewiseLinFunction
+
+ELEMENT_TYPES = {"lspace": mg.ELEM_LSPACE, "planestress2d": mg.ELEM_PLANESTRESS2D, "ltrspace": mg.ELEM_LTRSPACE}
+NODES_PER_ELEMENT = {mg.ELEM_LSPACE: 8, mg.ELEM_PLANESTRESS2D: 4, mg.ELEM_LTRSPACE: 4}
+
+
+class DeckError(ValueError):
+    pass
+
+
+def _tokens(line: str) -> List[str]:
+    """Whitespace tokens; `{...}` range groups and quoted strings stay one token."""
+    out, i, n = [], 0, len(line)
+    while i < n:
+        c = line[i]
+        if c.isspace():
+            i += 1
+        elif c == "{":
+            j = line.find("}", i)
+            if j < 0:
+                raise DeckError(f"unterminated range in: {line}")
+            out.append(line[i:j + 1])
+            i = j + 1
+        elif c in "\"'":
+            j = line.find(c, i + 1)
+            if j < 0:
+                raise DeckError(f"unterminated string in: {line}")
+            out.append(line[i + 1:j])
+            i = j + 1
+        else:
+            j = i
+            while j < n and not line[j].isspace():
+                j += 1
+            out.append(line[i:j])
+            i = j
+    return out
+
+
+def _ranges(tok: str) -> List[int]:
+    """`{(1 4) 7 (9 10)}` -> [1, 2, 3, 4, 7, 9, 10]."""
+    body = tok.strip()[1:-1]
+    out = []
+    for a, b, single in re.findall(r"\(\s*(-?\d+)\s+(-?\d+)\s*\)|(-?\d+)", body):
+        if single:
+            out.append(int(single))
+        else:
+            out.extend(range(int(a), int(b) + 1))
+    return out
+
+
+class Record:
+    def __init__(self, text: str, lineno: int):
+        self.text, self.lineno = text, lineno
+        self.tok = _tokens(text)
+        if not self.tok:
+            raise DeckError(f"line {lineno}: empty record")
+        self.keyword = self.tok[0].lower()
+        self.number: Optional[int] = None
+        if len(self.tok) > 1 and re.fullmatch(r"-?\d+", self.tok[1]):
+            self.number = int(self.tok[1])
+        self._low = [t.lower() for t in self.tok]
+
+    def _at(self, key: str) -> Optional[int]:
+        key = key.lower()
+        start = 2 if self.number is not None else 1
+        for i in range(start, len(self._low)):
+            if self._low[i] == key:
+                return i
+        return None
+
+    def has(self, key: str) -> bool:
+        return self._at(key) is not None
+
+    def _value(self, key: str, k: int = 1) -> str:
+        i = self._at(key)
+        if i is None or i + k >= len(self.tok):
+            raise DeckError(f"line {self.lineno}: field '{key}' missing in: {self.text}")
+        return self.tok[i + k]
+
+    def int(self, key: str, default=None) -> int:
+        if not self.has(key):
+            if default is None:
+                raise DeckError(f"line {self.lineno}: field '{key}' missing in: {self.text}")
+            return default
+        return int(self._value(key))
+
+    def float(self, key: str, default=None) -> float:
+        if not self.has(key):
+            if default is None:
+                raise DeckError(f"line {self.lineno}: field '{key}' missing in: {self.text}")
+            return default
+        return float(self._value(key))
+
+    def array(self, key: str, kind=builtins.float) -> list:
+        i = self._at(key)
+        if i is None:
+            raise DeckError(f"line {self.lineno}: field '{key}' missing in: {self.text}")
+        n = int(self.tok[i + 1])
+        vals = self.tok[i + 2:i + 2 + n]
+        if len(vals) != n:
+            raise DeckError(f"line {self.lineno}: field '{key}' has fewer than {n} values")
+        return [kind(v) for v in vals]
+
+    def ranges(self, key: str) -> List[int]:
+        return _ranges(self._value(key))
+
+
+@dataclasses.dataclass
+class Deck:
+    output: str
+    description: str
+    analysis: Record
+    mesh: mg.Mesh
+    node_ids: np.ndarray                 # deck number of each node (row of the mesh arrays)
+    elem_ids: np.ndarray
+    bc_ltf: np.ndarray                   # (nnodes, ndofpn) time function of each prescribed DOF (0: none)
+    load_terms: List[Tuple[np.ndarray, int]]   # (nodal load pattern, time function)
+    functions: Dict[int, object]
+
+    @property
+    def analysis_type(self) -> str:
+        return self.analysis.keyword
+
+    def bc_value_at(self, t: float) -> np.ndarray:
+        """Prescribed values at time t: value x f_ltf(t) per DOF."""
+        out = np.zeros_like(self.mesh.bc_value)
+        for f, fn in self.functions.items():
+            sel = self.bc_ltf == f
+            if sel.any():
+                out[sel] = self.mesh.bc_value[sel] * fn.evaluate_at_time(t)
+        return out
+
+    def nodal_load_at(self, t: float) -> np.ndarray:
+        out = np.zeros_like(self.mesh.nodal_load)
+        for pattern, f in self.load_terms:
+            out += pattern * self.functions[f].evaluate_at_time(t)
+        return out
+
+
+def _records(path: str):
+    with open(path) as fh:
+        for lineno, line in enumerate(fh, 1):
+            s = line.strip()
+            if not s or s.startswith("#"):
+                continue
+            yield lineno, s
+
+
+def read_deck(path: str) -> Deck:
+    it = _records(path)
+
+    def nxt(what: str) -> Tuple[int, str]:
+        try:
+            return next(it)
+        except StopIteration:
+            raise DeckError(f"{path}: deck ends before the {what}") from None
+
+    output = nxt("output file name")[1]
+    description = nxt("description")[1]
+    analysis = Record(*reversed(nxt("analysis record")))
+    if analysis.keyword not in ("linearstatic", "nonlinearstatic", "staticstructural"):
+        raise DeckError(f"analysis '{analysis.tok[0]}' is not supported (LinearStatic, NonLinearStatic, "
+                        f"StaticStructural)")
+    nms = analysis.int("nmsteps", 0)
+    if nms > 1:
+        raise DeckError("several metasteps are not supported")
+    if nms == 1:
+        # one metastep: its record (step count, solver keys) completes the analysis record
+        ms_line, ms_text = nxt("metastep record")
+        rest = analysis.text.split(None, 1)
+        analysis = Record(rest[0] + " " + ms_text + (" " + rest[1] if len(rest) > 1 else ""), analysis.lineno)
+    for _ in range(analysis.int("nmodules", 0)):
+        nxt("export modules")
+    dom = Record(*reversed(nxt("domain record")))
+    if dom.keyword != "domain":
+        raise DeckError(f"line {dom.lineno}: expected the domain record")
+    dtype = dom.tok[1].lower() if len(dom.tok) > 1 else "3d"
+    om = Record(*reversed(nxt("output manager record")))
+    if om.keyword != "outputmanager":
+        raise DeckError(f"line {om.lineno}: expected the OutputManager record")
+    comp = Record(*reversed(nxt("component counts")))
+    counts = dict.fromkeys(("ndofman", "nelem", "ncrosssect", "nmat", "nbc", "nic", "nltf", "nset", "nbarrier"), 0)
+    for i in range(len(comp.tok) - 1):   # the record starts with its first count
+        if comp._low[i] in counts:
+            counts[comp._low[i]] = int(comp.tok[i + 1])
+    if counts["nic"]:
+        raise DeckError("initial conditions are not supported")
+
+    def block(n, what):
+        return [Record(*reversed(nxt(what))) for _ in range(n)]
+
+    nodes = block(counts["ndofman"], "dof managers")
+    elems = block(counts["nelem"], "elements")
+    sections = block(counts["ncrosssect"], "cross sections")
+    mats = block(counts["nmat"], "materials")
+    block(counts["nbarrier"], "nonlocal barriers")
+    bcs = block(counts["nbc"], "boundary conditions")
+    funcs = block(counts["nltf"], "functions")
+    sets = block(counts["nset"], "sets")
+
+    # element type and dimensions
+    etypes = {e.keyword for e in elems}
+    if len(etypes) != 1 or next(iter(etypes)) not in ELEMENT_TYPES:
+        raise DeckError(f"elements {sorted(etypes)}: one of LSpace, PlaneStress2d, LTRSpace per deck is supported")
+    et = ELEMENT_TYPES[next(iter(etypes))]
+    ndim = 2 if et == mg.ELEM_PLANESTRESS2D else 3
+    nd = mg.DOFS_PER_NODE[et]
+    if et == mg.ELEM_PLANESTRESS2D and dtype not in ("2dplanestress", "planestress2d"):
+        raise DeckError(f"PlaneStress2d needs domain 2dPlaneStress, not '{dtype}'")
+
+    # nodes
+    for r in nodes:
+        if r.keyword != "node":
+            raise DeckError(f"line {r.lineno}: dof manager '{r.tok[0]}' is not supported")
+    node_ids = np.array([r.number for r in nodes], np.int64)
+    nmap = {int(i): k for k, i in enumerate(node_ids)}
+    coords = np.array([r.array("coords")[:ndim] for r in nodes], np.float64).reshape(len(nodes), ndim)
+
+    # sets
+    set_nodes: Dict[int, List[int]] = {}
+    set_elems: Dict[int, List[int]] = {}
+    for r in sets:
+        if r.keyword != "set":
+            raise DeckError(f"line {r.lineno}: expected a Set record")
+        ns, es = [], []
+        if r.has("nodes"):
+            ns += r.array("nodes", int)
+        if r.has("noderanges"):
+            ns += r.ranges("noderanges")
+        if r.has("elements"):
+            es += r.array("elements", int)
+        if r.has("elementranges"):
+            es += r.ranges("elementranges")
+        if r.has("allelements"):
+            es += [e.number for e in elems]
+        set_nodes[r.number] = ns
+        set_elems[r.number] = es
+
+    # elements
+    elem_ids = np.array([r.number for r in elems], np.int64)
+    emap = {int(i): k for k, i in enumerate(elem_ids)}
+    nnpe = NODES_PER_ELEMENT[et]
+    conn = np.zeros((len(elems), nnpe), np.int32)
+    for k, r in enumerate(elems):
+        ids = r.array("nodes", int)
+        if len(ids) != nnpe:
+            raise DeckError(f"line {r.lineno}: {r.tok[0]} needs {nnpe} nodes")
+        try:
+            conn[k] = [nmap[i] for i in ids]
+        except KeyError as e:
+            raise DeckError(f"line {r.lineno}: unknown node {e.args[0]}") from None
+
+    # materials
+    mat_index: Dict[int, int] = {}
+    materials: List[mg.Material] = []
+    for r in mats:
+        if r.keyword == "isole":
+            # talpha acts only through temperature loads, which are not accepted
+            m = mg.Material(mg.MAT_ISOLE, r.float("e"), r.float("n"))
+        elif r.keyword == "misesmat":
+            if r.int("htype", 0) != 0 or r.float("omega_crit", 0.0) != 0.0 or r.float("a", 0.0) != 0.0:
+                raise DeckError(f"line {r.lineno}: MisesMat with hardening type or damage is not supported")
+            m = mg.Material(mg.MAT_MISES, r.float("e"), r.float("n"), sig0=r.float("sig0"), H=r.float("h", 0.0))
+        elif r.keyword == "idm1":
+            if r.int("equivstraintype", 0) != 0 or r.int("damlaw", 0) != 0:
+                raise DeckError(f"line {r.lineno}: idm1 supports equivstraintype 0 and damlaw 0 only")
+            m = mg.Material(mg.MAT_IDM1, r.float("e"), r.float("n"), e0=r.float("e0"), gf=r.float("gf"))
+        else:
+            raise DeckError(f"line {r.lineno}: material '{r.tok[0]}' is not supported")
+        mat_index[r.number] = len(materials)
+        materials.append(m)
+
+    # cross sections -> element materials
+    cs_mat: Dict[int, int] = {}
+    thick = set()
+    elem_cs = np.zeros(len(elems), np.int64)
+    for r in sections:
+        if r.keyword != "simplecs":
+            raise DeckError(f"line {r.lineno}: cross section '{r.tok[0]}' is not supported")
+        if r.has("material"):
+            cs_mat[r.number] = r.int("material")
+        thick.add(r.float("thick", 1.0))
+        if r.has("set"):
+            for e in set_elems.get(r.int("set"), []):
+                elem_cs[emap[e]] = r.number
+    elem_mat = np.full(len(elems), -1, np.int32)
+    for k, r in enumerate(elems):
+        cs = r.int("crosssect", 0) or int(elem_cs[k])
+        mid = r.int("mat", 0) or cs_mat.get(cs, 0)
+        if mid not in mat_index:
+            raise DeckError(f"line {r.lineno}: element {r.number} has no material")
+        elem_mat[k] = mat_index[mid]
+    if len(thick) > 1 and et == mg.ELEM_PLANESTRESS2D:
+        raise DeckError("cross sections of different thickness are not supported")
+
+    # boundary conditions and nodal loads
+    nn = len(nodes)
+    bc_mask = np.zeros((nn, nd), np.uint8)
+    bc_value = np.zeros((nn, nd))
+    bc_ltf = np.zeros((nn, nd), np.int64)
+    load_terms: List[Tuple[np.ndarray, int]] = []
+    bc_by_id = {r.number: r for r in bcs}
+
+    def prescribe(node_rows, dofs, vals, f):
+        for a in node_rows:
+            for d, v in zip(dofs, vals):
+                if not 1 <= d <= nd:
+                    raise DeckError(f"DOF {d} outside 1..{nd}")
+                bc_mask[a, d - 1] = 1
+                bc_value[a, d - 1] = v
+                bc_ltf[a, d - 1] = f
+
+    for r in bcs:
+        f = r.int("loadtimefunction")
+        if r.keyword == "boundarycondition":
+            if r.has("set"):
+                rows = [nmap[i] for i in set_nodes.get(r.int("set"), [])]
+                dofs = r.array("dofs", int)
+                vals = r.array("values") if r.has("values") else [r.float("prescribedvalue", 0.0)] * len(dofs)
+                prescribe(rows, dofs, vals, f)
+        elif r.keyword == "nodalload":
+            if r.has("set"):
+                comps = r.array("components")
+                dofs = r.array("dofs", int) if r.has("dofs") else list(range(1, len(comps) + 1))
+                pat = np.zeros((nn, nd))
+                for i in set_nodes.get(r.int("set"), []):
+                    for d, v in zip(dofs, comps):
+                        pat[nmap[i], d - 1] += v
+                load_terms.append((pat, f))
+        else:
+            raise DeckError(f"line {r.lineno}: load '{r.tok[0]}' is not supported")
+    # old-style references from the node records
+    for a, r in enumerate(nodes):
+        if r.has("bc"):
+            for d, bid in enumerate(r.array("bc", int), 1):
+                if bid:
+                    b = bc_by_id[bid]
+                    prescribe([a], [d], [b.float("prescribedvalue", b.float("d", 0.0))], b.int("loadtimefunction"))
+        if r.has("load"):
+            for lid in r.array("load", int):
+                b = bc_by_id[lid]
+                comps = b.array("components")
+                pat = np.zeros((nn, nd))
+                pat[a, :len(comps)] = comps[:nd]
+                load_terms.append((pat, b.int("loadtimefunction")))
+
+    # time functions
+    functions: Dict[int, object] = {}
+    for r in funcs:
+        if r.keyword == "constantfunction":
+            functions[r.number] = ConstantFunction(r.float("f(t)"))
+        elif r.keyword == "piecewiselinfunction":
+            functions[r.number] = PiecewiseLinFunction(r.array("t"), r.array("f(t)"))
+        else:
+            raise DeckError(f"line {r.lineno}: function '{r.tok[0]}' is not supported")
+    for f in set(np.unique(bc_ltf[bc_mask == 1]).tolist()) | {f for _, f in load_terms}:
+        if f not in functions:
+            raise DeckError(f"time function {f} is not defined")
+
+    nodal_load = np.zeros((nn, nd))
+    for pat, _ in load_terms:
+        nodal_load += pat
+    mesh = mg.Mesh(et, coords, conn, elem_mat, materials, bc_mask, bc_value, nodal_load,
+                   thickness=thick.pop() if thick else 1.0, name=description)
+    return Deck(output, description, analysis, mesh, node_ids, elem_ids, bc_ltf, load_terms, functions)
+
+
+@dataclasses.dataclass
+class DeckStep:
+    number: int
+    time: float
+    u: np.ndarray
+    reactions: np.ndarray
+    iterations: int       # PCG iterations (LinearStatic) or Newton iterations
+
+
+def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optional[float] = None):
+    """Run the deck's analysis on the GPU path; a list of DeckStep.
+
+    LinearStatic: step k at time k (LinearStatic::giveNextStep, linearstatic.C:146-156), one PCG solve
+    with the deck's lstol / lsiter (IMLSolver defaults 1e-5 / 200 when absent). NonLinearStatic: step k
+    at time (k-1) * deltat (nlinearstatic.C:295-325). StaticStructural: oofem_gb300.engng.StaticStructural.
+    ``precision`` / ``lstol`` override the linear solver's arithmetic and tolerance."""
+    from . import engng, native
+    a = deck.analysis
+    ctx = ctx or native.Context(0)
+    model = native.GpuModel(ctx, deck.mesh)
+    K = native.GpuCsrMtrx(ctx)
+    prec = native.PREC_FP64 if precision is None else precision
+    nsteps = a.int("nsteps", 1)
+    out: List[DeckStep] = []
+    if deck.analysis_type == "linearstatic":
+        tol = lstol if lstol is not None else a.float("lstol", 1e-5)
+        maxit = a.int("lsiter", 200)
+        for k in range(1, nsteps + 1):
+            t = float(k)
+            u, reac, info = model.linear_static(K, deck.bc_value_at(t), deck.nodal_load_at(t), rtol=tol,
+                                                maxit=maxit, precision=prec)
+            if info.status != 0:
+                raise native.OgbError(info.status, f"LinearStatic step {k}: linear solver did not converge")
+            out.append(DeckStep(k, t, u, reac, info.iterations))
+        return out
+    tol = lstol if lstol is not None else a.float("lstol", 1e-12)
+    if deck.analysis_type == "nonlinearstatic":
+        if a.int("controlmode", 1) != 1:
+            raise DeckError("NonLinearStatic supports controlmode 1 (direct displacement / load control)")
+        model.set_initial_guess(a.int("initialguess", 0))
+        model.set_nr_mode(a.int("manrmsteps", 0))
+        dt = a.float("deltat", 1.0)
+        for k in range(1, nsteps + 1):
+            t = (k - 1) * dt
+            u, reac, nite = model.nonlinear_step(K, deck.bc_value_at(t), deck.nodal_load_at(t),
+                                                 rtolf=a.float("rtolf", 1e-3), maxiter=a.int("maxiter", 100000000),
+                                                 lin_rtol=tol, precision=prec)
+            out.append(DeckStep(k, t, u, reac, nite))
+        return out
+    if a.has("solvertype") and a._value("solvertype").lower() != "nrsolver":
+        raise DeckError("StaticStructural supports solvertype nrsolver")
+    ss = engng.StaticStructural(model, K, nsteps=nsteps, deltat=a.float("deltat", 1.0),
+                                prescribed_times=a.array("prescribedtimes") if a.has("prescribedtimes") else None,
+                                rtolf=a.float("rtolf", 1e-3), maxiter=a.int("maxiter", 100000000),
+                                manrmsteps=a.int("manrmsteps", 0), initial_guess=a.int("initialguess", 1),
+                                lstol=tol, precision=prec, bc_at=deck.bc_value_at, load_at=deck.nodal_load_at)
+    for r in ss.solve_yourself():
+        out.append(DeckStep(r.number, r.time, r.u, r.reactions, r.iterations))
+    return out
+
+
+def check_rules(deck_path: str, deck: Deck, steps: List[DeckStep]):
+    """The deck's embedded errorcheck rules (`#NODE tStep s number n dof d unknown d value v`,
+    `#REACTION tStep s number n dof d value v`, tolerance from `#%BEGIN_CHECK% tolerance t`;
+    ErrorCheckingExportModule, src/core/errorcheckingexportmodule.C): a list of
+    (rule text, computed value, expected value, passed)."""
+    tol = 1e-6
+    rules = []
+    nmap = {int(i): k for k, i in enumerate(deck.node_ids)}
+    by_step = {s.number: s for s in steps}
+    with open(deck_path) as fh:
+        for line in fh:
+            m = re.match(r"#%BEGIN_CHECK%\s+tolerance\s+(\S+)", line, re.I)
+            if m:
+                tol = float(m[1])
+            m = re.match(r"#NODE\s+tStep\s+(\d+)\s+number\s+(\d+)\s+dof\s+(\d+)\s+unknown\s+d\s+value\s+(\S+)", line, re.I)
+            if m and int(m[1]) in by_step:
+                got = by_step[int(m[1])].u[nmap[int(m[2])], int(m[3]) - 1]
+                rules.append((line.strip(), got, float(m[4]), abs(got - float(m[4])) <= tol))
+            m = re.match(r"#REACTION\s+tStep\s+(\d+)\s+number\s+(\d+)\s+dof\s+(\d+)\s+value\s+(\S+)", line, re.I)
+            if m and int(m[1]) in by_step:
+                got = by_step[int(m[1])].reactions[nmap[int(m[2])], int(m[3]) - 1]
+                rules.append((line.strip(), got, float(m[4]), abs(got - float(m[4])) <= tol))
+    return rules
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="run an OOFEM input deck on the GPU path")
+    ap.add_argument("deck")
+    ap.add_argument("--mixed", action="store_true", help="mixed-precision linear solves")
+    ap.add_argument("--check", action="store_true", help="verify the deck's embedded #NODE / #REACTION rules")
+    args = ap.parse_args(argv)
+    from . import native
+    deck = read_deck(args.deck)
+    steps = run_deck(deck, precision=native.PREC_MIXED if args.mixed else None)
+    for s in steps:
+        print(json.dumps({"step": s.number, "time": s.time, "iterations": s.iterations,
+                          "max_abs_u": float(np.abs(s.u).max())}))
+    if args.check:
+        rules = check_rules(args.deck, deck, steps)
+        bad = [r for r in rules if not r[3]]
+        print(json.dumps({"rules": len(rules), "failed": len(bad)}))
+        for r in bad:
+            print("FAILED", r[0], "got", r[1])
+        return 1 if bad else 0
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

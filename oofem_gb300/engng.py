@@ -81,7 +81,9 @@ class StaticStructural:
     nrsolver.C:103-140). ``lstol`` / ``precision`` configure the PCG of each
     linear solve (the lstol of the solver record). ``bc_function`` /
     ``load_function`` scale the mesh's prescribed values and nodal loads (the
-    loadTimeFunction of its boundary conditions and loads).
+    loadTimeFunction of its boundary conditions and loads); ``bc_at`` / ``load_at``
+    (callables of t) replace them when each condition has its own function, as
+    read from a deck (oofem_gb300.deck).
 
     Step times accumulate as in TimeStepController::giveNextStep
     (timestepcontroller.C:74-101): t_n = t_{n-1} + deltat. A step that does not
@@ -91,7 +93,8 @@ class StaticStructural:
     def __init__(self, model: "native.GpuModel", matrix: "native.GpuCsrMtrx", nsteps: int = 1,
                  deltat: float = 1.0, prescribed_times=None, bc_function=None, load_function=None,
                  rtolf: float = 1e-3, maxiter: int = 100000000, manrmsteps: int = 0,
-                 initial_guess: int = IG_TANGENT, lstol: float = 1e-12, precision: int = native.PREC_FP64):
+                 initial_guess: int = IG_TANGENT, lstol: float = 1e-12, precision: int = native.PREC_FP64,
+                 bc_at=None, load_at=None):
         if initial_guess not in (IG_NONE, IG_TANGENT):
             raise ValueError(f"Initial guess type: {initial_guess} not supported")
         self.model = model
@@ -101,6 +104,11 @@ class StaticStructural:
         self.deltat = float(deltat)
         self.bc_function = bc_function or ConstantFunction()
         self.load_function = load_function or ConstantFunction()
+        m = model.mesh
+        # prescribed values and nodal loads at time t: the mesh's patterns times one
+        # function each, unless a deck gives them per DOF and load (bc_at / load_at)
+        self.bc_at = bc_at or (lambda t: m.bc_value * self.bc_function.evaluate_at_time(t))
+        self.load_at = load_at or (lambda t: m.nodal_load * self.load_function.evaluate_at_time(t))
         self.rtolf = float(rtolf)
         self.maxiter = int(maxiter)
         self.manrmsteps = int(manrmsteps)
@@ -128,9 +136,8 @@ class StaticStructural:
         if self.step >= self.nsteps:
             raise RuntimeError("StaticStructural: all steps solved")
         t = self._next_time()
-        m = self.model.mesh
-        bcv = m.bc_value * self.bc_function.evaluate_at_time(t)
-        load = m.nodal_load * self.load_function.evaluate_at_time(t)
+        bcv = self.bc_at(t)
+        load = self.load_at(t)
         u, reac, nite = self.model.nonlinear_step(self.matrix, bcv, load, rtolf=self.rtolf, maxiter=self.maxiter,
                                                   lin_rtol=self.lstol, precision=self.precision)
         self.step += 1

@@ -165,6 +165,25 @@ def patch300(ref_src):
         json.dump(rules, fh, indent=1)
 
 
+def reference_patch_decks(ref_src):
+    """The reference's PlaneStress2d / LTRSpace patch decks (tests/sm/patch100.in, patch101.in,
+    patch300.in) read with oofem_gb300.deck, rewritten by decks.write_deck, with the deck's own
+    errorcheck rules (#NODE / #REACTION lines and the tolerance) appended as comment lines, so the GPU
+    tests can run them through the deck reader without the reference tree."""
+    from oofem_gb300 import deck as dk
+    for name in ("patch100", "patch101", "patch300"):
+        src = os.path.join(ref_src, "tests", "sm", name + ".in")
+        d = dk.read_deck(src)
+        out = os.path.join(HERE, name + ".in")
+        write_deck(d.mesh, out, "StaticStructural nsteps 1")
+        rules = [ln.strip() for ln in open(src)
+                 if re.match(r"#(NODE|REACTION|%BEGIN_CHECK%)", ln.strip())]
+        with open(out, "a") as fh:
+            fh.write("# errorcheck rules of tests/sm/%s.in\n" % name)
+            fh.write("\n".join(rules) + "\n")
+        print(f"{name}: {len(rules)} rule lines")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-src", default="/root/reference")
@@ -173,6 +192,7 @@ def main():
     args = ap.parse_args()
     os.makedirs(args.work, exist_ok=True)
     patch300(args.ref_src)
+    reference_patch_decks(args.ref_src)
     def nonlinear(name, mesh, nsteps, rtolf=1e-8, maxiter=100, initial_guess=0):
         analysis = (f"NonLinearStatic nsteps {nsteps} controlmode 1 rtolf {rtolf!r} maxiter {maxiter} "
                     f"manrmsteps 1 stiffmode 0" + (" initialguess 1" if initial_guess else ""))
@@ -193,6 +213,9 @@ def main():
                  extra_funcs=(ramp,), extra=dict(rtolf=np.float64(rtolf), ramp_time=np.float64(tend),
                                                  deltat=np.float64(deltat), maxiter=np.int32(maxiter),
                                                  manrmsteps=np.int32(-1 if manrmsteps is None else manrmsteps)))
+        # the deck itself, for the deck-reader tests
+        with open(os.path.join(args.work, name + ".in")) as src, open(os.path.join(HERE, name + ".in"), "w") as dst:
+            dst.write(src.read())
 
     ey = 250e6 / 210e9
     cases = {
