@@ -278,6 +278,21 @@ OGB_API int ogb_model_set_nr_mode(ogb_model *md, int manrmsteps);
 OGB_API int ogb_model_state_bytes(ogb_model *md, size_t *bytes);
 OGB_API int ogb_model_save_state(ogb_model *md, void *buf, size_t bytes);
 OGB_API int ogb_model_restore_state(ogb_model *md, const void *buf, size_t bytes);
+/* Bulk read of one block of records of an OOFEM text input deck (host code, no
+ * device): `count` records starting at byte `offset`, blank and `#` lines
+ * skipped, each `<keyword> <number> ... <field> <n> v1 .. vn ...` (keyword and
+ * field matched without regard to case, n <= maxvals). Per record: its number
+ * (ids), the n values (vals, maxvals per record), n (nvals), and other[r] = 1
+ * when the record carries further fields, which the caller reads with its
+ * general parser. *next_offset: byte offset after the block; *lines (optional):
+ * lines consumed. Replaces the per-record tokenizer and object instantiation of
+ * the dof-manager and element blocks (OOFEMTXTDataReader / OOFEMTXTInputRecord,
+ * src/core/oofemtxtdatareader.C, oofemtxtinputrecord.C;
+ * Domain::instanciateYourself, src/core/domain.C:485-700). OGB_E_ARG names the
+ * first record that does not fit. */
+OGB_API int ogb_deck_parse_block(const char *path, int64_t offset, int64_t count, const char *keyword,
+                                 const char *field, int maxvals, int64_t *ids, double *vals, int32_t *nvals,
+                                 uint8_t *other, int64_t *next_offset, int64_t *lines);
 /* Linear solves of the Newton drivers since the model was created or reset, and
  * their PCG iterations (summed over instances for batched steps). Instrumentation,
  * no reference counterpart. */

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liboofem_gb300.so")
-SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu", "newton.cu", "batch.cu", "halfsell.cu"]
+SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu", "newton.cu", "batch.cu", "halfsell.cu", "deckparse.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]
@@ -57,7 +57,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
                     raise RuntimeError(f"nvcc failed for {j[-3]}")
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
-        r = subprocess.run([cc, *ARCH, "-shared", "-o", LIB, *objs], capture_output=True, text=True)
+        r = subprocess.run([cc, *ARCH, "-shared", "-o", LIB, *objs, "-lpthread"], capture_output=True, text=True)
         if r.returncode != 0:
             print(r.stdout, r.stderr)
             raise RuntimeError("link failed")

@@ -42,32 +42,14 @@ class DeckError(ValueError):
     pass
 
 
+_TOKEN = re.compile(r"""\{[^}]*\}|"[^"]*"|'[^']*'|\S+""")
+
+
 def _tokens(line: str) -> List[str]:
     """Whitespace tokens; `{...}` range groups and quoted strings stay one token."""
-    out, i, n = [], 0, len(line)
-    while i < n:
-        c = line[i]
-        if c.isspace():
-            i += 1
-        elif c == "{":
-            j = line.find("}", i)
-            if j < 0:
-                raise DeckError(f"unterminated range in: {line}")
-            out.append(line[i:j + 1])
-            i = j + 1
-        elif c in "\"'":
-            j = line.find(c, i + 1)
-            if j < 0:
-                raise DeckError(f"unterminated string in: {line}")
-            out.append(line[i + 1:j])
-            i = j + 1
-        else:
-            j = i
-            while j < n and not line[j].isspace():
-                j += 1
-            out.append(line[i:j])
-            i = j
-    return out
+    if line.count("{") != line.count("}"):
+        raise DeckError(f"unterminated range in: {line[:80]}")
+    return [t[1:-1] if t[0] in "\"'" and len(t) > 1 and t[-1] == t[0] else t for t in _TOKEN.findall(line)]
 
 
 def _ranges(tok: str) -> List[int]:
@@ -133,6 +115,8 @@ class Record:
         vals = self.tok[i + 2:i + 2 + n]
         if len(vals) != n:
             raise DeckError(f"line {self.lineno}: field '{key}' has fewer than {n} values")
+        if n > 64:   # long lists (sets): converted in one numpy call
+            return np.array(vals, dtype=np.int64 if kind is int else np.float64).tolist()
         return [kind(v) for v in vals]
 
     def ranges(self, key: str) -> List[int]:
@@ -171,23 +155,76 @@ class Deck:
         return out
 
 
-def _records(path: str):
-    with open(path) as fh:
-        for lineno, line in enumerate(fh, 1):
-            s = line.strip()
-            if not s or s.startswith("#"):
-                continue
-            yield lineno, s
+class _Reader:
+    """Record lines of a deck with their line numbers and byte offsets."""
+
+    def __init__(self, path: str):
+        self.path = path
+        self.fh = open(path, "rb")
+        self.lineno = 0
+
+    def close(self):
+        self.fh.close()
+
+    def next(self, what: str) -> Tuple[int, str]:
+        while True:
+            b = self.fh.readline()
+            if not b:
+                raise DeckError(f"{self.path}: deck ends before the {what}")
+            self.lineno += 1
+            s = b.decode().strip()
+            if s and not s.startswith("#"):
+                return self.lineno, s
+
+    def peek_keyword(self) -> str:
+        pos, line = self.fh.tell(), self.lineno
+        try:
+            return self.next("block")[1].split(None, 1)[0].lower()
+        finally:
+            self.fh.seek(pos)
+            self.lineno = line
+
+    def block(self, count: int, keyword: str, field: str, maxvals: int):
+        """`count` records `<keyword> <n> ... <field> k v1..vk ...` through the
+        library's bulk reader; records with further fields are read in full."""
+        from . import native
+        import ctypes as C
+        lib = native.load()
+        ids = np.zeros(count, np.int64)
+        vals = np.zeros((count, maxvals))
+        nv = np.zeros(count, np.int32)
+        other = np.zeros(count, np.uint8)
+        start, first_line = self.fh.tell(), self.lineno
+        nxt, lines = C.c_int64(), C.c_int64()
+        code = lib.ogb_deck_parse_block(self.path.encode(), start, count, keyword.encode(), field.encode(), maxvals,
+                                        ids.ctypes.data, vals.ctypes.data, nv.ctypes.data, other.ctypes.data,
+                                        C.byref(nxt), C.byref(lines))
+        if code != 0:
+            raise DeckError(f"{self.path} after line {first_line}: {lib.ogb_last_error().decode()}")
+        full: Dict[int, Record] = {}
+        if other.any():
+            want = set(np.nonzero(other)[0].tolist())
+            k = 0
+            while k < count:
+                ln, text = self.next("block")
+                if k in want:
+                    full[k] = Record(text, ln)
+                k += 1
+        self.fh.seek(nxt.value)
+        self.lineno = first_line + lines.value
+        return ids, vals, nv, full
 
 
 def read_deck(path: str) -> Deck:
-    it = _records(path)
+    rd = _Reader(path)
+    try:
+        return _read(rd, path)
+    finally:
+        rd.close()
 
-    def nxt(what: str) -> Tuple[int, str]:
-        try:
-            return next(it)
-        except StopIteration:
-            raise DeckError(f"{path}: deck ends before the {what}") from None
+
+def _read(rd: "_Reader", path: str) -> Deck:
+    nxt = rd.next
 
     output = nxt("output file name")[1]
     description = nxt("description")[1]
@@ -200,7 +237,7 @@ def read_deck(path: str) -> Deck:
         raise DeckError("several metasteps are not supported")
     if nms == 1:
         # one metastep: its record (step count, solver keys) completes the analysis record
-        ms_line, ms_text = nxt("metastep record")
+        _, ms_text = nxt("metastep record")
         rest = analysis.text.split(None, 1)
         analysis = Record(rest[0] + " " + ms_text + (" " + rest[1] if len(rest) > 1 else ""), analysis.lineno)
     for _ in range(analysis.int("nmodules", 0)):
@@ -223,8 +260,14 @@ def read_deck(path: str) -> Deck:
     def block(n, what):
         return [Record(*reversed(nxt(what))) for _ in range(n)]
 
-    nodes = block(counts["ndofman"], "dof managers")
-    elems = block(counts["nelem"], "elements")
+    nn, ne = counts["ndofman"], counts["nelem"]
+    if nn == 0 or ne == 0:
+        raise DeckError(f"{path}: no nodes or no elements")
+    node_ids, node_vals, node_nv, node_full = rd.block(nn, "node", "coords", 3)
+    ekw = rd.peek_keyword()
+    if ekw not in ELEMENT_TYPES:
+        raise DeckError(f"elements '{ekw}': one of LSpace, PlaneStress2d, LTRSpace per deck is supported")
+    elem_ids, elem_vals, elem_nv, elem_full = rd.block(ne, ekw, "nodes", 8)
     sections = block(counts["ncrosssect"], "cross sections")
     mats = block(counts["nmat"], "materials")
     block(counts["nbarrier"], "nonlocal barriers")
@@ -233,22 +276,34 @@ def read_deck(path: str) -> Deck:
     sets = block(counts["nset"], "sets")
 
     # element type and dimensions
-    etypes = {e.keyword for e in elems}
-    if len(etypes) != 1 or next(iter(etypes)) not in ELEMENT_TYPES:
-        raise DeckError(f"elements {sorted(etypes)}: one of LSpace, PlaneStress2d, LTRSpace per deck is supported")
-    et = ELEMENT_TYPES[next(iter(etypes))]
+    et = ELEMENT_TYPES[ekw]
     ndim = 2 if et == mg.ELEM_PLANESTRESS2D else 3
     nd = mg.DOFS_PER_NODE[et]
     if et == mg.ELEM_PLANESTRESS2D and dtype not in ("2dplanestress", "planestress2d"):
         raise DeckError(f"PlaneStress2d needs domain 2dPlaneStress, not '{dtype}'")
 
     # nodes
-    for r in nodes:
-        if r.keyword != "node":
-            raise DeckError(f"line {r.lineno}: dof manager '{r.tok[0]}' is not supported")
-    node_ids = np.array([r.number for r in nodes], np.int64)
-    nmap = {int(i): k for k, i in enumerate(node_ids)}
-    coords = np.array([r.array("coords")[:ndim] for r in nodes], np.float64).reshape(len(nodes), ndim)
+    if (node_nv < ndim).any():
+        raise DeckError(f"node {int(node_ids[np.argmax(node_nv < ndim)])}: fewer than {ndim} coordinates")
+    coords = np.ascontiguousarray(node_vals[:, :ndim])
+    order = np.argsort(node_ids, kind="stable")
+    sorted_ids = node_ids[order]
+    if (np.diff(sorted_ids) == 0).any():
+        raise DeckError("duplicate node numbers")
+
+    dense = bool((node_ids == np.arange(1, nn + 1)).all())   # nodes numbered 1..n in order
+
+    def node_rows(ids) -> np.ndarray:
+        ids = np.asarray(ids, np.int64)
+        if dense:
+            if ids.size and (ids.min() < 1 or ids.max() > nn):
+                raise DeckError(f"unknown node {int(ids[(ids < 1) | (ids > nn)][0])}")
+            return ids - 1
+        pos = np.searchsorted(sorted_ids, ids)
+        ok = (pos < len(sorted_ids)) & (sorted_ids[np.minimum(pos, len(sorted_ids) - 1)] == ids)
+        if not ok.all():
+            raise DeckError(f"unknown node {int(ids[~ok][0])}")
+        return order[pos]
 
     # sets
     set_nodes: Dict[int, List[int]] = {}
@@ -266,23 +321,31 @@ def read_deck(path: str) -> Deck:
         if r.has("elementranges"):
             es += r.ranges("elementranges")
         if r.has("allelements"):
-            es += [e.number for e in elems]
+            es += elem_ids.tolist()
         set_nodes[r.number] = ns
         set_elems[r.number] = es
 
     # elements
-    elem_ids = np.array([r.number for r in elems], np.int64)
-    emap = {int(i): k for k, i in enumerate(elem_ids)}
     nnpe = NODES_PER_ELEMENT[et]
-    conn = np.zeros((len(elems), nnpe), np.int32)
-    for k, r in enumerate(elems):
-        ids = r.array("nodes", int)
-        if len(ids) != nnpe:
-            raise DeckError(f"line {r.lineno}: {r.tok[0]} needs {nnpe} nodes")
-        try:
-            conn[k] = [nmap[i] for i in ids]
-        except KeyError as e:
-            raise DeckError(f"line {r.lineno}: unknown node {e.args[0]}") from None
+    if (elem_nv != nnpe).any():
+        raise DeckError(f"element {int(elem_ids[np.argmax(elem_nv != nnpe)])}: {ekw} needs {nnpe} nodes")
+    conn = node_rows(elem_vals[:, :nnpe].astype(np.int64).ravel()).reshape(ne, nnpe).astype(np.int32)
+    eorder = np.argsort(elem_ids, kind="stable")
+    esorted = elem_ids[eorder]
+
+    edense = bool((elem_ids == np.arange(1, ne + 1)).all())
+
+    def elem_rows(ids) -> np.ndarray:
+        ids = np.asarray(ids, np.int64)
+        if edense:
+            if ids.size and (ids.min() < 1 or ids.max() > ne):
+                raise DeckError(f"unknown element {int(ids[(ids < 1) | (ids > ne)][0])}")
+            return ids - 1
+        pos = np.searchsorted(esorted, ids)
+        ok = (pos < len(esorted)) & (esorted[np.minimum(pos, len(esorted) - 1)] == ids)
+        if not ok.all():
+            raise DeckError(f"unknown element {int(ids[~ok][0])}")
+        return eorder[pos]
 
     # materials
     mat_index: Dict[int, int] = {}
@@ -307,48 +370,49 @@ def read_deck(path: str) -> Deck:
     # cross sections -> element materials
     cs_mat: Dict[int, int] = {}
     thick = set()
-    elem_cs = np.zeros(len(elems), np.int64)
+    elem_cs = np.zeros(ne, np.int64)
     for r in sections:
         if r.keyword != "simplecs":
             raise DeckError(f"line {r.lineno}: cross section '{r.tok[0]}' is not supported")
         if r.has("material"):
             cs_mat[r.number] = r.int("material")
         thick.add(r.float("thick", 1.0))
-        if r.has("set"):
-            for e in set_elems.get(r.int("set"), []):
-                elem_cs[emap[e]] = r.number
-    elem_mat = np.full(len(elems), -1, np.int32)
-    for k, r in enumerate(elems):
+        if r.has("set") and set_elems.get(r.int("set")):
+            elem_cs[elem_rows(set_elems[r.int("set")])] = r.number
+    elem_mid = np.array([cs_mat.get(int(c), 0) for c in range(int(elem_cs.max()) + 1)], np.int64)[elem_cs]
+    for k, r in elem_full.items():   # old-style crossSect / mat fields on the element record
         cs = r.int("crosssect", 0) or int(elem_cs[k])
-        mid = r.int("mat", 0) or cs_mat.get(cs, 0)
-        if mid not in mat_index:
-            raise DeckError(f"line {r.lineno}: element {r.number} has no material")
-        elem_mat[k] = mat_index[mid]
+        elem_mid[k] = r.int("mat", 0) or cs_mat.get(cs, 0)
+    missing = ~np.isin(elem_mid, list(mat_index))
+    if missing.any():
+        raise DeckError(f"element {int(elem_ids[np.argmax(missing)])} has no material")
+    lut = np.zeros(max(mat_index) + 1, np.int32)
+    for mid, i in mat_index.items():
+        lut[mid] = i
+    elem_mat = lut[elem_mid]
     if len(thick) > 1 and et == mg.ELEM_PLANESTRESS2D:
         raise DeckError("cross sections of different thickness are not supported")
 
     # boundary conditions and nodal loads
-    nn = len(nodes)
     bc_mask = np.zeros((nn, nd), np.uint8)
     bc_value = np.zeros((nn, nd))
     bc_ltf = np.zeros((nn, nd), np.int64)
     load_terms: List[Tuple[np.ndarray, int]] = []
     bc_by_id = {r.number: r for r in bcs}
 
-    def prescribe(node_rows, dofs, vals, f):
-        for a in node_rows:
-            for d, v in zip(dofs, vals):
-                if not 1 <= d <= nd:
-                    raise DeckError(f"DOF {d} outside 1..{nd}")
-                bc_mask[a, d - 1] = 1
-                bc_value[a, d - 1] = v
-                bc_ltf[a, d - 1] = f
+    def prescribe(rows, dofs, vals, f):
+        for d, v in zip(dofs, vals):
+            if not 1 <= d <= nd:
+                raise DeckError(f"DOF {d} outside 1..{nd}")
+            bc_mask[rows, d - 1] = 1
+            bc_value[rows, d - 1] = v
+            bc_ltf[rows, d - 1] = f
 
     for r in bcs:
         f = r.int("loadtimefunction")
         if r.keyword == "boundarycondition":
             if r.has("set"):
-                rows = [nmap[i] for i in set_nodes.get(r.int("set"), [])]
+                rows = node_rows(set_nodes.get(r.int("set"), []))
                 dofs = r.array("dofs", int)
                 vals = r.array("values") if r.has("values") else [r.float("prescribedvalue", 0.0)] * len(dofs)
                 prescribe(rows, dofs, vals, f)
@@ -357,19 +421,20 @@ def read_deck(path: str) -> Deck:
                 comps = r.array("components")
                 dofs = r.array("dofs", int) if r.has("dofs") else list(range(1, len(comps) + 1))
                 pat = np.zeros((nn, nd))
-                for i in set_nodes.get(r.int("set"), []):
-                    for d, v in zip(dofs, comps):
-                        pat[nmap[i], d - 1] += v
+                rows = node_rows(set_nodes.get(r.int("set"), []))
+                for d, v in zip(dofs, comps):
+                    np.add.at(pat[:, d - 1], rows, v)
                 load_terms.append((pat, f))
         else:
             raise DeckError(f"line {r.lineno}: load '{r.tok[0]}' is not supported")
     # old-style references from the node records
-    for a, r in enumerate(nodes):
+    for a, r in node_full.items():
         if r.has("bc"):
             for d, bid in enumerate(r.array("bc", int), 1):
                 if bid:
                     b = bc_by_id[bid]
-                    prescribe([a], [d], [b.float("prescribedvalue", b.float("d", 0.0))], b.int("loadtimefunction"))
+                    prescribe(np.array([a]), [d], [b.float("prescribedvalue", b.float("d", 0.0))],
+                              b.int("loadtimefunction"))
         if r.has("load"):
             for lid in r.array("load", int):
                 b = bc_by_id[lid]

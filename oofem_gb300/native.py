@@ -96,6 +96,8 @@ SIGNATURES = {
     "ogb_model_reset_state": (_i, [_vp]),
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
     "ogb_model_set_nr_mode": (_i, [_vp, _i]),
+    "ogb_deck_parse_block": (_i, [C.c_char_p, C.c_int64, C.c_int64, C.c_char_p, C.c_char_p, _i, _vp, _vp, _vp, _vp,
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ogb_model_state_bytes": (_i, [_vp, C.POINTER(C.c_size_t)]),
     "ogb_model_save_state": (_i, [_vp, _vp, C.c_size_t]),
     "ogb_model_restore_state": (_i, [_vp, _vp, C.c_size_t]),
