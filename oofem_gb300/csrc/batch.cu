@@ -816,6 +816,7 @@ __global__ void k_ns_to_eq_col(int neq, const int *__restrict__ ns_of_eq, int nr
 int batch_pcg(ogb_mtrx *m, int nrhs, const double *b, double *x, double rtol, int maxit, int precision, int *iters,
               double *achieved, int *status)
 {
+    if (m->precond != 1) return fail(OGB_E_ARG, "batched solves use the diagonal preconditioner (lsprecond 1)");
     if (!m->has_sell) return fail(OGB_E_STATE, "batched solves need a matrix built from a model");
     if (nrhs < 1 || nrhs > MAXNR) return fail(OGB_E_ARG, "nrhs must be 1..4");
     if (precision != OGB_PREC_FP64 && precision != OGB_PREC_MIXED) return fail(OGB_E_ARG, "unknown precision");

@@ -586,6 +586,15 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
     return OGB_OK;
 }
 
+int ogb_mtrx_set_preconditioner(ogb_mtrx *m, int type)
+{
+    if (!m) return fail(OGB_E_ARG, "null argument");
+    if (type == 2 || type == 3) return fail(OGB_E_ARG, "ILU preconditioners (lsprecond 2, 3) are not built");
+    if (type != 0 && type != 1 && type != 4) return fail(OGB_E_ARG, "unknown preconditioner type");
+    m->precond = type;
+    return OGB_OK;
+}
+
 int ogb_mtrx_version(ogb_mtrx *m, int64_t *version)
 {
     if (!m || !version) return fail(OGB_E_ARG, "null argument");
@@ -629,7 +638,7 @@ int ogb_pcg_solve_multi_dev(ogb_mtrx *m, int nrhs, const double *B, double *X, d
     if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
     OGB_CUDA(cudaSetDevice(m->ctx->device));
     if (nrhs == 0) return OGB_OK;
-    if (m->has_sell && m->sell.v32_version == m->version)
+    if (m->has_sell && m->sell.v32_version == m->version && m->precond == 1)
         return pcg_solve_multi(m, nrhs, B, X, rtol, maxit, precision, iterations, achieved, status);
     // no current node-block copy (location-array matrix, or values changed
     // through set_at): the reference's column loop (sparselinsystemnm.C:47-69)

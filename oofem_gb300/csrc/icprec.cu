@@ -1,0 +1,217 @@
+// Incomplete-Cholesky preconditioner of the IML solver (lsprecond 4,
+// CompCol_ICPreconditioner, src/core/iml/icprecond.C:40-226).
+//
+// Factorization (host, once per matrix version, as the reference does it on
+// its host): the lower triangle of the symmetric matrix by columns -- column k
+// holds rows >= k, the diagonal first; for the symmetric pattern stored here
+// that is row k of the CSR restricted to columns >= k -- then the reference's
+// ICFactor loop (icprecond.C:133-163) kept step for step: the diagonal takes a
+// square root, the column is divided by it, and the columns of the rows below
+// are updated by the same nested search over row indices. That search only
+// matches at the last entry of column k (its successor test reads into the next
+// column), so the factor it produces is not a textbook IC(0); parity requires
+// the same loop, not a cleaner one.
+//
+// Application (device): ICSolve (icprecond.C:166-190) is a forward solve by
+// columns and a backward solve by columns. On the device both run by rows,
+// level by level: row i's forward value needs the rows c < i of its transposed
+// column entries, its backward value the rows r > i of its own column. Each
+// level is one launch of one thread per row; the products are accumulated in
+// the reference's order (columns resp. rows ascending, starting from zero) with
+// separate rounded multiply and subtract, so z = M^-1 r is bitwise the
+// reference's.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace ogb {
+
+namespace {
+
+__global__ void k_ic_fwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
+                         const int *__restrict__ col, const double *__restrict__ val,
+                         const double *__restrict__ diag, const double *__restrict__ x, double *__restrict__ w,
+                         const PcgScal *sc)
+{
+    if (sc && (sc->done || sc->reliable)) return;
+    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= r1) return;
+    const int i = rows[t];
+    double acc = 0.0;
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], w[col[e]]));
+    w[i] = __ddiv_rn(__dadd_rn(x[i], acc), diag[i]);
+}
+
+__global__ void k_ic_bwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
+                         const int *__restrict__ col, const double *__restrict__ val,
+                         const double *__restrict__ diag, const double *__restrict__ w, double *__restrict__ y,
+                         const PcgScal *sc)
+{
+    if (sc && (sc->done || sc->reliable)) return;
+    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= r1) return;
+    const int i = rows[t];
+    double acc = 0.0;
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], y[col[e]]));
+    y[i] = __ddiv_rn(__dadd_rn(w[i], acc), diag[i]);
+}
+
+// Rows grouped by level (counting sort, rows ascending within a level).
+void group_levels(const std::vector<int> &lev, int nlev, std::vector<int> &rows, std::vector<int> &start)
+{
+    start.assign(nlev + 1, 0);
+    for (int l : lev) start[l + 1]++;
+    for (int l = 0; l < nlev; ++l) start[l + 1] += start[l];
+    rows.assign(lev.size(), 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < (int)lev.size(); ++i) rows[fill[lev[i]]++] = i;
+}
+
+}  // namespace
+
+int build_ic(ogb_mtrx *m)
+{
+    IcFactor &F = m->ic;
+    if (F.version == m->version) return OGB_OK;
+    cudaStream_t s = m->ctx->stream;
+    const int n = m->npad;
+    const int64_t ntot = m->nnz + (m->npad - m->neq);
+    std::vector<int64_t> rp(n + 1);
+    std::vector<int> ci(ntot);
+    std::vector<double> va(ntot);
+    OGB_CUDA(cudaMemcpyAsync(rp.data(), m->rowptr.p, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaMemcpyAsync(ci.data(), m->colind.p, ntot * sizeof(int), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaMemcpyAsync(va.data(), m->val.p, ntot * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OGB_CUDA(cudaStreamSynchronize(s));
+    // lower triangle by columns (CompCol_ICPreconditioner::initialize, icprecond.C:64-107)
+    std::vector<int> pntr(n + 1, 0);
+    for (int k = 0; k < n; ++k) {
+        int c = 0;
+        for (int64_t j = rp[k]; j < rp[k + 1]; ++j) c += ci[j] >= k;
+        pntr[k + 1] = pntr[k] + c;
+    }
+    const int nz = pntr[n];
+    std::vector<int> indx(nz);
+    std::vector<double> val(nz);
+    for (int k = 0; k < n; ++k) {
+        int t = pntr[k];
+        for (int64_t j = rp[k]; j < rp[k + 1]; ++j)
+            if (ci[j] >= k) {
+                indx[t] = ci[j];
+                val[t] = va[j];
+                ++t;
+            }
+        if (pntr[k] == pntr[k + 1] || indx[pntr[k]] != k) return fail(OGB_E_ZERODIAG, "IC preconditioner: diagonal not found");
+    }
+    // ICFactor (icprecond.C:133-163), the same loop nest. indx gets one sentinel
+    // entry: the successor test of the last entry of the last column reads one
+    // past the end there.
+    indx.push_back(n);
+    for (int k = 0; k < n - 1; ++k) {
+        const int d = pntr[k];
+        const double z = val[d] = sqrt(val[d]);
+        for (int i = d + 1; i < pntr[k + 1]; ++i) val[i] /= z;
+        for (int i = d + 1; i < pntr[k + 1]; ++i) {
+            const double zi = val[i];
+            const int h = indx[i];
+            int g = i;
+            for (int j = pntr[h]; j < pntr[h + 1]; ++j)
+                for (; g < pntr[k + 1] && indx[g + 1] <= indx[j]; ++g)
+                    if (indx[g] == indx[j]) val[j] -= zi * val[g];
+        }
+    }
+    if (n > 0) val[pntr[n - 1]] = sqrt(val[pntr[n - 1]]);
+    indx.pop_back();
+    // forward rows: entries (c, L_ic) from the columns c < i, c ascending
+    std::vector<int64_t> fp(n + 1, 0);
+    for (int c = 0; c < n; ++c)
+        for (int t = pntr[c] + 1; t < pntr[c + 1]; ++t) fp[indx[t] + 1]++;
+    for (int i = 0; i < n; ++i) fp[i + 1] += fp[i];
+    std::vector<int> fc(fp[n]);
+    std::vector<double> fv(fp[n]);
+    {
+        std::vector<int64_t> fill(fp.begin(), fp.end() - 1);
+        for (int c = 0; c < n; ++c)
+            for (int t = pntr[c] + 1; t < pntr[c + 1]; ++t) {
+                const int64_t e = fill[indx[t]]++;
+                fc[e] = c;
+                fv[e] = val[t];
+            }
+    }
+    // backward rows: row i's own column below the diagonal, rows ascending
+    std::vector<int64_t> bp(n + 1, 0);
+    for (int i = 0; i < n; ++i) bp[i + 1] = bp[i] + (pntr[i + 1] - pntr[i] - 1);
+    std::vector<int> bc(bp[n]);
+    std::vector<double> bv(bp[n]), dg(n);
+    for (int i = 0; i < n; ++i) {
+        dg[i] = val[pntr[i]];
+        for (int t = pntr[i] + 1; t < pntr[i + 1]; ++t) {
+            bc[bp[i] + (t - pntr[i] - 1)] = indx[t];
+            bv[bp[i] + (t - pntr[i] - 1)] = val[t];
+        }
+    }
+    // level schedules
+    std::vector<int> lf(n, 0), lb(n, 0);
+    int nlf = 0, nlb = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int64_t e = fp[i]; e < fp[i + 1]; ++e) l = std::max(l, lf[fc[e]] + 1);
+        lf[i] = l;
+        nlf = std::max(nlf, l + 1);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int64_t e = bp[i]; e < bp[i + 1]; ++e) l = std::max(l, lb[bc[e]] + 1);
+        lb[i] = l;
+        nlb = std::max(nlb, l + 1);
+    }
+    std::vector<int> frows, brows;
+    group_levels(lf, nlf, frows, F.flev);
+    group_levels(lb, nlb, brows, F.blev);
+    auto up = [&](auto &dst, const auto &src) -> int {
+        using T = typename std::decay_t<decltype(src)>::value_type;
+        OGB_CHECK(dst.alloc(src.empty() ? 1 : src.size()));
+        if (!src.empty())
+            OGB_CUDA(cudaMemcpyAsync(dst.p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        return OGB_OK;
+    };
+    OGB_CHECK(up(F.fptr, fp));
+    OGB_CHECK(up(F.fcol, fc));
+    OGB_CHECK(up(F.fval, fv));
+    OGB_CHECK(up(F.bptr, bp));
+    OGB_CHECK(up(F.bcol, bc));
+    OGB_CHECK(up(F.bval, bv));
+    OGB_CHECK(up(F.diag, dg));
+    OGB_CHECK(up(F.frows, frows));
+    OGB_CHECK(up(F.brows, brows));
+    OGB_CHECK(F.work.alloc(n));
+    OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
+    F.n = n;
+    F.version = m->version;
+    return OGB_OK;
+}
+
+int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
+{
+    IcFactor &F = m->ic;
+    cudaStream_t s = m->ctx->stream;
+    const int nlf = (int)F.flev.size() - 1, nlb = (int)F.blev.size() - 1;
+    for (int l = 0; l < nlf; ++l) {
+        const int r0 = F.flev[l], r1 = F.flev[l + 1];
+        k_ic_fwd<<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p,
+                                                                          F.fval.p, F.diag.p, r, F.work.p, sc);
+    }
+    for (int l = 0; l < nlb; ++l) {
+        const int r0 = F.blev[l], r1 = F.blev[l + 1];
+        k_ic_bwd<<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p,
+                                                                          F.bval.p, F.diag.p, F.work.p, z, sc);
+    }
+    count_launch(m->ctx, nlf + nlb);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+}  // namespace ogb

@@ -171,6 +171,18 @@ struct SellMat {
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
 };
 
+// Incomplete-Cholesky factor of the IML solver's IC preconditioner (icprec.cu):
+// forward rows (entries of the transposed columns), backward rows (each row's
+// own column below the diagonal), the diagonal, and both level schedules.
+struct IcFactor {
+    int64_t version = -1;
+    int n = 0;
+    DBuf<int64_t> fptr, bptr;
+    DBuf<int> fcol, bcol, frows, brows;
+    DBuf<double> fval, bval, diag, work;
+    std::vector<int> flev, blev;   // level starts into frows / brows
+};
+
 // Instances of a batch start on multiples of INST_ALIGN node-space rows.
 constexpr int INST_ALIGN = 1024;
 
@@ -237,6 +249,8 @@ struct ogb_mtrx {
     ogb::DBuf<double> n_b, n_x, n_r64, n_q64;   // node-space FP64 vectors
     ogb::DBuf<float> n_d32;                      // mixed: solution increment since the last replacement
     bool last_half = false;                      // the last mixed solve used the half-stored FP32 copy
+    int precond = 1;                             // IML preconditioner type: 0 none, 1 diagonal, 4 incomplete Cholesky
+    ogb::IcFactor ic;
 };
 
 struct ogb_model {
@@ -321,6 +335,10 @@ int build_sell(ogb_model *md, ogb_mtrx *m);
 // matrix does not fit its index packing); refresh_half copies the current FP32
 // values into it.
 int build_half(ogb_ctx *ctx, SellMat &S);
+// icprec.cu: the IC factor of m (host, cached per matrix version) and z = M^-1 r
+// (device, level-scheduled; kernels skip once sc reports done).
+int build_ic(ogb_mtrx *m);
+int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc);
 int refresh_half(ogb_ctx *ctx, SellMat &S);
 
 // element.cu

@@ -1254,6 +1254,27 @@ int launch_diag_inv(ogb_ctx *ctx, const Op &op, const V *val, X *dinv, PcgScal *
     return OGB_OK;
 }
 
+template <class X>
+__global__ void k_fill_one(int64_t n, X *__restrict__ v)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = (X)1;
+}
+
+// The preconditioner's diagonal: D^-1 (lsprecond 1, DiagPreconditioner) or the
+// identity (lsprecond 0, VoidPreconditioner: plain CG, z = r).
+template <class X, class V>
+int launch_prec_diag(ogb_mtrx *m, const Op &op, const V *val, X *dinv, PcgScal *sc)
+{
+    if (m->precond == 0) {
+        k_fill_one<X><<<NUM_SMS * 8, NTHREADS, 0, m->ctx->stream>>>(op.n, dinv);
+        count_launch(m->ctx);
+        OGB_CUDA(cudaGetLastError());
+        return OGB_OK;
+    }
+    return launch_diag_inv<X, V>(m->ctx, op, val, dinv, sc);
+}
+
 int ensure_workspace(ogb_mtrx *m, const Op &op, bool mixed)
 {
     const int64_t n = op.n;
@@ -1368,7 +1389,7 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
     double *r = m->w_r.p, *z = m->w_z.p, *p = m->w_p.p, *q = m->w_q.p, *dinv = m->w_dinv.p;
     OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
     OGB_CHECK((sell_autotune<double, double, double, false>(ctx, op, val, p, q, m->w_part.p, m->w_count.p, sc + 1)));
-    OGB_CHECK((launch_diag_inv<double, double>(ctx, op, val, dinv, sc)));
+    OGB_CHECK((launch_prec_diag<double, double>(m, op, val, dinv, sc)));
     OGB_CHECK((apply_op<double, double, false>(ctx, op, val, x, q, nullptr, nullptr, nullptr)));
     k_pcg_init<double><<<g, NTHREADS, 0, s>>>(nch, b, q, dinv, r, z, p, m->w_part.p, m->w_count.p, sc, rtol);
     count_launch(ctx);
@@ -1400,6 +1421,137 @@ int pcg64_core(ogb_mtrx *m, const Op &op, const double *val, const double *b, do
             OGB_CHECK(batch());
         }
         it += BATCH;
+    }
+    return OGB_OK;
+}
+
+// ---------------------------------------------------------------- IC-preconditioned CG
+// IML CG (iml/cg.h:22-71) with z = M^-1 r from the incomplete-Cholesky factor
+// (icprec.cu): x += alpha p, r -= alpha q, test ||r|| / ||b||; z = M^-1 r;
+// rho = r.z, beta = rho / rho_1 (none in the first iteration); p = z + beta p;
+// q = A p, alpha = rho / p.q.
+__global__ void __launch_bounds__(NTHREADS) k_ic_init(int64_t n, const double *__restrict__ b,
+                                                      const double *__restrict__ q, double *__restrict__ r,
+                                                      double *part, unsigned int *count, PcgScal *sc, double rtol)
+{
+    int64_t lo, hi;
+    block_range(n, lo, hi);
+    double v[2] = {0, 0};
+    for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) {
+        const double bb = b[row], rr = bb - q[row];
+        r[row] = rr;
+        v[0] += bb * bb;
+        v[1] += rr * rr;
+    }
+    block_sum<2>(v);
+    if (publish_partials<2>(v, part, count)) {
+        double t[2];
+        final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->bnorm2 = t[0];
+        sc->rnorm2 = t[1];
+        double normb = sqrt(t[0]);
+        if (normb == 0.0) normb = 1.0;
+        if (sqrt(t[1]) / normb <= rtol) sc->done = 1;
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_ic_rz(int64_t n, const double *__restrict__ r,
+                                                    const double *__restrict__ z, double *part, unsigned int *count,
+                                                    PcgScal *sc)
+{
+    if (halted(sc)) return;
+    int64_t lo, hi;
+    block_range(n, lo, hi);
+    double v[1] = {0};
+    for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) v[0] += r[row] * z[row];
+    block_sum<1>(v);
+    if (publish_partials<1>(v, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        if (!isfinite(t[0]) || !(t[0] > 0.0)) {
+            sc->done = 2;
+            return;
+        }
+        sc->beta = sc->iters == 0 ? 0.0 : t[0] / sc->rho;
+        sc->rho = t[0];
+        sc->zcoef = 1.0;
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_ic_xr(int64_t n, double *__restrict__ x, double *__restrict__ r,
+                                                    const double *__restrict__ p, const double *__restrict__ q,
+                                                    double *part, unsigned int *count, PcgScal *sc, double rtol,
+                                                    int maxit)
+{
+    if (halted(sc)) return;
+    const double alpha = sc->alpha;
+    int64_t lo, hi;
+    block_range(n, lo, hi);
+    double v[1] = {0};
+    for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) {
+        x[row] += alpha * p[row];
+        const double rr = r[row] - alpha * q[row];
+        r[row] = rr;
+        v[0] += rr * rr;
+    }
+    block_sum<1>(v);
+    if (publish_partials<1>(v, part, count)) {
+        double t[1];
+        final_sums<1>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        double normb = sqrt(sc->bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        if (sqrt(t[0]) / normb <= rtol) sc->done = 1;
+        else if (!isfinite(t[0])) sc->done = 2;
+        else if (sc->iters >= maxit) sc->done = 4;
+    }
+}
+
+int pcg_ic_core(ogb_mtrx *m, const Op &op, const double *b, double *x, double rtol, int maxit, PcgScal &res)
+{
+    ogb_ctx *ctx = m->ctx;
+    cudaStream_t s = ctx->stream;
+    const int gb = bal_grid(op.nchunks());
+    PcgScal *sc = m->w_scal.p;
+    double *r = m->w_r.p, *z = m->w_z.p, *p = m->w_p.p, *q = m->w_q.p;
+    OGB_CHECK(build_ic(m));
+    OGB_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScal), s));
+    OGB_CUDA(cudaMemsetAsync(p, 0, op.n * sizeof(double), s));
+    OGB_CHECK((apply_op<double, double, false>(ctx, op, m->val.p, x, q, nullptr, nullptr, nullptr)));
+    k_ic_init<<<gb, NTHREADS, 0, s>>>(op.n, b, q, r, m->w_part.p, m->w_count.p, sc, rtol);
+    count_launch(ctx);
+    OGB_CUDA(cudaGetLastError());
+    // iterations per captured graph: each holds one launch per level of both solves
+    const int per_it = (int)(m->ic.flev.size() + m->ic.blev.size()) + 4;
+    const int nb_it = std::max(1, std::min(BATCH, 8192 / per_it));
+    auto batch = [&]() -> int {
+        for (int k = 0; k < nb_it; ++k) {
+            OGB_CHECK(launch_ic_solve(m, r, z, sc));
+            k_ic_rz<<<gb, NTHREADS, 0, s>>>(op.n, r, z, m->w_part.p, m->w_count.p, sc);
+            k_pupdate4<double><<<gb, NTHREADS, 0, s>>>(op.n, z, p, sc);
+            count_launch(ctx, 2);
+            OGB_CHECK((apply_op<double, double, true>(ctx, op, m->val.p, p, q, m->w_part.p, m->w_count.p, sc)));
+            k_ic_xr<<<gb, NTHREADS, 0, s>>>(op.n, x, r, p, q, m->w_part.p, m->w_count.p, sc, rtol, maxit);
+            count_launch(ctx);
+        }
+        OGB_CUDA(cudaGetLastError());
+        return OGB_OK;
+    };
+    IterGraph graph;
+    if (ctx->use_graphs) OGB_CHECK(graph.capture(ctx, batch));
+    for (int it = 0;; it += nb_it) {
+        OGB_CHECK(read_scal(m, res));
+        if (ctx->use_graphs && it > 0) graph.harvest(ctx);
+        if (res.done || it >= maxit) break;
+        if (ctx->use_graphs) OGB_CHECK(graph.launch(ctx));
+        else OGB_CHECK(batch());
     }
     return OGB_OK;
 }
@@ -1436,7 +1588,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     if constexpr (F32) OGB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(X), s));
     OGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(P), s));
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
-    OGB_CHECK((launch_diag_inv<X, double>(ctx, op, v64, dinv, sc)));
+    OGB_CHECK((launch_prec_diag<X, double>(m, op, v64, dinv, sc)));
     const bool diff = op.sell && ctx->mixed_diff;
     // the half-stored FP32 copy for large node-block matrices (one warp per slice)
     bool half = false;
@@ -1643,6 +1795,21 @@ static int from_op_space(ogb_mtrx *m, const Op &op, double *x)
 // FP64 drop-in solve on padded equation-space device vectors (padding zero).
 int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
+    if (m->precond == 4) {   // IC: equation space, CSR operator
+        Op op = make_op(m, false);
+        OGB_CHECK(ensure_workspace(m, op, false));
+        PcgScal res{};
+        OGB_CHECK(pcg_ic_core(m, op, b, x, rtol, maxit, res));
+        double normb = sqrt(res.bnorm2);
+        if (normb == 0.0) normb = 1.0;
+        if (info) {
+            info->iterations = res.iters;
+            info->outer = 0;
+            info->achieved = sqrt(res.rnorm2) / normb;
+            info->status = map_status(res.done);
+        }
+        return OGB_OK;
+    }
     const bool use_sell = sell_current(m);
     Op op = make_op(m, use_sell);
     OGB_CHECK(ensure_workspace(m, op, false));
@@ -1666,6 +1833,7 @@ int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, og
 int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
     ogb_ctx *ctx = m->ctx;
+    if (m->precond == 4) return fail(OGB_E_ARG, "the IC preconditioner runs in FP64 only");
     const bool use_sell = sell_current(m);
     Op op = make_op(m, use_sell);
     OGB_CHECK(ensure_workspace(m, op, true));

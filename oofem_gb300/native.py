@@ -96,6 +96,7 @@ SIGNATURES = {
     "ogb_model_reset_state": (_i, [_vp]),
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
     "ogb_model_set_nr_mode": (_i, [_vp, _i]),
+    "ogb_mtrx_set_preconditioner": (_i, [_vp, _i]),
     "ogb_deck_parse_block": (_i, [C.c_char_p, C.c_int64, C.c_int64, C.c_char_p, C.c_char_p, _i, _vp, _vp, _vp, _vp,
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ogb_model_state_bytes": (_i, [_vp, C.POINTER(C.c_size_t)]),
@@ -247,6 +248,10 @@ class GpuCsrMtrx:
     def zero(self):
         _check(self.lib.ogb_mtrx_zero(self.h))
 
+    def set_preconditioner(self, lsprecond: int):
+        """IML lsprecond: 0 none, 1 diagonal (default), 4 incomplete Cholesky (FP64)."""
+        _check(self.lib.ogb_mtrx_set_preconditioner(self.h, int(lsprecond)))
+
     def spmv_forms(self):
         """(FP64 form, FP32 form, warps per slice) of the node-block SpMV."""
         a, b, c = C.c_int(), C.c_int(), C.c_int()
@@ -304,13 +309,15 @@ class GpuPcgSolver:
     """SparseLinearSystemNM::solve with IML CG + Jacobi semantics
     (lstol / lsiter as in IMLSolver::initializeFrom, imlsolver.C:66-98)."""
 
-    def __init__(self, lstol: float = 1e-5, lsiter: int = 200, precision: int = PREC_FP64):
+    def __init__(self, lstol: float = 1e-5, lsiter: int = 200, precision: int = PREC_FP64, lsprecond: int = 1):
         self.tol = lstol
         self.maxit = lsiter
         self.precision = precision
+        self.lsprecond = lsprecond
         self.last = SolveInfo()
 
     def solve(self, A: GpuCsrMtrx, b: np.ndarray, x: np.ndarray) -> int:
+        A.set_preconditioner(self.lsprecond)
         b = np.ascontiguousarray(b, dtype=np.float64)
         assert x.dtype == np.float64 and x.flags.c_contiguous
         info = SolveInfo()
@@ -326,6 +333,7 @@ class GpuPcgSolver:
         arrays (row c = column c of the reference's FloatMatrix); X holds the
         initial guesses and receives the solutions. Per-column iterations,
         achieved residuals and statuses are kept in self.last_multi."""
+        A.set_preconditioner(self.lsprecond)
         B = np.ascontiguousarray(B, dtype=np.float64)
         assert X.dtype == np.float64 and X.flags.c_contiguous and X.shape == B.shape
         nrhs = B.shape[0]

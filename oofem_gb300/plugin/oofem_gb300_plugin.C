@@ -53,6 +53,7 @@ namespace oofem {
 #define _IFT_GpuPcgSolver_lstol "lstol"
 #define _IFT_GpuPcgSolver_lsiter "lsiter"
 #define _IFT_GpuPcgSolver_gpuprec "gpuprec"
+#define _IFT_GpuPcgSolver_lsprecond "lsprecond"
 
 static ogb_ctx *gb300_context()
 {
@@ -296,6 +297,10 @@ protected:
     double tol = 1.e-5;   // IMLSolver defaults (imlsolver.C:66-98)
     int maxite = 200;
     int precision = OGB_PREC_FP64;
+    // IMLSolver's lsprecond numbering (imlsolver.C:78-94): 0 none, 1 diagonal,
+    // 4 incomplete Cholesky. The default is the diagonal one, this solver's
+    // Jacobi-PCG; IMLSolver's own default is 0 (no preconditioner).
+    int precond = 1;
 
 public:
     GpuPcgSolver(Domain *d, EngngModel *m) : SparseLinearSystemNM(d, m) { }
@@ -305,6 +310,7 @@ public:
         IR_GIVE_OPTIONAL_FIELD(ir, tol, _IFT_GpuPcgSolver_lstol);
         IR_GIVE_OPTIONAL_FIELD(ir, maxite, _IFT_GpuPcgSolver_lsiter);
         IR_GIVE_OPTIONAL_FIELD(ir, precision, _IFT_GpuPcgSolver_gpuprec);
+        IR_GIVE_OPTIONAL_FIELD(ir, precond, _IFT_GpuPcgSolver_lsprecond);
     }
 
     ConvergedReason solve(SparseMtrx &A, FloatArray &b, FloatArray &x) override
@@ -317,6 +323,9 @@ public:
             OOFEM_ERROR("size mismatch");
         }
         ogb_solve_info info;
+        if ( ogb_mtrx_set_preconditioner(g->handle(), precond) != OGB_OK ) {
+            OOFEM_ERROR("GpuPcgSolver: %s", ogb_last_error());
+        }
         int r = ogb_pcg_solve(g->handle(), b.givePointer(), x.givePointer(), tol, maxite, precision, & info);
         OOFEM_LOG_INFO("GpuPcg(%s): status %d, nite %d, achieved tol. %g\n",
                        precision == OGB_PREC_MIXED ? "mixed" : "fp64", info.status, info.iterations, info.achieved);
@@ -343,6 +352,9 @@ public:
         }
         if ( X.giveNumberOfRows() != neq || X.giveNumberOfColumns() != nrhs ) {
             X.resize(neq, nrhs);
+        }
+        if ( ogb_mtrx_set_preconditioner(g->handle(), precond) != OGB_OK ) {
+            OOFEM_ERROR("GpuPcgSolver: %s", ogb_last_error());
         }
         std::vector< int > iters(nrhs), status(nrhs);
         std::vector< double > achieved(nrhs);

@@ -179,6 +179,102 @@ def pcg(rowptr, colind, val, b, rtol=1e-12, maxit=100000, x0=None):
     return x, st, it.value, ach.value
 
 
+def ic_factor(rowptr, colind, val):
+    """CompCol_ICPreconditioner::initialize + ICFactor (src/core/iml/icprecond.C:64-163)
+    for a symmetric matrix given as CSR: column k of the lower triangle is row k
+    restricted to columns >= k, diagonal first; the factorization loop is the
+    reference's, including its row search that only matches at the last entry of
+    a column. Returns (pntr, indx, val) of the factor by columns."""
+    n = rowptr.size - 1
+    pntr = np.zeros(n + 1, np.int64)
+    indx, vals = [], []
+    for k in range(n):
+        cols = colind[rowptr[k]:rowptr[k + 1]]
+        sel = cols >= k
+        indx.extend(cols[sel].tolist())
+        vals.extend(val[rowptr[k]:rowptr[k + 1]][sel].tolist())
+        pntr[k + 1] = len(indx)
+        if pntr[k] == pntr[k + 1] or indx[pntr[k]] != k:
+            raise RuntimeError("IC preconditioner: diagonal not found")
+    indx.append(n)   # the successor test of a column's last entry reads the next column's first row
+    v = vals
+    for k in range(n - 1):
+        d = pntr[k]
+        z = v[d] = np.sqrt(v[d])
+        for i in range(d + 1, pntr[k + 1]):
+            v[i] /= z
+        for i in range(d + 1, pntr[k + 1]):
+            zi = v[i]
+            h = indx[i]
+            g = i
+            for j in range(pntr[h], pntr[h + 1]):
+                while g < pntr[k + 1] and indx[g + 1] <= indx[j]:
+                    if indx[g] == indx[j]:
+                        v[j] -= zi * v[g]
+                    g += 1
+    if n:
+        v[pntr[n - 1]] = np.sqrt(v[pntr[n - 1]])
+    return pntr, np.array(indx[:-1], np.int64), np.array(v)
+
+
+def ic_solve(F, x):
+    """CompCol_ICPreconditioner::ICSolve (icprecond.C:166-190): forward and
+    backward solves by columns."""
+    pntr, indx, val = F
+    n = pntr.size - 1
+    dest = np.array(x, dtype=np.float64)
+    work = np.zeros(n)
+    for i in range(n):
+        temp = work[i] = (dest[i] + work[i]) / val[pntr[i]]
+        for t in range(pntr[i] + 1, pntr[i + 1]):
+            work[indx[t]] -= val[t] * temp
+    dest[:] = 0.0
+    for i in range(n - 1, -1, -1):
+        for t in range(pntr[i] + 1, pntr[i + 1]):
+            dest[i] -= val[t] * dest[indx[t]]
+        dest[i] = (work[i] + dest[i]) / val[pntr[i]]
+    return dest
+
+
+def cg_iml(rowptr, colind, val, b, rtol, maxit, precond: int):
+    """IML++ CG (iml/cg.h:22-71) with lsprecond 0 (none), 1 (diagonal) or 4
+    (incomplete Cholesky). Pure Python / numpy: small cases only. Returns
+    (x, status, iterations, achieved) like pcg."""
+    import scipy.sparse as sp
+    n = rowptr.size - 1
+    A = sp.csr_matrix((val, colind, rowptr), shape=(n, n))
+    if precond == 4:
+        F = ic_factor(rowptr, colind, val)
+        msolve = lambda r: ic_solve(F, r)
+    elif precond == 1:
+        d = A.diagonal()
+        msolve = lambda r: r / d
+    else:
+        msolve = lambda r: r.copy()
+    x = np.zeros(n)
+    normb = np.linalg.norm(b)
+    r = b - A @ x
+    if normb == 0.0:
+        normb = 1.0
+    resid = np.linalg.norm(r) / normb
+    if resid <= rtol:
+        return x, 0, 0, resid
+    rho_1, p = 0.0, None
+    for i in range(1, maxit + 1):
+        z = msolve(r)
+        rho = float(r @ z)
+        p = z.copy() if i == 1 else z + (rho / rho_1) * p
+        q = A @ p
+        alpha = rho / float(p @ q)
+        x += alpha * p
+        r -= alpha * q
+        resid = np.linalg.norm(r) / normb
+        if resid <= rtol:
+            return x, 0, i, resid
+        rho_1 = rho
+    return x, 1, maxit, resid
+
+
 def mesh_dict(mesh) -> dict:
     """Arrays of a meshgen.Mesh in the fixture layout."""
     return dict(etype=mesh.elem_type, coords=mesh.coords, conn=mesh.conn, elem_mat=mesh.elem_mat,
@@ -186,10 +282,11 @@ def mesh_dict(mesh) -> dict:
                 nodal_load=mesh.nodal_load, thickness=mesh.thickness)
 
 
-def linear_static(m: dict, rtol=1e-12, maxit=100000, load_factor=1.0, bc_factor=1.0):
+def linear_static(m: dict, rtol=1e-12, maxit=100000, load_factor=1.0, bc_factor=1.0, precond: int = 1):
     """LinearStatic::solveYourselfAt (linearstatic.C:177-253): K, load vector
-    f_ext - f_int(prescribed u), Jacobi-PCG, then reactions
-    (StructuralEngngModel::computeReaction, structengngmodel.C:183-201)."""
+    f_ext - f_int(prescribed u), Jacobi-PCG (or IML CG with lsprecond 0 / 4,
+    cg_iml), then reactions (StructuralEngngModel::computeReaction,
+    structengngmodel.C:183-201)."""
     et = int(m["etype"])
     bc_mask = np.asarray(m["bc_mask"])
     neq, npeq, eq = number_equations(bc_mask)
@@ -202,7 +299,10 @@ def linear_static(m: dict, rtol=1e-12, maxit=100000, load_factor=1.0, bc_factor=
     free = eq > 0
     b = np.zeros(neq)
     b[eq[free] - 1] = fext[free] - fint[free]
-    x, status, iters, ach = pcg(rowptr, colind, val, b, rtol, maxit)
+    if precond == 1:
+        x, status, iters, ach = pcg(rowptr, colind, val, b, rtol, maxit)
+    else:
+        x, status, iters, ach = cg_iml(rowptr, colind, val, b, rtol, maxit, precond)
     u_node[free] = x[eq[free] - 1]
     fint, sig, eps = internal_forces(m, u_node)
     reac = np.where(bc_mask == 1, fint - fext, 0.0)

@@ -225,6 +225,19 @@ def main():
             "hex_cantilever_6x3x3_jit", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work),
         "quad_rve_8_s3": lambda: [run_case(
             f"quad_rve_8_s3_lc{lc}", mg.quad_rve(8, seed=3, load_case=lc), args.work) for lc in range(3)],
+        # IML CG with the incomplete-Cholesky and with no preconditioner (lsprecond 4 / 0), CompCol matrix
+        "hex_cantilever_6x3x3_jit_ic": lambda: run_case(
+            "hex_cantilever_6x3x3_jit_ic", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work,
+            analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 4",
+            extra=dict(lsprecond=np.int32(4), lstol=np.float64(1e-10))),
+        "quad_rve_8_s3_ic": lambda: run_case(
+            "quad_rve_8_s3_ic", mg.quad_rve(8, seed=3, load_case=2), args.work,
+            analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 4",
+            extra=dict(lsprecond=np.int32(4), lstol=np.float64(1e-10))),
+        "hex_cantilever_6x3x3_jit_void": lambda: run_case(
+            "hex_cantilever_6x3x3_jit_void", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work,
+            analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 0",
+            extra=dict(lsprecond=np.int32(0), lstol=np.float64(1e-10))),
         "tet_cube_3_jit": lambda: run_case(
             "tet_cube_3_jit", mg.tet_cube_linear(3, jitter=0.15, seed=5), args.work),
         "mises_hex_4x2x2": lambda: nonlinear(

@@ -305,3 +305,34 @@ def test_half_stored_fp32_operator(kind, native_lib, oracle):
     assert np.array_equal(out[2][0][0], out[2][1][0]) and out[2][0][1] == out[2][1][1]
     with pytest.raises(native_lib.OgbError):
         native_lib.Context(0).set_option(native_lib.OPT_SPMV_HALF, 3)
+
+
+@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_void"])
+def test_iml_preconditioners(case, ctx, native_lib, oracle):
+    """lsprecond 4 (incomplete Cholesky: the reference's factorization, level-
+    scheduled triangular solves on the device) and 0 (plain CG) against the
+    reference's runs: CG iterations within one of its log line, displacements
+    within 1e-9; the drop-in solver class gives the same on the assembled
+    matrix. IC is FP64 only; ILU is refused."""
+    g = load_golden(case)
+    mesh = mesh_from_golden(g)
+    model = native_lib.GpuModel(ctx, mesh)
+    A = native_lib.GpuCsrMtrx(ctx)
+    pc = int(g["lsprecond"])
+    A.set_preconditioner(pc)
+    u, reac, info = model.linear_static(A, rtol=float(g["lstol"]))
+    assert info.status == 0
+    assert abs(info.iterations - int(g["cg_nite"][0])) <= 1, (info.iterations, int(g["cg_nite"][0]))
+    assert rel(u, g["s1_u"]) < 1e-9
+    assert rel(reac, g["s1_reac"]) < 1e-9
+    ref = oracle.linear_static(g, rtol=float(g["lstol"]), precond=pc)
+    solver = native_lib.GpuPcgSolver(lstol=float(g["lstol"]), lsiter=100000, lsprecond=pc)
+    x = np.zeros(ref["neq"])
+    assert solver.solve(A, ref["b"], x) == 0
+    assert abs(solver.last.iterations - ref["iters"]) <= 1
+    assert rel(x, ref["x"]) < 1e-9
+    if pc == 4:
+        with pytest.raises(native_lib.OgbError):
+            model.linear_static(A, rtol=1e-8, precision=native_lib.PREC_MIXED)
+    with pytest.raises(native_lib.OgbError):
+        A.set_preconditioner(2)

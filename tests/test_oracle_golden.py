@@ -139,3 +139,17 @@ def test_static_structural(case, oracle):
         assert rel(r["reac"], g[f"s{k}_reac"]) < 1e-8
         assert rel(r["stress"], g[f"s{k}_stress"]) < 1e-8
         assert rel(r["state"][:, 6], g[f"s{k}_kappa"].ravel()) < 1e-8
+
+
+@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_void"])
+def test_iml_cg_preconditioners(case, oracle):
+    """IML CG with the incomplete-Cholesky preconditioner (lsprecond 4, the
+    reference's factorization loop) and without one (lsprecond 0) against the
+    reference's runs: the CG iteration count from its log line and the
+    displacements."""
+    g = load_golden(case)
+    r = oracle.linear_static(g, rtol=float(g["lstol"]), precond=int(g["lsprecond"]))
+    assert r["status"] == 0
+    assert abs(r["iters"] - int(g["cg_nite"][0])) <= 1, (r["iters"], int(g["cg_nite"][0]))
+    assert rel(r["u"], g["s1_u"]) < 1e-8
+    assert rel(r["reac"], g["s1_reac"]) < 1e-8
