@@ -158,11 +158,13 @@ OGB_API int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value);
 /* Preconditioner of the solves on this matrix, numbered as the IML solver's
  * `lsprecond` (IMLSolver::initializeFrom, src/core/iml/imlsolver.C:78-94):
  * 0 = none (VoidPreconditioner, plain CG), 1 = diagonal (DiagPreconditioner,
- * the default here), 4 = incomplete Cholesky (CompCol_ICPreconditioner,
- * src/core/iml/icprecond.C: the reference's factorization loop on the host,
- * once per matrix version; its two triangular solves level by level on the
- * device, FP64 only, equation-space CSR operator). 2 / 3 (ILU) give OGB_E_ARG.
- * Batched solves (ogb_batch_*) use the diagonal preconditioner only. */
+ * the default here), 2 = ILU by columns (CompCol_ILUPreconditioner,
+ * src/core/iml/iluprecond.C), 4 = incomplete Cholesky
+ * (CompCol_ICPreconditioner, src/core/iml/icprecond.C). For 2 and 4 the
+ * reference's factorization loop runs on the host once per matrix version and
+ * the two triangular solves run level by level on the device (FP64 only,
+ * equation-space CSR operator). 3 (threshold ILU of a DynCompRow matrix) gives
+ * OGB_E_ARG. Batched solves (ogb_batch_*) use the diagonal preconditioner only. */
 OGB_API int ogb_mtrx_set_preconditioner(ogb_mtrx *m, int type);
 /* Node-block SpMV forms in use for this matrix (0 = not tuned yet, or no
  * node-block copy): the OGB_OPT_SPMV_VARIANT numbers 1..4 chosen for FP64 and

@@ -589,8 +589,8 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
 int ogb_mtrx_set_preconditioner(ogb_mtrx *m, int type)
 {
     if (!m) return fail(OGB_E_ARG, "null argument");
-    if (type == 2 || type == 3) return fail(OGB_E_ARG, "ILU preconditioners (lsprecond 2, 3) are not built");
-    if (type != 0 && type != 1 && type != 4) return fail(OGB_E_ARG, "unknown preconditioner type");
+    if (type == 3) return fail(OGB_E_ARG, "the threshold ILU of compressed rows (lsprecond 3) is not built");
+    if (type != 0 && type != 1 && type != 2 && type != 4) return fail(OGB_E_ARG, "unknown preconditioner type");
     m->precond = type;
     return OGB_OK;
 }

@@ -20,6 +20,13 @@
 // the reference's order (columns resp. rows ascending, starting from zero) with
 // separate rounded multiply and subtract, so z = M^-1 r is bitwise the
 // reference's.
+//
+// lsprecond 2 (CompCol_ILUPreconditioner, src/core/iml/iluprecond.C:75-193,
+// 265-289) is built the same way: the matrix split by columns into a strictly
+// lower L (unit diagonal implied) and an upper U with the diagonal last, the
+// reference's factorization loop, and its solves L w = x (columns ascending,
+// each row's sum started from zero and x added last) and U y = w (columns
+// descending, each row's sum started from w).
 #include <math.h>
 
 #include <algorithm>
@@ -59,6 +66,35 @@ __global__ void k_ic_bwd(int r0, int r1, const int *__restrict__ rows, const int
     y[i] = __ddiv_rn(__dadd_rn(w[i], acc), diag[i]);
 }
 
+// ILU: w_i = (sum over c < i, ascending, of -L_ic w_c) + x_i.
+__global__ void k_ilu_fwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
+                          const int *__restrict__ col, const double *__restrict__ val, const double *__restrict__ x,
+                          double *__restrict__ w, const PcgScal *sc)
+{
+    if (sc && (sc->done || sc->reliable)) return;
+    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= r1) return;
+    const int i = rows[t];
+    double acc = 0.0;
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], w[col[e]]));
+    w[i] = __dadd_rn(acc, x[i]);
+}
+
+// ILU: y_i = (w_i - sum over c > i, descending, of U_ic y_c) / U_ii.
+__global__ void k_ilu_bwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
+                          const int *__restrict__ col, const double *__restrict__ val,
+                          const double *__restrict__ diag, const double *__restrict__ w, double *__restrict__ y,
+                          const PcgScal *sc)
+{
+    if (sc && (sc->done || sc->reliable)) return;
+    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= r1) return;
+    const int i = rows[t];
+    double acc = w[i];
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], y[col[e]]));
+    y[i] = __ddiv_rn(acc, diag[i]);
+}
+
 // Rows grouped by level (counting sort, rows ascending within a level).
 void group_levels(const std::vector<int> &lev, int nlev, std::vector<int> &rows, std::vector<int> &start)
 {
@@ -72,20 +108,171 @@ void group_levels(const std::vector<int> &lev, int nlev, std::vector<int> &rows,
 
 }  // namespace
 
-int build_ic(ogb_mtrx *m)
+namespace {
+
+// Device copy of a factor given by its forward / backward rows and diagonal.
+int upload_factor(ogb_mtrx *m, int kind, const std::vector<int64_t> &fp, const std::vector<int> &fc,
+                  const std::vector<double> &fv, const std::vector<int64_t> &bp, const std::vector<int> &bc,
+                  const std::vector<double> &bv, const std::vector<double> &dg)
 {
     IcFactor &F = m->ic;
-    if (F.version == m->version) return OGB_OK;
+    cudaStream_t s = m->ctx->stream;
+    const int n = (int)dg.size();
+    std::vector<int> lf(n, 0), lb(n, 0);
+    int nlf = 0, nlb = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int64_t e = fp[i]; e < fp[i + 1]; ++e) l = std::max(l, lf[fc[e]] + 1);
+        lf[i] = l;
+        nlf = std::max(nlf, l + 1);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int64_t e = bp[i]; e < bp[i + 1]; ++e) l = std::max(l, lb[bc[e]] + 1);
+        lb[i] = l;
+        nlb = std::max(nlb, l + 1);
+    }
+    std::vector<int> frows, brows;
+    group_levels(lf, nlf, frows, F.flev);
+    group_levels(lb, nlb, brows, F.blev);
+    auto up = [&](auto &dst, const auto &src) -> int {
+        using T = typename std::decay_t<decltype(src)>::value_type;
+        OGB_CHECK(dst.alloc(src.empty() ? 1 : src.size()));
+        if (!src.empty())
+            OGB_CUDA(cudaMemcpyAsync(dst.p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        return OGB_OK;
+    };
+    OGB_CHECK(up(F.fptr, fp));
+    OGB_CHECK(up(F.fcol, fc));
+    OGB_CHECK(up(F.fval, fv));
+    OGB_CHECK(up(F.bptr, bp));
+    OGB_CHECK(up(F.bcol, bc));
+    OGB_CHECK(up(F.bval, bv));
+    OGB_CHECK(up(F.diag, dg));
+    OGB_CHECK(up(F.frows, frows));
+    OGB_CHECK(up(F.brows, brows));
+    OGB_CHECK(F.work.alloc(n > 0 ? n : 1));
+    OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
+    F.n = n;
+    F.kind = kind;
+    F.version = m->version;
+    return OGB_OK;
+}
+
+// The matrix by rows on the host (npad rows, identity padding included).
+int host_csr(ogb_mtrx *m, std::vector<int64_t> &rp, std::vector<int> &ci, std::vector<double> &va)
+{
     cudaStream_t s = m->ctx->stream;
     const int n = m->npad;
     const int64_t ntot = m->nnz + (m->npad - m->neq);
-    std::vector<int64_t> rp(n + 1);
-    std::vector<int> ci(ntot);
-    std::vector<double> va(ntot);
+    rp.resize(n + 1);
+    ci.resize(ntot);
+    va.resize(ntot);
     OGB_CUDA(cudaMemcpyAsync(rp.data(), m->rowptr.p, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     OGB_CUDA(cudaMemcpyAsync(ci.data(), m->colind.p, ntot * sizeof(int), cudaMemcpyDeviceToHost, s));
     OGB_CUDA(cudaMemcpyAsync(va.data(), m->val.p, ntot * sizeof(double), cudaMemcpyDeviceToHost, s));
     OGB_CUDA(cudaStreamSynchronize(s));
+    return OGB_OK;
+}
+
+int build_ilu(ogb_mtrx *m)
+{
+    std::vector<int64_t> rp;
+    std::vector<int> ci;
+    std::vector<double> va;
+    OGB_CHECK(host_csr(m, rp, ci, va));
+    const int n = m->npad;
+    // column i of the (symmetric) matrix = row i: L takes rows > i, U rows <= i
+    // (CompCol_ILUPreconditioner::initialize, iluprecond.C:75-130)
+    std::vector<int> lp(n + 1, 0), up_(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        int l = 0, u = 0;
+        for (int64_t j = rp[i]; j < rp[i + 1]; ++j) (ci[j] > i ? l : u) += 1;
+        lp[i + 1] = lp[i] + l;
+        up_[i + 1] = up_[i] + u;
+    }
+    std::vector<int> lr(lp[n]), ur(up_[n]);
+    std::vector<double> lv(lp[n]), uv(up_[n]);
+    for (int i = 0; i < n; ++i) {
+        int a = lp[i], b = up_[i];
+        for (int64_t j = rp[i]; j < rp[i + 1]; ++j) {
+            if (ci[j] > i) {
+                lr[a] = ci[j];
+                lv[a++] = va[j];
+            } else {
+                ur[b] = ci[j];
+                uv[b++] = va[j];
+            }
+        }
+        if (up_[i + 1] == up_[i] || ur[up_[i + 1] - 1] != i)
+            return fail(OGB_E_ZERODIAG, "ILU preconditioner: diagonal not found");
+    }
+    // the factorization loop (iluprecond.C:134-167)
+    for (int i = 0; i < n - 1; ++i) {
+        double multiplier = uv[up_[i + 1] - 1];
+        for (int j = lp[i]; j < lp[i + 1]; ++j) lv[j] /= multiplier;
+        for (int j = up_[i + 1]; j < up_[i + 2] - 1; ++j) {
+            multiplier = uv[j];
+            int qn = j + 1, rn = lp[i + 1], pn;
+            for (pn = lp[ur[j]]; pn < lp[ur[j] + 1] && lr[pn] <= i + 1; ++pn) {
+                while (qn < up_[i + 2] && ur[qn] < lr[pn]) ++qn;
+                if (qn < up_[i + 2] && lr[pn] == ur[qn]) uv[qn] -= multiplier * lv[pn];
+            }
+            for (; pn < lp[ur[j] + 1]; ++pn) {
+                while (rn < lp[i + 2] && lr[rn] < lr[pn]) ++rn;
+                if (rn < lp[i + 2] && lr[pn] == lr[rn]) lv[rn] -= multiplier * lv[pn];
+            }
+        }
+    }
+    // forward rows: (c, L_ic) from the columns c < i, c ascending
+    std::vector<int64_t> fp(n + 1, 0);
+    for (int c = 0; c < n; ++c)
+        for (int t = lp[c]; t < lp[c + 1]; ++t) fp[lr[t] + 1]++;
+    for (int i = 0; i < n; ++i) fp[i + 1] += fp[i];
+    std::vector<int> fc(fp[n]);
+    std::vector<double> fv(fp[n]);
+    {
+        std::vector<int64_t> fill(fp.begin(), fp.end() - 1);
+        for (int c = 0; c < n; ++c)
+            for (int t = lp[c]; t < lp[c + 1]; ++t) {
+                const int64_t e = fill[lr[t]]++;
+                fc[e] = c;
+                fv[e] = lv[t];
+            }
+    }
+    // backward rows: (c, U_rc) from the columns c > r, c descending; the diagonal
+    std::vector<int64_t> bp(n + 1, 0);
+    for (int c = 0; c < n; ++c)
+        for (int t = up_[c]; t < up_[c + 1] - 1; ++t) bp[ur[t] + 1]++;
+    for (int i = 0; i < n; ++i) bp[i + 1] += bp[i];
+    std::vector<int> bc(bp[n]);
+    std::vector<double> bv(bp[n]), dg(n);
+    {
+        std::vector<int64_t> fill(bp.begin(), bp.end() - 1);
+        for (int c = n - 1; c >= 0; --c) {
+            dg[c] = uv[up_[c + 1] - 1];
+            for (int t = up_[c]; t < up_[c + 1] - 1; ++t) {
+                const int64_t e = fill[ur[t]]++;
+                bc[e] = c;
+                bv[e] = uv[t];
+            }
+        }
+    }
+    return upload_factor(m, 2, fp, fc, fv, bp, bc, bv, dg);
+}
+
+}  // namespace
+
+int build_ic(ogb_mtrx *m)
+{
+    IcFactor &F = m->ic;
+    if (F.version == m->version && F.kind == m->precond) return OGB_OK;
+    if (m->precond == 2) return build_ilu(m);
+    const int n = m->npad;
+    std::vector<int64_t> rp;
+    std::vector<int> ci;
+    std::vector<double> va;
+    OGB_CHECK(host_csr(m, rp, ci, va));
     // lower triangle by columns (CompCol_ICPreconditioner::initialize, icprecond.C:64-107)
     std::vector<int> pntr(n + 1, 0);
     for (int k = 0; k < n; ++k) {
@@ -153,45 +340,7 @@ int build_ic(ogb_mtrx *m)
             bv[bp[i] + (t - pntr[i] - 1)] = val[t];
         }
     }
-    // level schedules
-    std::vector<int> lf(n, 0), lb(n, 0);
-    int nlf = 0, nlb = 0;
-    for (int i = 0; i < n; ++i) {
-        int l = 0;
-        for (int64_t e = fp[i]; e < fp[i + 1]; ++e) l = std::max(l, lf[fc[e]] + 1);
-        lf[i] = l;
-        nlf = std::max(nlf, l + 1);
-    }
-    for (int i = n - 1; i >= 0; --i) {
-        int l = 0;
-        for (int64_t e = bp[i]; e < bp[i + 1]; ++e) l = std::max(l, lb[bc[e]] + 1);
-        lb[i] = l;
-        nlb = std::max(nlb, l + 1);
-    }
-    std::vector<int> frows, brows;
-    group_levels(lf, nlf, frows, F.flev);
-    group_levels(lb, nlb, brows, F.blev);
-    auto up = [&](auto &dst, const auto &src) -> int {
-        using T = typename std::decay_t<decltype(src)>::value_type;
-        OGB_CHECK(dst.alloc(src.empty() ? 1 : src.size()));
-        if (!src.empty())
-            OGB_CUDA(cudaMemcpyAsync(dst.p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-        return OGB_OK;
-    };
-    OGB_CHECK(up(F.fptr, fp));
-    OGB_CHECK(up(F.fcol, fc));
-    OGB_CHECK(up(F.fval, fv));
-    OGB_CHECK(up(F.bptr, bp));
-    OGB_CHECK(up(F.bcol, bc));
-    OGB_CHECK(up(F.bval, bv));
-    OGB_CHECK(up(F.diag, dg));
-    OGB_CHECK(up(F.frows, frows));
-    OGB_CHECK(up(F.brows, brows));
-    OGB_CHECK(F.work.alloc(n));
-    OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
-    F.n = n;
-    F.version = m->version;
-    return OGB_OK;
+    return upload_factor(m, 4, fp, fc, fv, bp, bc, bv, dg);
 }
 
 int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
@@ -201,13 +350,22 @@ int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
     const int nlf = (int)F.flev.size() - 1, nlb = (int)F.blev.size() - 1;
     for (int l = 0; l < nlf; ++l) {
         const int r0 = F.flev[l], r1 = F.flev[l + 1];
-        k_ic_fwd<<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p,
-                                                                          F.fval.p, F.diag.p, r, F.work.p, sc);
+        const unsigned g = (unsigned)ceil_div(r1 - r0, NTHREADS);
+        if (F.kind == 2)
+            k_ilu_fwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, r, F.work.p, sc);
+        else
+            k_ic_fwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p,
+                                            sc);
     }
     for (int l = 0; l < nlb; ++l) {
         const int r0 = F.blev[l], r1 = F.blev[l + 1];
-        k_ic_bwd<<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p,
-                                                                          F.bval.p, F.diag.p, F.work.p, z, sc);
+        const unsigned g = (unsigned)ceil_div(r1 - r0, NTHREADS);
+        if (F.kind == 2)
+            k_ilu_bwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
+                                             sc);
+        else
+            k_ic_bwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
+                                            sc);
     }
     count_launch(m->ctx, nlf + nlb);
     OGB_CUDA(cudaGetLastError());

@@ -176,6 +176,7 @@ struct SellMat {
 // own column below the diagonal), the diagonal, and both level schedules.
 struct IcFactor {
     int64_t version = -1;
+    int kind = 0;   // 4 incomplete Cholesky, 2 ILU (lsprecond)
     int n = 0;
     DBuf<int64_t> fptr, bptr;
     DBuf<int> fcol, bcol, frows, brows;
@@ -249,7 +250,7 @@ struct ogb_mtrx {
     ogb::DBuf<double> n_b, n_x, n_r64, n_q64;   // node-space FP64 vectors
     ogb::DBuf<float> n_d32;                      // mixed: solution increment since the last replacement
     bool last_half = false;                      // the last mixed solve used the half-stored FP32 copy
-    int precond = 1;                             // IML preconditioner type: 0 none, 1 diagonal, 4 incomplete Cholesky
+    int precond = 1;                             // IML preconditioner type: 0 none, 1 diagonal, 2 ILU, 4 incomplete Cholesky
     ogb::IcFactor ic;
 };
 

@@ -1795,7 +1795,7 @@ static int from_op_space(ogb_mtrx *m, const Op &op, double *x)
 // FP64 drop-in solve on padded equation-space device vectors (padding zero).
 int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
-    if (m->precond == 4) {   // IC: equation space, CSR operator
+    if (m->precond == 4 || m->precond == 2) {   // IC / ILU: equation space, CSR operator
         Op op = make_op(m, false);
         OGB_CHECK(ensure_workspace(m, op, false));
         PcgScal res{};
@@ -1833,7 +1833,8 @@ int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, og
 int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info)
 {
     ogb_ctx *ctx = m->ctx;
-    if (m->precond == 4) return fail(OGB_E_ARG, "the IC preconditioner runs in FP64 only");
+    if (m->precond == 4 || m->precond == 2)
+        return fail(OGB_E_ARG, "the IC and ILU preconditioners run in FP64 only");
     const bool use_sell = sell_current(m);
     Op op = make_op(m, use_sell);
     OGB_CHECK(ensure_workspace(m, op, true));

@@ -236,9 +236,67 @@ def ic_solve(F, x):
     return dest
 
 
+def ilu_factor(rowptr, colind, val):
+    """CompCol_ILUPreconditioner::initialize (src/core/iml/iluprecond.C:75-167):
+    column i of the symmetric matrix (= row i) split into L (rows > i) and U
+    (rows <= i, the diagonal last), then the reference's factorization loop.
+    Returns (lp, lr, lv, up, ur, uv) by columns."""
+    n = rowptr.size - 1
+    lp, up_ = [0], [0]
+    lr, lv, ur, uv = [], [], [], []
+    for i in range(n):
+        for j in range(rowptr[i], rowptr[i + 1]):
+            if colind[j] > i:
+                lr.append(int(colind[j]))
+                lv.append(float(val[j]))
+            else:
+                ur.append(int(colind[j]))
+                uv.append(float(val[j]))
+        lp.append(len(lr))
+        up_.append(len(ur))
+    for i in range(n - 1):
+        multiplier = uv[up_[i + 1] - 1]
+        for j in range(lp[i], lp[i + 1]):
+            lv[j] /= multiplier
+        for j in range(up_[i + 1], up_[i + 2] - 1):
+            multiplier = uv[j]
+            qn, rn = j + 1, lp[i + 1]
+            pn = lp[ur[j]]
+            while pn < lp[ur[j] + 1] and lr[pn] <= i + 1:
+                while qn < up_[i + 2] and ur[qn] < lr[pn]:
+                    qn += 1
+                if qn < up_[i + 2] and lr[pn] == ur[qn]:
+                    uv[qn] -= multiplier * lv[pn]
+                pn += 1
+            while pn < lp[ur[j] + 1]:
+                while rn < lp[i + 2] and lr[rn] < lr[pn]:
+                    rn += 1
+                if rn < lp[i + 2] and lr[pn] == lr[rn]:
+                    lv[rn] -= multiplier * lv[pn]
+                pn += 1
+    return lp, lr, lv, up_, ur, uv
+
+
+def ilu_solve(F, x):
+    """CompCol_ILUPreconditioner::solve (iluprecond.C:265-289)."""
+    lp, lr, lv, up_, ur, uv = F
+    n = len(lp) - 1
+    work = np.zeros(n)
+    for i in range(n):
+        work[i] += x[i]
+        for t in range(lp[i], lp[i + 1]):
+            work[lr[t]] -= lv[t] * work[i]
+    y = np.zeros(n)
+    for i in range(n - 1, -1, -1):
+        y[i] = work[i] / uv[up_[i + 1] - 1]
+        for t in range(up_[i], up_[i + 1] - 1):
+            work[ur[t]] -= uv[t] * y[i]
+    return y
+
+
 def cg_iml(rowptr, colind, val, b, rtol, maxit, precond: int):
-    """IML++ CG (iml/cg.h:22-71) with lsprecond 0 (none), 1 (diagonal) or 4
-    (incomplete Cholesky). Pure Python / numpy: small cases only. Returns
+    """IML++ CG (iml/cg.h:22-71) with lsprecond 0 (none), 1 (diagonal), 2 (ILU
+    by columns) or 4 (incomplete Cholesky). Pure Python / numpy: small cases only. Returns
     (x, status, iterations, achieved) like pcg."""
     import scipy.sparse as sp
     n = rowptr.size - 1
@@ -246,6 +304,9 @@ def cg_iml(rowptr, colind, val, b, rtol, maxit, precond: int):
     if precond == 4:
         F = ic_factor(rowptr, colind, val)
         msolve = lambda r: ic_solve(F, r)
+    elif precond == 2:
+        F = ilu_factor(rowptr, colind, val)
+        msolve = lambda r: ilu_solve(F, r)
     elif precond == 1:
         d = A.diagonal()
         msolve = lambda r: r / d

@@ -19,10 +19,10 @@ def load_golden(name: str) -> dict:
     return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
 
 
-# LinearStatic goldens solved with the direct solver (the _ic / _void cases are
+# LinearStatic goldens solved with the direct solver (the _ic / _ilu / _void cases are
 # CG runs to 1e-10 and have tests of their own)
 LINEAR_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                      if "mises" not in p and "idm" not in p and not p.endswith(("_ic.npz", "_void.npz")))
+                      if "mises" not in p and "idm" not in p and not p.endswith(("_ic.npz", "_ilu.npz", "_void.npz")))
 
 
 @pytest.fixture(scope="session")

@@ -234,6 +234,14 @@ def main():
             "quad_rve_8_s3_ic", mg.quad_rve(8, seed=3, load_case=2), args.work,
             analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 4",
             extra=dict(lsprecond=np.int32(4), lstol=np.float64(1e-10))),
+        "hex_cantilever_6x3x3_jit_ilu": lambda: run_case(
+            "hex_cantilever_6x3x3_jit_ilu", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work,
+            analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 2",
+            extra=dict(lsprecond=np.int32(2), lstol=np.float64(1e-10))),
+        "tet_cube_3_jit_ilu": lambda: run_case(
+            "tet_cube_3_jit_ilu", mg.tet_cube_linear(3, jitter=0.15, seed=5), args.work,
+            analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 2",
+            extra=dict(lsprecond=np.int32(2), lstol=np.float64(1e-10))),
         "hex_cantilever_6x3x3_jit_void": lambda: run_case(
             "hex_cantilever_6x3x3_jit_void", mg.hex_cantilever(6, 3, 3, jitter=0.2, seed=7), args.work,
             analysis="LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 lsprecond 0",

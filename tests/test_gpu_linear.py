@@ -307,13 +307,15 @@ def test_half_stored_fp32_operator(kind, native_lib, oracle):
         native_lib.Context(0).set_option(native_lib.OPT_SPMV_HALF, 3)
 
 
-@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_void"])
+@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_ilu",
+                                  "tet_cube_3_jit_ilu", "hex_cantilever_6x3x3_jit_void"])
 def test_iml_preconditioners(case, ctx, native_lib, oracle):
-    """lsprecond 4 (incomplete Cholesky: the reference's factorization, level-
-    scheduled triangular solves on the device) and 0 (plain CG) against the
+    """lsprecond 4 (incomplete Cholesky) and 2 (column ILU): the reference's
+    factorizations, level-scheduled triangular solves on the device; and 0
+    (plain CG); against the
     reference's runs: CG iterations within one of its log line, displacements
     within 1e-9; the drop-in solver class gives the same on the assembled
-    matrix. IC is FP64 only; ILU is refused."""
+    matrix. IC and ILU are FP64 only; the threshold ILU (3) is refused."""
     g = load_golden(case)
     mesh = mesh_from_golden(g)
     model = native_lib.GpuModel(ctx, mesh)
@@ -331,8 +333,8 @@ def test_iml_preconditioners(case, ctx, native_lib, oracle):
     assert solver.solve(A, ref["b"], x) == 0
     assert abs(solver.last.iterations - ref["iters"]) <= 1
     assert rel(x, ref["x"]) < 1e-9
-    if pc == 4:
+    if pc in (2, 4):
         with pytest.raises(native_lib.OgbError):
             model.linear_static(A, rtol=1e-8, precision=native_lib.PREC_MIXED)
     with pytest.raises(native_lib.OgbError):
-        A.set_preconditioner(2)
+        A.set_preconditioner(3)

@@ -141,10 +141,12 @@ def test_static_structural(case, oracle):
         assert rel(r["state"][:, 6], g[f"s{k}_kappa"].ravel()) < 1e-8
 
 
-@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_void"])
+@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "quad_rve_8_s3_ic", "hex_cantilever_6x3x3_jit_ilu",
+                                  "tet_cube_3_jit_ilu", "hex_cantilever_6x3x3_jit_void"])
 def test_iml_cg_preconditioners(case, oracle):
-    """IML CG with the incomplete-Cholesky preconditioner (lsprecond 4, the
-    reference's factorization loop) and without one (lsprecond 0) against the
+    """IML CG with the incomplete-Cholesky (lsprecond 4) and the column ILU
+    (lsprecond 2) preconditioners (the reference's factorization loops) and
+    without one (lsprecond 0) against the
     reference's runs: the CG iteration count from its log line and the
     displacements."""
     g = load_golden(case)
