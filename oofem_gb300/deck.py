@@ -36,6 +36,7 @@ from .engng import ConstantFunction, PiecewiseLinFunction
 
 ELEMENT_TYPES = {"lspace": mg.ELEM_LSPACE, "planestress2d": mg.ELEM_PLANESTRESS2D, "ltrspace": mg.ELEM_LTRSPACE}
 NODES_PER_ELEMENT = {mg.ELEM_LSPACE: 8, mg.ELEM_PLANESTRESS2D: 4, mg.ELEM_LTRSPACE: 4}
+DIRECT_TOL = 1e-12   # PCG tolerance standing in for the reference's direct solver (lstype 0)
 
 
 class DeckError(ValueError):
@@ -476,8 +477,10 @@ class DeckStep:
 def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optional[float] = None):
     """Run the deck's analysis on the GPU path; a list of DeckStep.
 
-    LinearStatic: step k at time k (LinearStatic::giveNextStep, linearstatic.C:146-156), one PCG solve
-    with the deck's lstol / lsiter (IMLSolver defaults 1e-5 / 200 when absent). NonLinearStatic: step k
+    LinearStatic: step k at time k (LinearStatic::giveNextStep, linearstatic.C:146-156), one PCG solve.
+    Decks for an iterative solver (lstype 1 IML, 9 this library) keep its lstol / lsiter / lsprecond
+    (IMLSolver defaults 1e-5 / 200 / none; lstype 9 defaults to the diagonal preconditioner); decks for
+    the default direct solver (lstype 0) get PCG to DIRECT_TOL. NonLinearStatic: step k
     at time (k-1) * deltat (nlinearstatic.C:295-325). StaticStructural: oofem_gb300.engng.StaticStructural.
     ``precision`` / ``lstol`` override the linear solver's arithmetic and tolerance."""
     from . import engng, native
@@ -488,9 +491,14 @@ def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optio
     prec = native.PREC_FP64 if precision is None else precision
     nsteps = a.int("nsteps", 1)
     out: List[DeckStep] = []
+    # lstype 0 (the default, a direct Skyline LDL^T solve) has no device counterpart: such decks are
+    # solved by PCG to DIRECT_TOL; an iterative lstype keeps its lstol / lsiter / lsprecond
+    direct = a.int("lstype", 0) == 0
+    if not direct:
+        K.set_preconditioner(a.int("lsprecond", 0 if a.int("lstype", 0) == 1 else 1))
     if deck.analysis_type == "linearstatic":
-        tol = lstol if lstol is not None else a.float("lstol", 1e-5)
-        maxit = a.int("lsiter", 200)
+        tol = lstol if lstol is not None else (DIRECT_TOL if direct else a.float("lstol", 1e-5))
+        maxit = 1000000 if direct else a.int("lsiter", 200)
         for k in range(1, nsteps + 1):
             t = float(k)
             u, reac, info = model.linear_static(K, deck.bc_value_at(t), deck.nodal_load_at(t), rtol=tol,
@@ -499,7 +507,7 @@ def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optio
                 raise native.OgbError(info.status, f"LinearStatic step {k}: linear solver did not converge")
             out.append(DeckStep(k, t, u, reac, info.iterations))
         return out
-    tol = lstol if lstol is not None else a.float("lstol", 1e-12)
+    tol = lstol if lstol is not None else (DIRECT_TOL if direct else a.float("lstol", 1e-5))
     if deck.analysis_type == "nonlinearstatic":
         if a.int("controlmode", 1) != 1:
             raise DeckError("NonLinearStatic supports controlmode 1 (direct displacement / load control)")

@@ -39,3 +39,23 @@ def test_static_structural_deck_matches_reference(native_lib):
         assert abs(s.iterations - int(g[f"s{k}_nite"])) <= 1
         assert rel(s.u, g[f"s{k}_u"]) < 1e-7
         assert rel(s.reactions, g[f"s{k}_reac"]) < 1e-7
+
+
+@pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "hex_cantilever_6x3x3_jit_ilu",
+                                  "hex_cantilever_6x3x3_jit_void"])
+def test_iterative_solver_deck_keeps_its_preconditioner(case, native_lib, tmp_path):
+    """A LinearStatic deck for the IML solver (lstype 1 with lsprecond 4 / 2 / 0)
+    runs with the same preconditioner: CG iterations within one of the
+    reference's run of that deck, displacements within 1e-9."""
+    import sys
+    from oofem_gb300 import deck as dk
+    from test_gpu_linear import mesh_from_golden
+    sys.path.insert(0, GOLDEN)
+    from decks import write_deck
+    g = load_golden(case)
+    path = str(tmp_path / (case + ".in"))
+    write_deck(mesh_from_golden(g), path, "LinearStatic nsteps 1 lstype 1 smtype 2 lstol 1e-10 lsiter 100000 "
+               f"lsprecond {int(g['lsprecond'])}")
+    steps = dk.run_deck(dk.read_deck(path), ctx=native_lib.Context(0))
+    assert abs(steps[0].iterations - int(g["cg_nite"][0])) <= 1, (steps[0].iterations, int(g["cg_nite"][0]))
+    assert rel(steps[0].u, g["s1_u"]) < 1e-9
