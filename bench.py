@@ -108,6 +108,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+ARGS = None
+
+
+def apply_options(ctx):
+    """Library options given on the command line (defaults: the library's)."""
+    if ARGS is not None and ARGS.mixed_x64 >= 0:
+        ctx.set_option(native.OPT_MIXED_X64, ARGS.mixed_x64)
+
+
 def profile_traffic(form: int):
     """DRAM bytes per SpMV launch of this form from the committed ncu summary (if any)."""
     p = os.path.join(ROOT, "profiles", "spmv_half_traffic.json" if form == 8 else "spmv_traffic.json")
@@ -222,6 +231,7 @@ def run_gpu(args):
                              jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"] + rank)
     nfree = mesh.nfree
     ctx = native.Context(local)
+    apply_options(ctx)
     if args.spmv_variant:
         ctx.set_option(native.OPT_SPMV_VARIANT, args.spmv_variant)
     ctx.set_option(native.OPT_SPMV_HALF, args.spmv_half)
@@ -397,6 +407,7 @@ def run_gpu_batch(args):
     nfree = big.nfree
     bcv_h = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(nrhs)])
     ctx = native.Context(local)
+    apply_options(ctx)
     model = native.GpuModel(ctx, big)
     model.set_instances(ns)
     A = native.GpuCsrMtrx(ctx)
@@ -510,6 +521,7 @@ def run_gpu_newton(args):
     mesh = mg.hex_block_pull(nx, ny, nz, h=h, end_disp=3.0 * eps_y * nx * h)
     nfree = mesh.nfree
     ctx = native.Context(local)
+    apply_options(ctx)
     model = native.GpuModel(ctx, mesh)
     model.set_initial_guess(1)   # IG_Tangent, as for changing Dirichlet values
     A = native.GpuCsrMtrx(ctx)
@@ -587,6 +599,7 @@ def run_gpu_idm1_batch(args):
     big, ns = mg.concat_meshes(meshes)
     nfree = big.nfree
     ctx = native.Context(local)
+    apply_options(ctx)
     model = native.GpuModel(ctx, big)
     model.set_instances(ns)
     A = native.GpuCsrMtrx(ctx)
@@ -655,9 +668,14 @@ def main():
     ap.add_argument("--rve-count", type=int, default=256)
     ap.add_argument("--spmv-variant", type=int, default=0,
                     help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
+    ap.add_argument("--mixed-x64", type=int, default=-1, choices=(-1, 0, 1),
+                    help="mixed solves: 1 accumulate the solution in FP64 every iteration, 0 as an FP32 increment "
+                         "folded at each FP64 residual (OGB_OPT_MIXED_X64; -1 = library default)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()
+    global ARGS
+    ARGS = args
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -31,10 +31,13 @@ namespace {
 struct BatchScal {
     double bnorm2, rho, pq, rnorm2, alpha, beta;
     double mark;   // mixed precision: FP64 residual^2 at the last halving
+    double rrep;   // mixed precision: FP64 residual^2 at the last replacement (the drop test's reference)
     int done;      // 0 running, 1 converged, 2 breakdown, 3 zero pivot, 4 iteration limit, 5 stalled (mixed)
     int iters;
     int pause;     // mixed precision: waits for the next FP64 residual replacement
     int since;     // mixed precision: replacements since the FP64 residual last halved
+    int repl;      // mixed precision: replaced in the last replacement pass, p update pending
+    int pad_;
 };
 
 constexpr int RPT = 4;                       // scalar rows per thread in the vector kernels
@@ -409,24 +412,31 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
 // replaced residual, a running pair keeps it.
 
 // Residual replacement (init: the first one, which also sets ||b|| and p = z).
+// FP64 residual replacement (reliable update) of the pairs that paused -- their
+// recursive FP32 residual dropped by the drop factor since their last
+// replacement, or reached half the tolerance, or the FP32 recurrences ended --
+// and of every pair at init: r = b - K64 x (FP64, stored FP32), z = D^-1 r; per
+// pair ||b||^2 (init), ||r||^2 and r.z; the convergence test on the FP64
+// residual; for pairs that go on, beta = r.z / rho of the last iteration (0 at
+// init) for the pending p = z + beta p (k_bpupdate32 in replacement mode).
+// Pairs that are still running are left alone: their p already holds this
+// iteration's update, so replacing their r and z would break the recurrence.
 template <int NR>
 __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict__ b, const double *__restrict__ q64,
                                                        const float *__restrict__ dinv, float *__restrict__ r,
-                                                       float *__restrict__ z, float *__restrict__ p, double *part,
-                                                       unsigned int *cnt, BatchScal *sc,
-                                                       const int *__restrict__ unit_inst,
+                                                       float *__restrict__ z, double *part, unsigned int *cnt,
+                                                       BatchScal *sc, const int *__restrict__ unit_inst,
                                                        const int64_t *__restrict__ unit_ptr, double rtol, int maxit,
                                                        int init)
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 2)) return;
-    bool live[NR], restart[NR];
+    bool live[NR];
     double v[3 * NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         const BatchScal &s = sc[inst * NR + c];
-        live[c] = s.done == 0;
-        restart[c] = init || s.pause;
+        live[c] = s.done == 0 && (init || s.pause);
         v[c] = 0.0;
         v[NR + c] = 0.0;
         v[2 * NR + c] = 0.0;
@@ -445,7 +455,6 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
             const float zf = rf * di;
             r[k] = rf;
             z[k] = zf;
-            if (restart[c]) p[k] = zf;
             v[c] += bb * bb;
             v[NR + c] += r6 * r6;
             v[2 * NR + c] += (double)(rf * zf);
@@ -461,7 +470,7 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         BatchScal &s = sc[inst * NR + c];
-        if (s.done) continue;
+        if (s.done || !(init || s.pause)) continue;
         if (init) {
             s.bnorm2 = t[c];
             s.iters = 0;
@@ -487,22 +496,27 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
         else if (s.iters >= maxit) s.done = 4;
         else if (!isfinite(rz) || !(rz > 0.0) || s.since >= 6) s.done = 5;
         else {
+            s.beta = init ? 0.0 : rz / s.rho;
             s.rho = rz;
+            s.rrep = t[NR + c];
             s.pause = 0;
+            s.repl = 1;
         }
     }
 }
 
-// x64 += alpha p, r -= alpha q, z = D^-1 r for running pairs (FP32 but x);
-// per pair ||r||^2 and r.z (FP32 per thread and warp, FP64 above), the pause
-// test and beta.
-template <int NR>
-__global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, float *__restrict__ r,
+// x64 += alpha p (X = double), or the FP32 increment since the last residual
+// replacement d += alpha p (X = float, folded into x64 by k_bfold), r -= alpha q,
+// z = D^-1 r for running pairs; per pair ||r||^2 and r.z (FP32 per thread and
+// warp, FP64 above), the pause test and beta.
+template <int NR, class X>
+__global__ void __launch_bounds__(NTHREADS) k_bupdate32(X *__restrict__ x, float *__restrict__ r,
                                                         float *__restrict__ z, const float *__restrict__ p,
                                                         const float *__restrict__ q, const float *__restrict__ dinv,
                                                         double *part, unsigned int *cnt, BatchScal *sc,
                                                         const int *__restrict__ unit_inst,
-                                                        const int64_t *__restrict__ unit_ptr, double rtol, int maxit)
+                                                        const int64_t *__restrict__ unit_ptr, double rtol, int maxit,
+                                                        double drop2)
 {
     const int inst = unit_inst[blockIdx.x];
     if (inst_skip<NR>(sc, inst, 1)) return;
@@ -526,7 +540,8 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
             if (!run[c]) continue;
             const int64_t k = row * NR + c;
             const float pp = p[k];
-            x[k] = fma(alpha[c], (double)pp, x[k]);
+            if constexpr (sizeof(X) == 8) x[k] = fma(alpha[c], (double)pp, x[k]);
+            else x[k] = fmaf((float)alpha[c], pp, x[k]);
             const float rr = fmaf(-(float)alpha[c], q[k], r[k]);
             const float zz = rr * di;
             r[k] = rr;
@@ -549,11 +564,16 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
         if (!pair_running<NR>(s)) continue;
         s.rnorm2 = t[c];
         s.iters += 1;
+        s.repl = 0;
         double normb = sqrt(s.bnorm2);
         if (normb == 0.0) normb = 1.0;
         const double half = 0.5 * rtol * normb;
+        // pause for an FP64 replacement once the recursive residual has dropped by
+        // the drop factor since the last one (or reached half the tolerance); rho
+        // stays that of this iteration's direction for the continuation
         if (!isfinite(t[c]) || !isfinite(t[NR + c])) s.done = 5;
-        else if (t[c] <= half * half || !(t[NR + c] > 0.0) || s.iters >= maxit) s.pause = 1;
+        else if (t[c] <= half * half || t[c] <= drop2 * s.rrep || !(t[NR + c] > 0.0) || s.iters >= maxit)
+            s.pause = 1;
         else {
             s.beta = t[NR + c] / s.rho;
             s.rho = t[NR + c];
@@ -561,18 +581,21 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
     }
 }
 
+// p = z + beta p: mode 0 for the running pairs of an iteration, mode 1 for the
+// pairs a replacement pass just restarted (k_breplace's beta; 0 at init).
 template <int NR>
 __global__ void __launch_bounds__(NTHREADS) k_bpupdate32(const float *__restrict__ z, float *__restrict__ p,
-                                                         const BatchScal *sc, const int *__restrict__ unit_inst)
+                                                         const BatchScal *sc, const int *__restrict__ unit_inst,
+                                                         int mode)
 {
     const int inst = unit_inst[blockIdx.x];
-    if (inst_skip<NR>(sc, inst, 1)) return;
+    if (mode == 0 && inst_skip<NR>(sc, inst, 1)) return;
     bool run[NR];
     float beta[NR];
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         const BatchScal &s = sc[inst * NR + c];
-        run[c] = pair_running<NR>(s);
+        run[c] = mode == 0 ? pair_running<NR>(s) : (s.repl != 0 && s.done == 0);
         beta[c] = (float)s.beta;
     }
 #pragma unroll
@@ -587,12 +610,46 @@ __global__ void __launch_bounds__(NTHREADS) k_bpupdate32(const float *__restrict
     }
 }
 
+// x = 0 for the pairs that ended stalled with a residual above their starting
+// one (or not finite): their FP64 pass must not start from diverged iterates.
+template <int NR>
+__global__ void __launch_bounds__(NTHREADS) k_bzero_diverged(double *__restrict__ x, const BatchScal *sc,
+                                                              const int *__restrict__ unit_inst)
+{
+    const int inst = unit_inst[blockIdx.x];
+    bool zero[NR];
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        const BatchScal &s = sc[inst * NR + c];
+        zero[c] = s.done == 5 && !(s.rnorm2 <= s.bnorm2);
+        any = any || zero[c];
+    }
+    if (!any) return;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < NR; ++c)
+            if (zero[c]) x[row * NR + c] = 0.0;
+    }
+}
+
+// x64 += d, d = 0 (the FP32 increments of the finished cycle).
+__global__ void k_bfold(int64_t n, double *__restrict__ x, float *__restrict__ d)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += (double)d[i];
+        d[i] = 0.f;
+    }
+}
+
 struct BatchWork {
     DBuf<int> vinst, sinst, zero;
     DBuf<int64_t> vptr, sptr;
     DBuf<BatchScal> sc;
     DBuf<double> part, r, z, p, q, dinv, q64;
-    DBuf<float> r32, z32, p32, q32, dinv32;
+    DBuf<float> r32, z32, p32, q32, dinv32, d32;
     DBuf<unsigned int> cnt;
 };
 
@@ -660,6 +717,10 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         OGB_CHECK(w.q32.alloc(nv));
         OGB_CHECK(w.dinv32.alloc(nrows));
         OGB_CHECK(w.q64.alloc(nv));
+        if (!ctx->mixed_x64) {
+            OGB_CHECK(w.d32.alloc(nv));
+            OGB_CUDA(cudaMemsetAsync(w.d32.p, 0, nv * sizeof(float), st));
+        }
     } else {
         OGB_CHECK(w.r.alloc(nv));
         OGB_CHECK(w.z.alloc(nv));
@@ -683,13 +744,27 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             w.sptr.p, 2);
     };
     std::function<void()> iteration;
+    // mixed: the solution accumulates in FP64 directly, or as an FP32 increment
+    // folded into it before every FP64 residual
+    const bool x64 = ctx->mixed_x64;
+    auto fold = [&]() -> int {
+        if (!mixed || x64) return OGB_OK;
+        k_bfold<<<NUM_SMS * 8, NTHREADS, 0, st>>>(nv, x, w.d32.p);
+        count_launch(ctx);
+        OGB_CUDA(cudaGetLastError());
+        return OGB_OK;
+    };
     if (mixed) {
         k_bdiag<ND, float><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv32.p, w.zero.p);
         residual_spmv(w.q64.p);
-        k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.p32.p, w.part.p, w.cnt.p,
-                                                 w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 1);
+        // p starts at zero: the init pass's p = z + 0 p is z
+        OGB_CUDA(cudaMemsetAsync(w.p32.p, 0, nv * sizeof(float), st));
+        k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p, w.sc.p,
+                                                 w.vinst.p, w.vptr.p, rtol, maxit, 1);
+        k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
         const bool diff = ctx->mixed_diff;
-        iteration = [&, diff]() {
+        const double drop2 = ctx->mixed_drop * ctx->mixed_drop;
+        iteration = [&, diff, x64, drop2]() {
             if (diff)
                 k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(
                     S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
@@ -698,9 +773,15 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
                 k_bspmv<ND, NR, true, float, float, false><<<nsu, NTHREADS, 0, st>>>(
                     S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
                     w.sinst.p, w.sptr.p, 1);
-            k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
-                                                      w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit);
-            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p);
+            if (x64)
+                k_bupdate32<NR, double><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p,
+                                                                  w.part.p, w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p,
+                                                                  rtol, maxit, drop2);
+            else
+                k_bupdate32<NR, float><<<nvu, NTHREADS, 0, st>>>(w.d32.p, w.r32.p, w.z32.p, w.p32.p, w.q32.p,
+                                                                 w.dinv32.p, w.part.p, w.cnt.p, w.sc.p, w.vinst.p,
+                                                                 w.vptr.p, rtol, maxit, drop2);
+            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);
         };
     } else {
         k_bdiag<ND, double><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
@@ -731,17 +812,21 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             for (auto &s : res) s.done = 3;
             break;
         }
-        bool all = true, running = false;
+        bool all = true, running = false, paused = false;
         for (auto &s : res) {
             all = all && s.done;
             running = running || (s.done == 0 && s.pause == 0);
+            paused = paused || (s.done == 0 && s.pause != 0);
         }
         if (all || it > maxit + 2 * REPLACE_EVERY) break;
-        if (mixed && (!running || since >= REPLACE_EVERY)) {
+        // replace when nothing runs, or when paused pairs have waited REPLACE_EVERY iterations
+        if (mixed && (!running || (paused && since >= REPLACE_EVERY))) {
+            OGB_CHECK(fold());
             residual_spmv(w.q64.p);
-            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.p32.p, w.part.p,
-                                                     w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
-            count_launch(ctx, 2);
+            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
+                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
+            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
+            count_launch(ctx, 3);
             OGB_CUDA(cudaGetLastError());
             since = 0;
             continue;
@@ -755,6 +840,13 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         OGB_CUDA(cudaGetLastError());
         it += BBATCH;
         since += BBATCH;
+    }
+    OGB_CHECK(fold());   // an exit on the iteration bound leaves the last increments unfolded
+    if (mixed) {
+        // a pair whose FP32 iterates diverged restarts its FP64 pass from zero
+        k_bzero_diverged<NR><<<nvu, NTHREADS, 0, st>>>(x, w.sc.p, w.vinst.p);
+        count_launch(ctx);
+        OGB_CUDA(cudaGetLastError());
     }
     return OGB_OK;
 }

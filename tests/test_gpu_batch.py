@@ -216,3 +216,25 @@ def test_batch_mixed_below_fp32_reach_finishes_in_fp64(ctx, native_lib):
         assert (st == 0).all(), (prec, st)
         out[prec] = u
     assert rel(out[native_lib.PREC_MIXED], out[native_lib.PREC_FP64]) < 1e-9
+
+
+def test_rve_batch_mixed_fp32_increment(native_lib, oracle):
+    """Mixed batch with the solution accumulated as an FP32 increment between
+    FP64 residual replacements (OGB_OPT_MIXED_X64 0): every pair converges on
+    its FP64 residual and agrees with the oracle to 1e-6."""
+    from oofem_gb300 import meshgen as mg
+    c = native_lib.Context(0)
+    c.set_option(native_lib.OPT_MIXED_X64, 0)
+    meshes = mg.rve_batch(4, seed=8, side_min=6, side_max=30)
+    big, ns = mg.concat_meshes(meshes)
+    model = native_lib.GpuModel(c, big)
+    model.set_instances(ns)
+    A = native_lib.GpuCsrMtrx(c)
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
+    u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-10, precision=native_lib.PREC_MIXED)
+    assert (st == 0).all() and (ach <= 1e-10).all()
+    for i, m in enumerate(meshes):
+        sl = slice(ns[i], ns[i + 1])
+        for lc in range(3):
+            ref = _oracle_case(oracle, m, mg.rve_bc_values(m, lc), np.zeros_like(m.bc_value), 1e-13)
+            assert rel(u[lc, sl], ref["u"]) < 1e-6, (i, lc)
