@@ -113,6 +113,7 @@ ARGS = None
 
 def apply_options(ctx):
     """Library options given on the command line (defaults: the library's)."""
+    from oofem_gb300 import native
     if ARGS is not None and ARGS.mixed_x64 >= 0:
         ctx.set_option(native.OPT_MIXED_X64, ARGS.mixed_x64)
 
@@ -669,8 +670,8 @@ def main():
     ap.add_argument("--spmv-variant", type=int, default=0,
                     help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
     ap.add_argument("--mixed-x64", type=int, default=-1, choices=(-1, 0, 1),
-                    help="mixed solves: 1 accumulate the solution in FP64 every iteration, 0 as an FP32 increment "
-                         "folded at each FP64 residual (OGB_OPT_MIXED_X64; -1 = library default)")
+                    help="single mixed solves: 1 accumulate the solution in FP64 every iteration, 0 as an FP32 "
+                         "increment folded at each FP64 residual (OGB_OPT_MIXED_X64; -1 = library default)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()

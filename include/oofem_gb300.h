@@ -93,7 +93,8 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 /*   OGB_OPT_MIXED_P32 (0/1): mixed solves keep p and q = K p in FP32 only. */
 #define OGB_OPT_MIXED_P32 5
 /*   OGB_OPT_MIXED_X64 (0/1): with FP32 vectors, accumulate the solution in FP64
- *   directly (default 1; 0 accumulates an FP32 increment between replacements). */
+ *   directly (default 1; 0 accumulates an FP32 increment between replacements).
+ *   Single-matrix solves only: batched solves always accumulate in FP64. */
 #define OGB_OPT_MIXED_X64 6
 /*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
  *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 = values and columns

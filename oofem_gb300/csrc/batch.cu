@@ -45,7 +45,6 @@ constexpr int UNIT = RPT * NTHREADS;         // scalar rows per vector block (10
 constexpr int SPMV_SLICES = NTHREADS / 32;   // slices (of 32 node rows) per SpMV block
 constexpr int MAXNR = 4;
 constexpr int BBATCH = 16;                   // iterations per captured graph
-constexpr int REPLACE_EVERY = 64;            // mixed precision: FP64 residual replacement period
 
 // Publish the block sums v (valid in thread 0) for block `unit`; true in every
 // thread of the block that completed its instance (count reaches its units).
@@ -82,7 +81,8 @@ __device__ __forceinline__ void inst_sums(const double *part, int64_t u0, int64_
 
 // Instance skip test (the same for every block of the instance within one
 // launch). mode 1: no pair of the instance is running (all converged, failed or
-// waiting for a residual replacement); mode 2: every pair is finished.
+// waiting for a residual replacement); mode 2: every pair is finished; mode 3:
+// no pair waits for a residual replacement.
 template <int NR>
 __device__ __forceinline__ bool inst_skip(const BatchScal *sc, int inst, int mode)
 {
@@ -90,7 +90,8 @@ __device__ __forceinline__ bool inst_skip(const BatchScal *sc, int inst, int mod
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
         const BatchScal &q = sc[inst * NR + c];
-        all = all && (q.done != 0 || (mode == 1 && q.pause != 0));
+        if (mode == 3) all = all && !(q.done == 0 && q.pause != 0);
+        else all = all && (q.done != 0 || (mode == 1 && q.pause != 0));
     }
     return all;
 }
@@ -404,14 +405,12 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
 }
 
 // ---- mixed precision: FP32 matrix (difference form) and FP32 r, z, p, q per
-// pair, FP64 solution x. Every REPLACE_EVERY iterations, and whenever no pair is
-// running, the true residual b - K64 x is formed in FP64 for every unfinished
-// pair; convergence is decided on it only. A pair whose recursive residual
-// reaches half the tolerance (or the iteration limit) pauses until then; a
-// paused pair that is not converged restarts its search direction from the
-// replaced residual, a running pair keeps it.
-
-// Residual replacement (init: the first one, which also sets ||b|| and p = z).
+// pair, FP64 solution x. A pair whose recursive residual has dropped by the drop
+// factor since its last replacement, or reached half the tolerance, or the
+// iteration limit, pauses in the update; in the same iteration its true residual
+// b - K64 x is formed in FP64 and replaces r, z and the CG scalars (reliable
+// update), convergence being decided on it only, and p = z + beta p continues
+// the recurrence. Running pairs are not touched by a replacement.
 // FP64 residual replacement (reliable update) of the pairs that paused -- their
 // recursive FP32 residual dropped by the drop factor since their last
 // replacement, or reached half the tolerance, or the FP32 recurrences ended --
@@ -430,7 +429,7 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
                                                        int init)
 {
     const int inst = unit_inst[blockIdx.x];
-    if (inst_skip<NR>(sc, inst, 2)) return;
+    if (inst_skip<NR>(sc, inst, init ? 2 : 3)) return;
     bool live[NR];
     double v[3 * NR];
 #pragma unroll
@@ -505,12 +504,11 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
     }
 }
 
-// x64 += alpha p (X = double), or the FP32 increment since the last residual
-// replacement d += alpha p (X = float, folded into x64 by k_bfold), r -= alpha q,
-// z = D^-1 r for running pairs; per pair ||r||^2 and r.z (FP32 per thread and
-// warp, FP64 above), the pause test and beta.
-template <int NR, class X>
-__global__ void __launch_bounds__(NTHREADS) k_bupdate32(X *__restrict__ x, float *__restrict__ r,
+// x64 += alpha p, r -= alpha q, z = D^-1 r for running pairs (FP32 but x);
+// per pair ||r||^2 and r.z (FP32 per thread and warp, FP64 above), the pause
+// test and beta.
+template <int NR>
+__global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, float *__restrict__ r,
                                                         float *__restrict__ z, const float *__restrict__ p,
                                                         const float *__restrict__ q, const float *__restrict__ dinv,
                                                         double *part, unsigned int *cnt, BatchScal *sc,
@@ -540,8 +538,7 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(X *__restrict__ x, float
             if (!run[c]) continue;
             const int64_t k = row * NR + c;
             const float pp = p[k];
-            if constexpr (sizeof(X) == 8) x[k] = fma(alpha[c], (double)pp, x[k]);
-            else x[k] = fmaf((float)alpha[c], pp, x[k]);
+            x[k] = fma(alpha[c], (double)pp, x[k]);
             const float rr = fmaf(-(float)alpha[c], q[k], r[k]);
             const float zz = rr * di;
             r[k] = rr;
@@ -635,21 +632,12 @@ __global__ void __launch_bounds__(NTHREADS) k_bzero_diverged(double *__restrict_
     }
 }
 
-// x64 += d, d = 0 (the FP32 increments of the finished cycle).
-__global__ void k_bfold(int64_t n, double *__restrict__ x, float *__restrict__ d)
-{
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] += (double)d[i];
-        d[i] = 0.f;
-    }
-}
-
 struct BatchWork {
     DBuf<int> vinst, sinst, zero;
     DBuf<int64_t> vptr, sptr;
     DBuf<BatchScal> sc;
     DBuf<double> part, r, z, p, q, dinv, q64;
-    DBuf<float> r32, z32, p32, q32, dinv32, d32;
+    DBuf<float> r32, z32, p32, q32, dinv32;
     DBuf<unsigned int> cnt;
 };
 
@@ -717,10 +705,6 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         OGB_CHECK(w.q32.alloc(nv));
         OGB_CHECK(w.dinv32.alloc(nrows));
         OGB_CHECK(w.q64.alloc(nv));
-        if (!ctx->mixed_x64) {
-            OGB_CHECK(w.d32.alloc(nv));
-            OGB_CUDA(cudaMemsetAsync(w.d32.p, 0, nv * sizeof(float), st));
-        }
     } else {
         OGB_CHECK(w.r.alloc(nv));
         OGB_CHECK(w.z.alloc(nv));
@@ -738,25 +722,16 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
     const int nr = S.nslices * 32;
     const unsigned gd = (unsigned)ceil_div(nr, NTHREADS);
     // FP64 K x for every unfinished pair (the initial residual; the replacements)
-    auto residual_spmv = [&](double *q64) {
+    // skip 2: every unfinished pair (FP64 path, init); skip 3: instances with a paused pair
+    auto residual_spmv = [&](double *q64, int skip) {
         k_bspmv<ND, NR, false, double, double, false><<<nsu, NTHREADS, 0, st>>>(
             S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v64.p, x, q64, nullptr, nullptr, w.sc.p, w.sinst.p,
-            w.sptr.p, 2);
+            w.sptr.p, skip);
     };
     std::function<void()> iteration;
-    // mixed: the solution accumulates in FP64 directly, or as an FP32 increment
-    // folded into it before every FP64 residual
-    const bool x64 = ctx->mixed_x64;
-    auto fold = [&]() -> int {
-        if (!mixed || x64) return OGB_OK;
-        k_bfold<<<NUM_SMS * 8, NTHREADS, 0, st>>>(nv, x, w.d32.p);
-        count_launch(ctx);
-        OGB_CUDA(cudaGetLastError());
-        return OGB_OK;
-    };
     if (mixed) {
         k_bdiag<ND, float><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv32.p, w.zero.p);
-        residual_spmv(w.q64.p);
+        residual_spmv(w.q64.p, 2);
         // p starts at zero: the init pass's p = z + 0 p is z
         OGB_CUDA(cudaMemsetAsync(w.p32.p, 0, nv * sizeof(float), st));
         k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p, w.sc.p,
@@ -764,7 +739,12 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
         const bool diff = ctx->mixed_diff;
         const double drop2 = ctx->mixed_drop * ctx->mixed_drop;
-        iteration = [&, diff, x64, drop2]() {
+        // one iteration: q = K p (FP32), the updates (pairs whose recursive residual
+        // dropped by the drop factor pause), p = z + beta p for the running pairs,
+        // then the FP64 replacement of the paused pairs -- residual, r, z, beta and
+        // their p = z + beta p -- inside the same captured graph, so a paused pair
+        // resumes at the next iteration
+        iteration = [&, diff, drop2]() {
             if (diff)
                 k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(
                     S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
@@ -773,19 +753,17 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
                 k_bspmv<ND, NR, true, float, float, false><<<nsu, NTHREADS, 0, st>>>(
                     S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
                     w.sinst.p, w.sptr.p, 1);
-            if (x64)
-                k_bupdate32<NR, double><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p,
-                                                                  w.part.p, w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p,
-                                                                  rtol, maxit, drop2);
-            else
-                k_bupdate32<NR, float><<<nvu, NTHREADS, 0, st>>>(w.d32.p, w.r32.p, w.z32.p, w.p32.p, w.q32.p,
-                                                                 w.dinv32.p, w.part.p, w.cnt.p, w.sc.p, w.vinst.p,
-                                                                 w.vptr.p, rtol, maxit, drop2);
+            k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
+                                                      w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, drop2);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);
+            residual_spmv(w.q64.p, 3);
+            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
+                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
+            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
         };
     } else {
         k_bdiag<ND, double><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
-        residual_spmv(w.q.p);
+        residual_spmv(w.q.p, 2);
         k_binit<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q.p, w.dinv.p, w.r.p, w.z.p, w.p.p, w.part.p, w.cnt.p, w.sc.p,
                                               w.vinst.p, w.vptr.p, rtol);
         iteration = [&]() {
@@ -804,7 +782,7 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
     int zero = 0;
     OGB_CUDA(cudaMemcpyAsync(&zero, w.zero.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     res.resize(npair);
-    int since = 0;   // iterations since the last residual replacement
+    const int per_it = mixed ? 6 : 3;   // launches per iteration
     for (int it = 0;;) {
         OGB_CUDA(cudaMemcpyAsync(res.data(), w.sc.p, npair * sizeof(BatchScal), cudaMemcpyDeviceToHost, st));
         OGB_CUDA(cudaStreamSynchronize(st));
@@ -812,36 +790,18 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             for (auto &s : res) s.done = 3;
             break;
         }
-        bool all = true, running = false, paused = false;
-        for (auto &s : res) {
-            all = all && s.done;
-            running = running || (s.done == 0 && s.pause == 0);
-            paused = paused || (s.done == 0 && s.pause != 0);
-        }
-        if (all || it > maxit + 2 * REPLACE_EVERY) break;
-        // replace when nothing runs, or when paused pairs have waited REPLACE_EVERY iterations
-        if (mixed && (!running || (paused && since >= REPLACE_EVERY))) {
-            OGB_CHECK(fold());
-            residual_spmv(w.q64.p);
-            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
-                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
-            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
-            count_launch(ctx, 3);
-            OGB_CUDA(cudaGetLastError());
-            since = 0;
-            continue;
-        }
+        bool all = true;
+        for (auto &s : res) all = all && s.done;
+        if (all || it > maxit + BBATCH) break;
         if (graph.e) {
             OGB_CUDA(cudaGraphLaunch(graph.e, st));
         } else {
             for (int k = 0; k < BBATCH; ++k) iteration();
         }
-        count_launch(ctx, 3 * BBATCH);
+        count_launch(ctx, per_it * BBATCH);
         OGB_CUDA(cudaGetLastError());
         it += BBATCH;
-        since += BBATCH;
     }
-    OGB_CHECK(fold());   // an exit on the iteration bound leaves the last increments unfolded
     if (mixed) {
         // a pair whose FP32 iterates diverged restarts its FP64 pass from zero
         k_bzero_diverged<NR><<<nvu, NTHREADS, 0, st>>>(x, w.sc.p, w.vinst.p);

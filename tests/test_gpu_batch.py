@@ -218,21 +218,26 @@ def test_batch_mixed_below_fp32_reach_finishes_in_fp64(ctx, native_lib):
     assert rel(out[native_lib.PREC_MIXED], out[native_lib.PREC_FP64]) < 1e-9
 
 
-def test_rve_batch_mixed_fp32_increment(native_lib, oracle):
-    """Mixed batch with the solution accumulated as an FP32 increment between
-    FP64 residual replacements (OGB_OPT_MIXED_X64 0): every pair converges on
-    its FP64 residual and agrees with the oracle to 1e-6."""
+def test_rve_batch_mixed_small_rves_reliable(ctx, native_lib, oracle):
+    """Small RVEs (6..30 elements a side) in a mixed batch: every pair's FP64
+    replacements keep its CG recurrence consistent, so the iteration counts stay
+    near the FP64 batch's and the displacements agree with the oracle to 1e-6
+    (a batch that replaced running pairs' residuals under a stale direction
+    diverged here and ended on a drifted recursive residual)."""
     from oofem_gb300 import meshgen as mg
-    c = native_lib.Context(0)
-    c.set_option(native_lib.OPT_MIXED_X64, 0)
     meshes = mg.rve_batch(4, seed=8, side_min=6, side_max=30)
     big, ns = mg.concat_meshes(meshes)
-    model = native_lib.GpuModel(c, big)
-    model.set_instances(ns)
-    A = native_lib.GpuCsrMtrx(c)
     bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
-    u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-10, precision=native_lib.PREC_MIXED)
-    assert (st == 0).all() and (ach <= 1e-10).all()
+    out = {}
+    for prec in (native_lib.PREC_FP64, native_lib.PREC_MIXED):
+        model = native_lib.GpuModel(ctx, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(ctx)
+        u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-10, precision=prec)
+        assert (st == 0).all() and (ach <= 1e-10).all()
+        out[prec] = (u, its)
+    u, its = out[native_lib.PREC_MIXED]
+    assert (its <= 1.5 * out[native_lib.PREC_FP64][1] + 16).all(), (its, out[native_lib.PREC_FP64][1])
     for i, m in enumerate(meshes):
         sl = slice(ns[i], ns[i + 1])
         for lc in range(3):
