@@ -407,10 +407,11 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
 // ---- mixed precision: FP32 matrix (difference form) and FP32 r, z, p, q per
 // pair, FP64 solution x. A pair whose recursive residual has dropped by the drop
 // factor since its last replacement, or reached half the tolerance, or the
-// iteration limit, pauses in the update; in the same iteration its true residual
-// b - K64 x is formed in FP64 and replaces r, z and the CG scalars (reliable
-// update), convergence being decided on it only, and p = z + beta p continues
-// the recurrence. Running pairs are not touched by a replacement.
+// iteration limit, pauses in the update; after the current batch of captured
+// iterations its true residual b - K64 x is formed in FP64 and replaces r, z and
+// the CG scalars (reliable update), convergence being decided on it only, and
+// p = z + beta p continues the recurrence. Running pairs are not touched by a
+// replacement.
 // FP64 residual replacement (reliable update) of the pairs that paused -- their
 // recursive FP32 residual dropped by the drop factor since their last
 // replacement, or reached half the tolerance, or the FP32 recurrences ended --
@@ -740,10 +741,7 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         const bool diff = ctx->mixed_diff;
         const double drop2 = ctx->mixed_drop * ctx->mixed_drop;
         // one iteration: q = K p (FP32), the updates (pairs whose recursive residual
-        // dropped by the drop factor pause), p = z + beta p for the running pairs,
-        // then the FP64 replacement of the paused pairs -- residual, r, z, beta and
-        // their p = z + beta p -- inside the same captured graph, so a paused pair
-        // resumes at the next iteration
+        // dropped by the drop factor pause), p = z + beta p for the running pairs
         iteration = [&, diff, drop2]() {
             if (diff)
                 k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(
@@ -756,10 +754,6 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
                                                       w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, drop2);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);
-            residual_spmv(w.q64.p, 3);
-            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
-                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
-            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
         };
     } else {
         k_bdiag<ND, double><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
@@ -782,7 +776,6 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
     int zero = 0;
     OGB_CUDA(cudaMemcpyAsync(&zero, w.zero.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     res.resize(npair);
-    const int per_it = mixed ? 6 : 3;   // launches per iteration
     for (int it = 0;;) {
         OGB_CUDA(cudaMemcpyAsync(res.data(), w.sc.p, npair * sizeof(BatchScal), cudaMemcpyDeviceToHost, st));
         OGB_CUDA(cudaStreamSynchronize(st));
@@ -790,15 +783,30 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             for (auto &s : res) s.done = 3;
             break;
         }
-        bool all = true;
-        for (auto &s : res) all = all && s.done;
-        if (all || it > maxit + BBATCH) break;
+        bool all = true, paused = false;
+        for (auto &s : res) {
+            all = all && s.done;
+            paused = paused || (s.done == 0 && s.pause != 0);
+        }
+        if (all || it > maxit + 2 * BBATCH) break;
+        if (mixed && paused) {
+            // FP64 replacement of the pairs that paused during the last batch of
+            // iterations (instances without one skip every kernel): residual, r, z,
+            // beta, and their p = z + beta p
+            residual_spmv(w.q64.p, 3);
+            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
+                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
+            k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
+            count_launch(ctx, 3);
+            OGB_CUDA(cudaGetLastError());
+            continue;
+        }
         if (graph.e) {
             OGB_CUDA(cudaGraphLaunch(graph.e, st));
         } else {
             for (int k = 0; k < BBATCH; ++k) iteration();
         }
-        count_launch(ctx, per_it * BBATCH);
+        count_launch(ctx, 3 * BBATCH);
         OGB_CUDA(cudaGetLastError());
         it += BBATCH;
     }
