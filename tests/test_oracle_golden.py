@@ -78,8 +78,8 @@ def test_patch300_reference_deck(oracle):
 
 
 def test_pcg_matches_reference_iteration_count(oracle):
-    """cfg1 with IML Jacobi-CG at lstol 1e-12: the survey's reference run logged
-    'nite 111, achieved tol 9.19e-13' (imlsolver.C:131)."""
+    """The 20x4x4 cantilever with IML Jacobi-CG at lstol 1e-12: a run of the
+    reference executable logged 'nite 111, achieved tol 9.19e-13' (imlsolver.C:131)."""
     g = load_golden("hex_cantilever_20x4x4")
     r = oracle.linear_static(g, rtol=1e-12)
     assert abs(r["iters"] - 111) <= 1
