@@ -126,3 +126,84 @@ def test_time_functions_metastep_and_sets(tmp_path):
     p.write_text(DECK.replace("loadTimeFunction 2", "loadTimeFunction 5"))
     with pytest.raises(dk.DeckError, match="time function 5"):
         dk.read_deck(str(p))
+
+
+OLD_STYLE = """old.out
+old-style references: node bc / load fields, element mat / crossSect fields
+LinearStatic nsteps 1 nmodules 0
+domain 3d
+OutputManager tstep_all dofman_all element_all
+ndofman 5 nelem 2 ncrosssect 1 nmat 1 nbc 3 nic 0 nltf 1
+# a comment line inside the node block and a blank line
+
+node 1 coords 3 0.0 0.0 0.0 bc 3 1 1 1
+node 2 coords 3 1.0 0.0 0.0 bc 3 1 1 1
+node 3 coords 3 0.0 1.0 0.0 bc 3 1 1 1
+node 4 coords 3 0.0 0.0 1.0 bc 3 0 2 0 load 1 3
+node 5 coords 3 1.0 1.0 1.0
+LTRSpace 1 nodes 4 1 2 3 4 crossSect 1 mat 1
+ltrspace 2 nodes 4 2 3 4 5 mat 1 crossSect 1
+SimpleCS 1
+IsoLE 1 d 1.0 E 10.0 n 0.2 tAlpha 0.0
+BoundaryCondition 1 loadTimeFunction 1 prescribedvalue 0.0
+BoundaryCondition 2 loadTimeFunction 1 prescribedvalue 0.5
+NodalLoad 3 loadTimeFunction 1 Components 3 0.0 0.0 -1.0
+ConstantFunction 1 f(t) 2.0
+"""
+
+
+def test_old_style_references(tmp_path):
+    """Node-record `bc` / `load` references and element-record `mat` /
+    `crossSect` fields (records the bulk reader flags and the general parser
+    completes), comment and blank lines inside the node block."""
+    p = tmp_path / "old.in"
+    p.write_text(OLD_STYLE)
+    d = dk.read_deck(str(p))
+    m = d.mesh
+    assert m.elem_type == mg.ELEM_LTRSPACE and m.nnodes == 5 and m.nelem == 2
+    np.testing.assert_array_equal(m.bc_mask[:3], 1)
+    np.testing.assert_array_equal(m.bc_mask[3], [0, 1, 0])
+    assert m.bc_value[3, 1] == 0.5 and d.bc_value_at(0.0)[3, 1] == 1.0      # f(t) = 2
+    np.testing.assert_array_equal(d.nodal_load_at(1.0)[3], [0.0, 0.0, -2.0])
+    np.testing.assert_array_equal(m.conn, [[0, 1, 2, 3], [1, 2, 3, 4]])
+    assert m.materials[m.elem_mat[1]].E == 10.0
+
+
+def _parse_block(text, tmp_path, count, keyword, field, maxvals):
+    import ctypes as C
+    from oofem_gb300 import native
+    lib = native.load()
+    p = tmp_path / "blk.in"
+    p.write_bytes(text.encode())
+    ids = np.zeros(max(count, 1), np.int64)
+    vals = np.zeros((max(count, 1), maxvals))
+    nv = np.zeros(max(count, 1), np.int32)
+    other = np.zeros(max(count, 1), np.uint8)
+    nxt, lines = C.c_int64(), C.c_int64()
+    code = lib.ogb_deck_parse_block(str(p).encode(), 0, count, keyword.encode(), field.encode(), maxvals,
+                                    ids.ctypes.data, vals.ctypes.data, nv.ctypes.data, other.ctypes.data,
+                                    C.byref(nxt), C.byref(lines))
+    return code, ids, vals, nv, other, nxt.value, lines.value, lib
+
+
+def test_bulk_block_reader(tmp_path):
+    """ogb_deck_parse_block on its own: comments and blank lines skipped, values,
+    counts and the further-fields flag per record, the offset after the block,
+    case-insensitive keyword and field; the errors name the record."""
+    text = "# c\n\nNODE 7 COORDS 2 1.5 -2e-3\nnode 8 bc 2 1 0 coords 3 1 2 3\nnext record\n"
+    code, ids, vals, nv, other, nxt, lines, lib = _parse_block(text, tmp_path, 2, "node", "coords", 3)
+    assert code == 0
+    assert ids.tolist() == [7, 8] and nv.tolist() == [2, 3] and other.tolist() == [0, 1]
+    np.testing.assert_array_equal(vals[0, :2], [1.5, -2e-3])
+    np.testing.assert_array_equal(vals[1], [1.0, 2.0, 3.0])
+    assert text.encode()[nxt:].startswith(b"next record") and lines == 4
+    for bad, msg in [("elem 1 coords 1 0\n", "expected a node record"),
+                     ("node 1 nodes 1 0\n", "field coords missing"),
+                     ("node 1 coords 4 1 2 3 4\n", "bad coords count"),
+                     ("node 1 coords 3 1 2\nnode 2 coords 3 1 2 3\n", "bad coords value"),
+                     ("node x coords 1 0\n", "record number missing"),
+                     ("node 1 coords 1 0\n", "deck ends inside a block")]:
+        count = 2 if "deck ends" in msg or "bad coords value" in msg else 1
+        code, *_, lib = _parse_block(bad, tmp_path, count, "node", "coords", 3)
+        assert code == -1, bad
+        assert msg in lib.ogb_last_error().decode(), (bad, lib.ogb_last_error())
