@@ -3,7 +3,8 @@
     python -m oofem_gb300.spmv_sweep [--sizes 100x20x20,200x40x40,290x58x58]
 
 For each mesh and precision it runs one LinearStatic solve to 1e-8 per form
-(OGB_OPT_SPMV_VARIANT 1..6, and 0 = the library's own choice) after a warm-up
+(OGB_OPT_SPMV_VARIANT 1..6, 0 = the library's own choice of the full-copy form,
+and 8 = the half-stored FP32 operator of mixed solves) after a warm-up
 solve, with kernel timing on, and prints one JSON line per run: the step time,
 the PCG iterations and the mean device time and bandwidth of the sampled SpMV
 launches. This is how the split rule and the autotuner's candidate forms in
@@ -18,7 +19,7 @@ from . import meshgen as mg
 from . import native
 
 FORMS = {1: "plain loop", 2: "prefetch 1", 3: "prefetch 4", 4: "TMA-staged", 5: "2 warps per slice",
-         6: "4 warps per slice", 0: "library choice"}
+         6: "4 warps per slice", 0: "library choice", 8: "half-stored (mixed only)"}
 
 
 def sweep(sizes, device=0):
@@ -29,8 +30,12 @@ def sweep(sizes, device=0):
         A = native.GpuCsrMtrx(ctx)
         model.build_matrix(A)
         for prec in (native.PREC_MIXED, native.PREC_FP64):
-            for v in (1, 2, 3, 4, 5, 6, 0):
-                ctx.set_option(native.OPT_SPMV_VARIANT, v)
+            for v in (1, 2, 3, 4, 5, 6, 0, 8):
+                if v == 8 and prec != native.PREC_MIXED:
+                    continue
+                # 8: the half-stored FP32 operator (OGB_OPT_SPMV_HALF 2); the others the full copy
+                ctx.set_option(native.OPT_SPMV_VARIANT, 0 if v == 8 else v)
+                ctx.set_option(native.OPT_SPMV_HALF, 2 if v == 8 else 0)
                 model.linear_static(A, rtol=1e-8, maxit=200000, precision=prec)
                 ctx.profile(True)
                 ctx.profile_read()
