@@ -202,12 +202,13 @@ def main():
                                                  maxiter=np.int32(maxiter),
                                                  initial_guess=np.int32(initial_guess)))
 
-    def static_structural(name, mesh, nsteps, deltat=1.0, rtolf=1e-8, maxiter=400, manrmsteps=None):
+    def static_structural(name, mesh, nsteps, deltat=1.0, rtolf=1e-8, maxiter=400, manrmsteps=None,
+                          ramp_time=None):
         # StaticStructural with the reference's defaults: nrsolver, IG_Tangent,
         # modified Newton unless manrmsteps is given
         analysis = (f"StaticStructural nsteps {nsteps} deltat {deltat!r} rtolf {rtolf!r} maxiter {maxiter}"
                     + (f" manrmsteps {manrmsteps}" if manrmsteps is not None else ""))
-        tend = nsteps * deltat
+        tend = nsteps * deltat if ramp_time is None else ramp_time
         ramp = f"PiecewiseLinFunction 2 nPoints 2 t 2 0.0 {float(tend)!r} f(t) 2 0.0 1.0"
         run_case(name, mesh, args.work, analysis=analysis, dumpK=False, bc_ltf=2, load_ltf=2,
                  extra_funcs=(ramp,), extra=dict(rtolf=np.float64(rtolf), ramp_time=np.float64(tend),
@@ -271,6 +272,10 @@ def main():
                                                           material=mg.Material(mg.MAT_MISES, 210e9, 0.3,
                                                                                sig0=250e6, H=2e9),
                                                           end_disp=3 * ey * 0.25), 8, manrmsteps=2),
+        "ss_idm1_tet_3": lambda: static_structural(
+            "ss_idm1_tet_3", mg.tet_cube(3, jitter=0.15, seed=6,
+                                         material=mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=1000.0),
+                                         end_disp=3e-4), 5, rtolf=1e-6, maxiter=400, manrmsteps=1, ramp_time=6.0),
         "idm1_tet_3": lambda: nonlinear(
             "idm1_tet_3", mg.tet_cube(3, jitter=0.15, seed=5,
                                       material=mg.Material(mg.MAT_IDM1, 30e9, 0.2, e0=1e-4, gf=1000.0),

@@ -59,6 +59,11 @@ def test_fixture_decks():
     np.testing.assert_array_equal(d.mesh.coords, g["coords"])
     # PiecewiseLinFunction 0 -> 1 over t in [0, 8]
     np.testing.assert_allclose(d.bc_value_at(2.0), g["bc_value"] * 0.25)
+    d = dk.read_deck(os.path.join(GOLDEN, "ss_idm1_tet_3.in"))
+    g = np.load(os.path.join(GOLDEN, "ss_idm1_tet_3.npz"))
+    assert d.mesh.elem_type == mg.ELEM_LTRSPACE and d.analysis.int("manrmsteps") == 1
+    np.testing.assert_array_equal(d.mesh.conn, g["conn"])
+    assert d.mesh.materials[0].kind == mg.MAT_IDM1 and d.mesh.materials[0].gf == 1000.0
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SM), reason="reference tree not present")

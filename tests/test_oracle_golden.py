@@ -155,3 +155,22 @@ def test_iml_cg_preconditioners(case, oracle):
     assert abs(r["iters"] - int(g["cg_nite"][0])) <= 1, (r["iters"], int(g["cg_nite"][0]))
     assert rel(r["u"], g["s1_u"]) < 1e-8
     assert rel(r["reac"], g["s1_reac"]) < 1e-8
+
+
+def test_static_structural_idm1(oracle):
+    """StaticStructural (IG_Tangent, full Newton) with IsotropicDamageMaterial1
+    through the softening branch (damage up to 0.93) against the reference run:
+    same Newton iterations per step, displacements, reactions, stresses, kappa
+    and damage."""
+    g = load_golden("ss_idm1_tet_3")
+    ns = int(g["nsteps"])
+    res = oracle.static_structural(g, ns, float(g["ramp_time"]), deltat=float(g["deltat"]),
+                                   rtolf=float(g["rtolf"]), maxiter=int(g["maxiter"]),
+                                   manrmsteps=int(g["manrmsteps"]))
+    for k, r in enumerate(res, 1):
+        assert r["nite"] == int(g[f"s{k}_nite"]), (k, r["nite"], int(g[f"s{k}_nite"]))
+        assert rel(r["u"], g[f"s{k}_u"]) < 1e-8
+        assert rel(r["reac"], g[f"s{k}_reac"]) < 1e-8
+        assert rel(r["stress"], g[f"s{k}_stress"]) < 1e-8
+        assert rel(r["state"][:, 0], g[f"s{k}_kappa"].ravel()) < 1e-8
+        assert rel(r["state"][:, 1], g[f"s{k}_omega"].ravel()) < 1e-8
