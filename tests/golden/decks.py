@@ -11,13 +11,18 @@ import numpy as np
 from oofem_gb300 import meshgen as mg
 
 
+def _f(v) -> str:
+    """Shortest round-trip text of a float (numpy scalars included)."""
+    return repr(float(v))
+
+
 def _mat_record(i: int, m: mg.Material) -> str:
     if m.kind == mg.MAT_ISOLE:
-        return f"IsoLE {i} d 1.0 E {m.E!r} n {m.nu!r} talpha 0.0"
+        return f"IsoLE {i} d 1.0 E {_f(m.E)} n {_f(m.nu)} talpha 0.0"
     if m.kind == mg.MAT_MISES:
-        return f"MisesMat {i} d 1.0 E {m.E!r} n {m.nu!r} sig0 {m.sig0!r} H {m.H!r} talpha 0.0"
+        return f"MisesMat {i} d 1.0 E {_f(m.E)} n {_f(m.nu)} sig0 {_f(m.sig0)} H {_f(m.H)} talpha 0.0"
     if m.kind == mg.MAT_IDM1:
-        return (f"idm1 {i} d 1.0 E {m.E!r} n {m.nu!r} talpha 0.0 e0 {m.e0!r} gf {m.gf!r} "
+        return (f"idm1 {i} d 1.0 E {_f(m.E)} n {_f(m.nu)} talpha 0.0 e0 {_f(m.e0)} gf {_f(m.gf)} "
                 f"equivstraintype 0 damlaw 0")
     raise ValueError(m.kind)
 
@@ -64,7 +69,7 @@ def write_deck(mesh: mg.Mesh, path: str, analysis: str, nsteps: int = 1,
         c = " ".join(str(int(v) + 1) for v in mesh.conn[e])
         lines.append(f"{name} {e + 1} nodes {mesh.nnpe} {c}")
     for i in range(ncs):
-        thick = f" thick {mesh.thickness!r}" if et == mg.ELEM_PLANESTRESS2D else ""
+        thick = f" thick {_f(mesh.thickness)}" if et == mg.ELEM_PLANESTRESS2D else ""
         lines.append(f"SimpleCS {i + 1}{thick} material {i + 1} set {i + 1}")
     for i, m in enumerate(mats):
         lines.append(_mat_record(i + 1, m))
