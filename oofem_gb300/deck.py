@@ -124,6 +124,30 @@ class Record:
         return _ranges(self._value(key))
 
 
+def _check_fields(r: Record, fields: Dict[str, str], allowed_values: Dict[str, tuple] = None):
+    """Every field of the record must be one of `fields` (name -> "array" for a
+    counted list, "scalar" for one value); a field listed in allowed_values must
+    hold one of those values. Anything else is a feature outside this reader."""
+    allowed_values = allowed_values or {}
+    i = 2 if r.number is not None else 1
+    while i < len(r.tok):
+        key = r._low[i]
+        kind = fields.get(key)
+        if kind is None:
+            raise DeckError(f"line {r.lineno}: field '{r.tok[i]}' of {r.tok[0]} is not supported")
+        if kind == "array":
+            try:
+                n = int(r.tok[i + 1])
+            except (IndexError, ValueError):
+                raise DeckError(f"line {r.lineno}: bad count of '{r.tok[i]}'") from None
+            i += 2 + n
+        else:
+            if key in allowed_values and (i + 1 >= len(r.tok) or r.tok[i + 1] not in allowed_values[key]):
+                raise DeckError(f"line {r.lineno}: {r.tok[i]} {r.tok[i + 1] if i + 1 < len(r.tok) else ''} "
+                                f"of {r.tok[0]} is not supported")
+            i += 2
+
+
 @dataclasses.dataclass
 class Deck:
     output: str
@@ -381,6 +405,12 @@ def _read(rd: "_Reader", path: str) -> Deck:
         if r.has("set") and set_elems.get(r.int("set")):
             elem_cs[elem_rows(set_elems[r.int("set")])] = r.number
     elem_mid = np.array([cs_mat.get(int(c), 0) for c in range(int(elem_cs.max()) + 1)], np.int64)[elem_cs]
+    nip_default = {mg.ELEM_LSPACE: ("8",), mg.ELEM_PLANESTRESS2D: ("4",), mg.ELEM_LTRSPACE: ("1",)}[et]
+    for r in elem_full.values():   # geometric nonlinearity, other integration rules, loads on elements: refused
+        _check_fields(r, {"nodes": "array", "crosssect": "scalar", "mat": "scalar", "nlgeo": "scalar",
+                          "nip": "scalar"}, {"nlgeo": ("0",), "nip": nip_default})
+    for r in node_full.values():
+        _check_fields(r, {"coords": "array", "bc": "array", "load": "array"})
     for k, r in elem_full.items():   # old-style crossSect / mat fields on the element record
         cs = r.int("crosssect", 0) or int(elem_cs[k])
         elem_mid[k] = r.int("mat", 0) or cs_mat.get(cs, 0)

@@ -80,8 +80,9 @@ def test_reference_patch_decks_with_oracle(name, oracle):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SM), reason="reference tree not present")
-@pytest.mark.parametrize("name,msg", [("patch103", "StructTemperatureLoad"), ("patch105", "ConstantEdgeLoad"),
-                                      ("Mises01", "truss1d"), ("idm11", "equivstraintype")])
+@pytest.mark.parametrize("name,msg", [("patch103", "StructTemperatureLoad"), ("patch105", "boundaryLoads"),
+                                      ("Mises01", "truss1d"), ("idm11", "equivstraintype"),
+                                      ("brick_nlgeo_1", "nlgeo 1")])
 def test_reference_decks_outside_the_path_are_refused(name, msg):
     with pytest.raises(dk.DeckError, match=msg):
         dk.read_deck(os.path.join(REF_SM, name + ".in"))
