@@ -265,6 +265,11 @@ def _read(rd: "_Reader", path: str) -> Deck:
         _, ms_text = nxt("metastep record")
         rest = analysis.text.split(None, 1)
         analysis = Record(rest[0] + " " + ms_text + (" " + rest[1] if len(rest) > 1 else ""), analysis.lineno)
+    # analysis and solver keys whose semantics this runner does not implement
+    for key, ok in (("linesearch", ("0",)), ("rtold", None), ("rtolv", None), ("ddm", None), ("ddv", None),
+                    ("stiffmode", ("0",)), ("miniter", ("0",)), ("initialguess", ("0", "1"))):
+        if analysis.has(key) and (ok is None or analysis._value(key) not in ok):
+            raise DeckError(f"analysis key '{key} {analysis._value(key)}' is not supported")
     for _ in range(analysis.int("nmodules", 0)):
         nxt("export modules")
     dom = Record(*reversed(nxt("domain record")))
@@ -441,6 +446,9 @@ def _read(rd: "_Reader", path: str) -> Deck:
 
     for r in bcs:
         f = r.int("loadtimefunction")
+        for key in ("isimposedtimefunction", "reference", "loadtype", "csys", "lcs"):
+            if r.has(key):
+                raise DeckError(f"line {r.lineno}: field '{key}' of {r.tok[0]} is not supported")
         if r.keyword == "boundarycondition":
             if r.has("set"):
                 rows = node_rows(set_nodes.get(r.int("set"), []))

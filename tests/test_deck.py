@@ -81,7 +81,7 @@ def test_reference_patch_decks_with_oracle(name, oracle):
 
 @pytest.mark.skipif(not os.path.isdir(REF_SM), reason="reference tree not present")
 @pytest.mark.parametrize("name,msg", [("patch103", "StructTemperatureLoad"), ("patch105", "boundaryLoads"),
-                                      ("Mises01", "truss1d"), ("idm11", "equivstraintype"),
+                                      ("Mises01", "truss1d"), ("idm11", "rtolv"),
                                       ("brick_nlgeo_1", "nlgeo 1")])
 def test_reference_decks_outside_the_path_are_refused(name, msg):
     with pytest.raises(dk.DeckError, match=msg):
@@ -213,3 +213,14 @@ def test_bulk_block_reader(tmp_path):
         code, *_, lib = _parse_block(bad, tmp_path, count, "node", "coords", 3)
         assert code == -1, bad
         assert msg in lib.ogb_last_error().decode(), (bad, lib.ogb_last_error())
+
+
+@pytest.mark.parametrize("edit,msg", [("controlmode 1 manrmsteps 1", "linesearch 1"), ("nsteps 3 rtolf", "rtolv")])
+def test_analysis_keys_outside_the_runner_are_refused(edit, msg, tmp_path):
+    text = DECK.replace("nsteps 3 rtolf 1e-6 controlmode 1 manrmsteps 1",
+                        "nsteps 3 rtolf 1e-6 controlmode 1 manrmsteps 1 linesearch 1" if "linesearch" in msg
+                        else "nsteps 3 rtolv 1e-6 controlmode 1 manrmsteps 1")
+    p = tmp_path / "k.in"
+    p.write_text(text)
+    with pytest.raises(dk.DeckError, match=msg.split()[0]):
+        dk.read_deck(str(p))
