@@ -380,7 +380,13 @@ def _read(rd: "_Reader", path: str) -> Deck:
     # materials
     mat_index: Dict[int, int] = {}
     materials: List[mg.Material] = []
+    scalar = lambda *k: {name: "scalar" for name in k}
+    mat_fields = {"isole": scalar("d", "e", "n", "talpha"),
+                  "misesmat": scalar("d", "e", "n", "talpha", "sig0", "h", "htype", "omega_crit", "a", "yieldtol"),
+                  "idm1": scalar("d", "e", "n", "talpha", "e0", "gf", "equivstraintype", "damlaw")}
     for r in mats:
+        if r.keyword in mat_fields:   # any other parameter changes the model: refused
+            _check_fields(r, mat_fields[r.keyword])
         if r.keyword == "isole":
             # talpha acts only through temperature loads, which are not accepted
             m = mg.Material(mg.MAT_ISOLE, r.float("e"), r.float("n"))

@@ -224,3 +224,10 @@ def test_analysis_keys_outside_the_runner_are_refused(edit, msg, tmp_path):
     p.write_text(text)
     with pytest.raises(dk.DeckError, match=msg.split()[0]):
         dk.read_deck(str(p))
+
+
+def test_material_parameters_outside_the_model_are_refused(tmp_path):
+    p = tmp_path / "m.in"
+    p.write_text(DECK.replace("IsoLE 1 d 1.0 E 100.0 n 0.2 tAlpha 1e-5", "IsoLE 1 d 1.0 E 100.0 n 0.2 maxOmega 0.9"))
+    with pytest.raises(dk.DeckError, match="maxOmega"):
+        dk.read_deck(str(p))
