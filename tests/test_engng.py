@@ -72,3 +72,34 @@ def test_static_structural_prescribed_times():
     assert ss.give_end_of_time_of_interest() == 2.0
     with pytest.raises(ValueError):
         engng.StaticStructural(_Model(), None, initial_guess=5)
+
+
+class _StateModel(_Model):
+    def __init__(self):
+        super().__init__()
+        self.restored = None
+
+    def save_state(self):
+        return b"DEVICE-STATE"
+
+    def restore_state(self, blob):
+        self.restored = blob
+
+
+def test_context_round_trip_host_side():
+    """save_context prefixes the step number and time to the model's state blob;
+    restore_context checks the prefix and resumes after the saved step."""
+    m = _StateModel()
+    ss = engng.StaticStructural(m, None, nsteps=4, deltat=0.25)
+    ss.solve_yourself_at()
+    ss.solve_yourself_at()
+    blob = ss.save_context()
+    m2 = _StateModel()
+    ss2 = engng.StaticStructural(m2, None, nsteps=4, deltat=0.25)
+    ss2.restore_context(blob)
+    assert m2.restored == b"DEVICE-STATE" and ss2.step == 2 and ss2.time == 0.5
+    assert [r.time for r in ss2.solve_yourself()] == [0.75, 1.0]
+    with pytest.raises(ValueError):
+        ss2.restore_context(b"X" * len(blob))
+    with pytest.raises(ValueError):
+        engng.StaticStructural(_StateModel(), None, nsteps=1).restore_context(blob)   # step 2 > nsteps 1
