@@ -212,6 +212,34 @@ OGB_API int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr_dev, const int *c
                                   const double *b_dev, double *x_dev, double rtol, int maxit, void *stream,
                                   ogb_solve_info *info);
 
+/* ---- direct solver: replaces LDLTFactorization (lstype 0, src/core/ldltfact.C:50-63)
+ *      on a Skyline matrix (SparseMtrx::factorized skyline.C:429-491,
+ *      backSubstitutionWith skyline.C:248-290) ------------------------------- */
+/* Linear solver of every solve on this matrix, numbered as the reference's
+ * `lstype` (LinSystSolverType, src/core/linsystsolvertype.h:47-57):
+ * OGB_LS_DIRECT (0, ST_Direct) factors the matrix as L D L^T (no pivoting, the
+ * upper triangle K(i,j), i <= j, as Skyline::assemble stores it, skyline.C:189-223)
+ * once per matrix version and solves by substitution: ogb_pcg_solve*, the Newton
+ * and LinearStatic drivers then ignore rtol / maxit / precision and report 0
+ * iterations and the FP64 relative residual of the result. OGB_LS_IML (1) and
+ * OGB_LS_GPUPCG (9, the default) run the PCG. Batched solves
+ * (ogb_batch_*, multi-RHS on model matrices) always run the batched PCG. */
+#define OGB_LS_DIRECT 0
+#define OGB_LS_IML 1
+#define OGB_LS_GPUPCG 9
+OGB_API int ogb_mtrx_set_solver(ogb_mtrx *m, int lstype);
+/* SparseMtrx::factorized (skyline.C:429-491): factor the current values (the
+ * factor is kept until the next mutation). The factor is a dense band of
+ * neq x (bw+1) doubles, bw the half bandwidth of the pattern (OGB_E_LIMIT when
+ * it does not fit in device memory); OGB_E_ZERODIAG names a zero pivot. */
+OGB_API int ogb_ldlt_factorize(ogb_mtrx *m);
+/* Half bandwidth of the current factor (OGB_E_STATE before ogb_ldlt_factorize). */
+OGB_API int ogb_ldlt_bandwidth(ogb_mtrx *m, int *bandwidth);
+/* LDLTFactorization::solve (ldltfact.C:50-63): x = A^-1 b, factoring first when
+ * the values changed. Host vectors of neq doubles / device vectors (_dev). */
+OGB_API int ogb_ldlt_solve(ogb_mtrx *m, const double *b, double *x);
+OGB_API int ogb_ldlt_solve_dev(ogb_mtrx *m, const double *b_dev, double *x_dev);
+
 /* SparseLinearSystemNM::solve(A, B, X) (sparselinsystemnm.h:91, default column
  * loop sparselinsystemnm.C:47-69): nrhs right-hand sides at once. B and X are
  * column-major neq x nrhs (FloatMatrix storage); X holds the initial guesses and

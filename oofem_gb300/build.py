@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liboofem_gb300.so")
-SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu", "newton.cu", "batch.cu", "halfsell.cu", "deckparse.cu", "icprec.cu"]
+SOURCES = ["capi.cu", "scan.cu", "pattern.cu", "element.cu", "assembly.cu", "solver.cu", "newton.cu", "batch.cu", "halfsell.cu", "deckparse.cu", "icprec.cu", "direct.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]

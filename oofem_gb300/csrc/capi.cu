@@ -3,6 +3,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -23,6 +25,19 @@ void ctx_release(ogb_ctx *ctx)
 }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
+
+int num_sms()
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    const int slot = dev >= 0 && dev < 64 ? dev : 0;
+    int n = cache[slot].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+    cache[slot].store(n, std::memory_order_relaxed);
+    return n;
+}
 
 int fail(int code, const std::string &msg)
 {
@@ -256,11 +271,13 @@ int solve_padded(ogb_mtrx *m, double rtol, int maxit, int precision, ogb_solve_i
 {
     ogb_solve_info tmp{};
     ogb_solve_info *inf = info ? info : &tmp;
-    int r = precision == OGB_PREC_MIXED ? pcg_mixed(m, m->w_b.p, m->w_x.p, rtol, maxit, inf)
-                                        : pcg_fp64(m, m->w_b.p, m->w_x.p, rtol, maxit, inf);
+    int r = m->lstype == OGB_LS_DIRECT          ? ldl_solve(m, m->w_b.p, m->w_x.p, inf)
+            : precision == OGB_PREC_MIXED ? pcg_mixed(m, m->w_b.p, m->w_x.p, rtol, maxit, inf)
+                                          : pcg_fp64(m, m->w_b.p, m->w_x.p, rtol, maxit, inf);
     if (r != OGB_OK) return r;
     if (inf->status != OGB_OK) {
-        const char *why = inf->status == OGB_E_ZERODIAG ? "zero diagonal detected"
+        const char *why = m->lstype == OGB_LS_DIRECT    ? "direct solver: zero or non-finite pivot"
+                          : inf->status == OGB_E_ZERODIAG ? "zero diagonal detected"
                           : inf->status == OGB_E_BREAKDOWN ? "PCG breakdown (rho or p'q not positive/finite)"
                                                           : "PCG did not converge within maxit";
         set_error(why);
@@ -582,7 +599,7 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
     if (fp64_form) *fp64_form = sell ? m->sell.group[0] : 0;
     if (fp32_form) *fp32_form = sell ? (m->last_half ? 8 : m->sell.group[1]) : 0;
     if (warps_per_slice) *warps_per_slice = sell ? (m->sell.force_split ? m->sell.force_split
-                                                    : (m->sell.nslices < NUM_SMS * 16 ? 4 : 1)) : 0;
+                                                    : (m->sell.nslices < num_sms() * 16 ? 4 : 1)) : 0;
     return OGB_OK;
 }
 
@@ -638,7 +655,7 @@ int ogb_pcg_solve_multi_dev(ogb_mtrx *m, int nrhs, const double *B, double *X, d
     if (!m->has_structure) return fail(OGB_E_STATE, "no structure");
     OGB_CUDA(cudaSetDevice(m->ctx->device));
     if (nrhs == 0) return OGB_OK;
-    if (m->has_sell && m->sell.v32_version == m->version && m->precond == 1)
+    if (m->has_sell && m->sell.v32_version == m->version && m->precond == 1 && m->lstype != OGB_LS_DIRECT)
         return pcg_solve_multi(m, nrhs, B, X, rtol, maxit, precision, iterations, achieved, status);
     // no current node-block copy (location-array matrix, or values changed
     // through set_at): the reference's column loop (sparselinsystemnm.C:47-69)

@@ -33,7 +33,9 @@ int cuda_fail(cudaError_t e, const char *what);
 // to one system and block-level reductions stay deterministic.
 constexpr int CHUNK = 1024;
 constexpr int NTHREADS = 256;
-constexpr int NUM_SMS = 152;
+// Multiprocessor count of the current device (queried once per device; 152 on a
+// GB300). Grids of the vector and reduction kernels are multiples of it.
+int num_sms();
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
@@ -184,6 +186,20 @@ struct IcFactor {
     std::vector<int> flev, blev;   // level starts into frows / brows
 };
 
+// LDL^T factor of the direct solver (direct.cu): dense band of n x (bw+1)
+// doubles, column j holds L(j..j+bw, j) with d_j in its diagonal slot.
+struct LdlFactor {
+    int64_t version = -1;   // matrix version the factor belongs to
+    bool ok = false;
+    int n = 0, bw = 0;      // equations, half bandwidth
+    DBuf<double> band;
+    DBuf<int> d_int;        // [0] half bandwidth, [1] 1-based equation of a zero pivot
+    HBuf<int> h_int;
+    DBuf<double> y, part, out;   // residual check of a solve
+    DBuf<unsigned int> cnt;
+    HBuf<double> h_out;
+};
+
 // Instances of a batch start on multiples of INST_ALIGN node-space rows.
 constexpr int INST_ALIGN = 1024;
 
@@ -252,6 +268,8 @@ struct ogb_mtrx {
     bool last_half = false;                      // the last mixed solve used the half-stored FP32 copy
     int precond = 1;                             // IML preconditioner type: 0 none, 1 diagonal, 2 ILU, 4 incomplete Cholesky
     ogb::IcFactor ic;
+    int lstype = OGB_LS_GPUPCG;                  // linear solver: OGB_LS_DIRECT factors (direct.cu), else PCG
+    ogb::LdlFactor ldl;
 };
 
 struct ogb_model {
@@ -357,6 +375,11 @@ int pcg_fp64(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, og
 int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, ogb_solve_info *info);
 int extract_diag(ogb_mtrx *m);
 int pick_tpr(const ogb_mtrx *m);
+
+// direct.cu: LDL^T factor of m (cached per version) and x = A^-1 b on padded
+// equation-space device vectors (info: 0 iterations, FP64 relative residual).
+int ldl_factor(ogb_mtrx *m);
+int ldl_solve(ogb_mtrx *m, const double *b, double *x, ogb_solve_info *info);
 
 // newton.cu
 int nr_ensure(ogb_model *md);   // Newton work buffers; nr_X and nr_bcprev zeroed on first allocation

@@ -36,7 +36,10 @@ from .engng import ConstantFunction, PiecewiseLinFunction
 
 ELEMENT_TYPES = {"lspace": mg.ELEM_LSPACE, "planestress2d": mg.ELEM_PLANESTRESS2D, "ltrspace": mg.ELEM_LTRSPACE}
 NODES_PER_ELEMENT = {mg.ELEM_LSPACE: 8, mg.ELEM_PLANESTRESS2D: 4, mg.ELEM_LTRSPACE: 4}
-DIRECT_TOL = 1e-12   # PCG tolerance standing in for the reference's direct solver (lstype 0)
+# lstype values of the reference's direct solvers (linsystsolvertype.h:47-57: ST_Direct, ST_Spooles,
+# ST_DSS, ST_MKLPardiso, ST_SuperLU_MT, ST_PardisoProjectOrg): decks asking for one run the device
+# LDL^T factorization
+DIRECT_LSTYPES = (0, 2, 4, 6, 7, 8)
 
 
 class DeckError(ValueError):
@@ -524,7 +527,8 @@ def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optio
     LinearStatic: step k at time k (LinearStatic::giveNextStep, linearstatic.C:146-156), one PCG solve.
     Decks for an iterative solver (lstype 1 IML, 9 this library) keep its lstol / lsiter / lsprecond
     (IMLSolver defaults 1e-5 / 200 / none; lstype 9 defaults to the diagonal preconditioner); decks for
-    the default direct solver (lstype 0) get PCG to DIRECT_TOL. NonLinearStatic: step k
+    the default direct solver (lstype 0) or another direct one run the device LDL^T factorization
+    (LDLTFactorization on a Skyline matrix). NonLinearStatic: step k
     at time (k-1) * deltat (nlinearstatic.C:295-325). StaticStructural: oofem_gb300.engng.StaticStructural.
     ``precision`` / ``lstol`` override the linear solver's arithmetic and tolerance."""
     from . import engng, native
@@ -535,14 +539,22 @@ def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optio
     prec = native.PREC_FP64 if precision is None else precision
     nsteps = a.int("nsteps", 1)
     out: List[DeckStep] = []
-    # lstype 0 (the default, a direct Skyline LDL^T solve) has no device counterpart: such decks are
-    # solved by PCG to DIRECT_TOL; an iterative lstype keeps its lstol / lsiter / lsprecond
-    direct = a.int("lstype", 0) == 0
-    if not direct:
-        K.set_preconditioner(a.int("lsprecond", 0 if a.int("lstype", 0) == 1 else 1))
+    # lstype 0 (the default) and the other direct solvers factor the matrix; a caller asking for
+    # mixed precision or for a PCG tolerance runs such a deck by PCG instead (to `lstol`, else
+    # 1e-12); an iterative lstype keeps its lstol / lsiter / lsprecond
+    lstype = a.int("lstype", 0)
+    if lstype not in DIRECT_LSTYPES + (1, 9):
+        raise DeckError(f"lstype {lstype} is not a linear solver of the reference")
+    direct = lstype in DIRECT_LSTYPES and lstol is None and prec == native.PREC_FP64
+    if direct:
+        K.set_solver(native.LS_DIRECT)
+    elif lstype in DIRECT_LSTYPES and lstol is None:
+        lstol = 1e-12
+    elif lstype not in DIRECT_LSTYPES:
+        K.set_preconditioner(a.int("lsprecond", 0 if lstype == 1 else 1))
     if deck.analysis_type == "linearstatic":
-        tol = lstol if lstol is not None else (DIRECT_TOL if direct else a.float("lstol", 1e-5))
-        maxit = 1000000 if direct else a.int("lsiter", 200)
+        tol = lstol if lstol is not None else (0.0 if direct else a.float("lstol", 1e-5))
+        maxit = 1 if direct else (1000000 if lstype in DIRECT_LSTYPES else a.int("lsiter", 200))
         for k in range(1, nsteps + 1):
             t = float(k)
             u, reac, info = model.linear_static(K, deck.bc_value_at(t), deck.nodal_load_at(t), rtol=tol,
@@ -551,7 +563,7 @@ def run_deck(deck: Deck, ctx=None, precision: Optional[int] = None, lstol: Optio
                 raise native.OgbError(info.status, f"LinearStatic step {k}: linear solver did not converge")
             out.append(DeckStep(k, t, u, reac, info.iterations))
         return out
-    tol = lstol if lstol is not None else (DIRECT_TOL if direct else a.float("lstol", 1e-5))
+    tol = lstol if lstol is not None else (0.0 if direct else a.float("lstol", 1e-5))
     if deck.analysis_type == "nonlinearstatic":
         if a.int("controlmode", 1) != 1:
             raise DeckError("NonLinearStatic supports controlmode 1 (direct displacement / load control)")

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import struct
 from typing import Optional
 
 import numpy as np
@@ -34,6 +35,10 @@ OPT_MIXED_P32 = 5
 OPT_MIXED_X64 = 6
 OPT_SPMV_VARIANT = 7
 OPT_SPMV_HALF = 8
+# linear solver types (the reference's lstype numbers)
+LS_DIRECT = 0
+LS_IML = 1
+LS_GPUPCG = 9
 # solver outcomes returned (not raised), like SparseLinearSystemNM::solve's ConvergedReason
 SOLVER_STATUS = (0, -5, -6, -7)
 
@@ -97,6 +102,11 @@ SIGNATURES = {
     "ogb_model_set_initial_guess": (_i, [_vp, _i]),
     "ogb_model_set_nr_mode": (_i, [_vp, _i]),
     "ogb_mtrx_set_preconditioner": (_i, [_vp, _i]),
+    "ogb_mtrx_set_solver": (_i, [_vp, _i]),
+    "ogb_ldlt_factorize": (_i, [_vp]),
+    "ogb_ldlt_bandwidth": (_i, [_vp, _pi]),
+    "ogb_ldlt_solve": (_i, [_vp, _vp, _vp]),
+    "ogb_ldlt_solve_dev": (_i, [_vp, _vp, _vp]),
     "ogb_deck_parse_block": (_i, [C.c_char_p, C.c_int64, C.c_int64, C.c_char_p, C.c_char_p, _i, _vp, _vp, _vp, _vp,
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ogb_model_state_bytes": (_i, [_vp, C.POINTER(C.c_size_t)]),
@@ -252,6 +262,29 @@ class GpuCsrMtrx:
         """IML lsprecond: 0 none, 1 diagonal (default), 4 incomplete Cholesky (FP64)."""
         _check(self.lib.ogb_mtrx_set_preconditioner(self.h, int(lsprecond)))
 
+    def set_solver(self, lstype: int):
+        """Linear solver of every solve on this matrix, as the reference's lstype:
+        0 direct LDL^T (LDLTFactorization on a Skyline matrix), 1 / 9 PCG."""
+        _check(self.lib.ogb_mtrx_set_solver(self.h, int(lstype)))
+
+    def factorized(self):
+        """SparseMtrx::factorized: factor the current values (L D L^T)."""
+        _check(self.lib.ogb_ldlt_factorize(self.h))
+        return self
+
+    @property
+    def bandwidth(self) -> int:
+        v = C.c_int()
+        _check(self.lib.ogb_ldlt_bandwidth(self.h, C.byref(v)))
+        return v.value
+
+    def ldlt_solve(self, b: np.ndarray) -> np.ndarray:
+        """LDLTFactorization::solve: x = A^-1 b (factors first when the values changed)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.neq)
+        _check(self.lib.ogb_ldlt_solve(self.h, _ptr(b), _ptr(x)))
+        return x
+
     def spmv_forms(self):
         """(FP64 form, FP32 form, warps per slice) of the node-block SpMV."""
         a, b, c = C.c_int(), C.c_int(), C.c_int()
@@ -343,6 +376,21 @@ class GpuPcgSolver:
         code = A.lib.ogb_pcg_solve_multi(A.h, nrhs, _ptr(B), _ptr(X), self.tol, self.maxit, self.precision,
                                          _ptr(its), _ptr(ach), _ptr(st))
         self.last_multi = (its, ach, st)
+        if code not in SOLVER_STATUS:
+            _check(code)
+        return code
+
+
+class GpuLdltSolver:
+    """LDLTFactorization (src/core/ldltfact.C:50-63), the reference's default
+    solver (lstype 0): factor the matrix once per version as L D L^T on the
+    device, then solve by substitution. Returns 0 (CR_CONVERGED) or the status
+    of a zero pivot."""
+
+    def solve(self, A: GpuCsrMtrx, b: np.ndarray, x: np.ndarray) -> int:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        code = A.lib.ogb_ldlt_solve(A.h, _ptr(b), _ptr(x))
         if code not in SOLVER_STATUS:
             _check(code)
         return code
@@ -477,6 +525,33 @@ class GpuModel:
     def restore_state(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(self.lib.ogb_model_restore_state(self.h, buf, len(blob)))
+
+    # layout of the checkpoint header (StateHeader in csrc/capi.cu): magic, format, etype,
+    # nnodes, nelem, ngp, ndofpn, neq, nstate (int32), state_len, nrb_len (int64)
+    _STATE_HEADER = struct.Struct("<8s8i2q")
+
+    def committed_state(self) -> np.ndarray:
+        """Committed Gauss-point state (nelem, ngp, nstate) as it stands in the
+        checkpoint: MisesMat [0..5] plastic strain, [6] kappa; IDM1 [0] kappa,
+        [1] damage, [2] crack band length Le (MaterialStatus::saveContext per point)."""
+        blob = self.save_state()
+        h = self._STATE_HEADER.unpack_from(blob, 0)
+        ngp, nstate, state_len = h[5], h[8], h[9]
+        st = np.frombuffer(blob, dtype=np.float64, count=state_len, offset=self._STATE_HEADER.size)
+        return st.reshape(-1, ngp, nstate).copy() if state_len else np.zeros((0, ngp, nstate))
+
+    def load_committed_state(self, state: np.ndarray):
+        """Replace the committed Gauss-point state (same layout as committed_state)
+        through the checkpoint path (MaterialStatus::restoreContext per point)."""
+        blob = bytearray(self.save_state())
+        h = self._STATE_HEADER.unpack_from(blob, 0)
+        state_len = h[9]
+        st = np.ascontiguousarray(state, dtype=np.float64).ravel()
+        if st.size != state_len:
+            raise ValueError(f"state has {st.size} values, the model {state_len}")
+        off = self._STATE_HEADER.size
+        blob[off:off + 8 * state_len] = st.tobytes()
+        self.restore_state(bytes(blob))
 
     def set_nr_mode(self, manrmsteps: int):
         """NRSolver manrmsteps: 0 modified Newton, k > 0 re-assembles the tangent

@@ -16,13 +16,16 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.mark.parametrize("name", ["patch100", "patch101", "patch300"])
-@pytest.mark.parametrize("mixed", [False, True])
-def test_patch_decks_meet_their_rules(name, mixed, native_lib):
+@pytest.mark.parametrize("mode", ["direct", "pcg", "mixed"])
+def test_patch_decks_meet_their_rules(name, mode, native_lib):
+    """The decks ask for the default direct solver: as written they run the
+    device LDL^T factorization; PCG to 1e-12 in FP64 and mixed precision meet
+    the same rules."""
     from oofem_gb300 import deck as dk
     path = os.path.join(GOLDEN, name + ".in")
     d = dk.read_deck(path)
-    steps = dk.run_deck(d, ctx=native_lib.Context(0), lstol=1e-12,
-                        precision=native_lib.PREC_MIXED if mixed else native_lib.PREC_FP64)
+    steps = dk.run_deck(d, ctx=native_lib.Context(0), lstol=None if mode == "direct" else 1e-12,
+                        precision=native_lib.PREC_MIXED if mode == "mixed" else native_lib.PREC_FP64)
     rules = dk.check_rules(path, d, steps)
     assert len(rules) >= 10
     assert all(ok for *_, ok in rules), [r for r in rules if not r[3]]
@@ -39,6 +42,21 @@ def test_static_structural_deck_matches_reference(native_lib):
         assert abs(s.iterations - int(g[f"s{k}_nite"])) <= 1
         assert rel(s.u, g[f"s{k}_u"]) < 1e-7
         assert rel(s.reactions, g[f"s{k}_reac"]) < 1e-7
+
+
+def test_static_structural_deck_direct_matches_reference(native_lib):
+    """The same deck as written (lstype 0): the device factorization in every
+    Newton iteration takes exactly the reference's iteration counts, fields
+    within 1e-10."""
+    from oofem_gb300 import deck as dk
+    g = load_golden("ss_mises_hex_5x2x2_accel")
+    d = dk.read_deck(os.path.join(GOLDEN, "ss_mises_hex_5x2x2_accel.in"))
+    steps = dk.run_deck(d, ctx=native_lib.Context(0))
+    assert len(steps) == int(g["nsteps"])
+    for k, s in enumerate(steps, 1):
+        assert s.iterations == int(g[f"s{k}_nite"]), (k, s.iterations, int(g[f"s{k}_nite"]))
+        assert rel(s.u, g[f"s{k}_u"]) < 1e-10
+        assert rel(s.reactions, g[f"s{k}_reac"]) < 1e-10
 
 
 @pytest.mark.parametrize("case", ["hex_cantilever_6x3x3_jit_ic", "hex_cantilever_6x3x3_jit_ilu",
