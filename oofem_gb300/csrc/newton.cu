@@ -23,7 +23,7 @@ namespace ogb {
 namespace {
 
 inline unsigned nblk(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
-constexpr int NR_GRID = NUM_SMS * 4;
+inline int nr_grid() { return num_sms() * 4; }
 
 __global__ void k_nr_assemble_u(int n, const int *__restrict__ eq, const double *__restrict__ X,
                                 const double *__restrict__ bcval, double *__restrict__ u)
@@ -245,7 +245,7 @@ int nr_ensure(ogb_model *md)
         OGB_CHECK(md->nr_X.alloc(md->neq > 0 ? md->neq : 1));
         OGB_CUDA(cudaMemsetAsync(md->nr_X.p, 0, (size_t)(md->neq > 0 ? md->neq : 1) * sizeof(double), md->ctx->stream));
     }
-    OGB_CHECK(md->nr_part.alloc((size_t)8 * NR_GRID));
+    OGB_CHECK(md->nr_part.alloc((size_t)8 * nr_grid()));
     if (!md->nr_count.p) {
         OGB_CHECK(md->nr_count.alloc(1));
         OGB_CUDA(cudaMemsetAsync(md->nr_count.p, 0, sizeof(unsigned int), md->ctx->stream));
@@ -328,14 +328,14 @@ int nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double
         OGB_CHECK(forces(md, u_node, md->v_fnode.p));   // updates the temp material state
         OGB_CUDA(cudaMemsetAsync(m->w_b.p, 0, (size_t)m->npad * sizeof(double), s));
         if (nd == 3) {
-            k_nr_rhs<3><<<NR_GRID, NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
+            k_nr_rhs<3><<<nr_grid(), NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
                                                      md->nr_count.p, out);
-            k_nr_enorm<3><<<NR_GRID, NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
+            k_nr_enorm<3><<<nr_grid(), NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
                                                        md->nr_count.p, out + 6);
         } else {
-            k_nr_rhs<2><<<NR_GRID, NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
+            k_nr_rhs<2><<<nr_grid(), NTHREADS, 0, s>>>(nn, md->eq.p, load, md->v_fnode.p, m->w_b.p, md->nr_part.p,
                                                      md->nr_count.p, out);
-            k_nr_enorm<2><<<NR_GRID, NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
+            k_nr_enorm<2><<<nr_grid(), NTHREADS, 0, s>>>((int64_t)md->nelem * md->nnpe, md->fe.p, md->nr_part.p,
                                                        md->nr_count.p, out + 4);
         }
         count_launch(ctx, 2);

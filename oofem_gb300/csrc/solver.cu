@@ -760,9 +760,9 @@ __global__ void k_ns_to_eq(int neq, const int *__restrict__ ns_of_eq, const doub
     if (e < neq) xe[e] = xn[ns_of_eq[e]];
 }
 
-inline int vec_grid(int nchunks) { return nchunks < NUM_SMS * GRID_MULT ? nchunks : NUM_SMS * GRID_MULT; }
+inline int vec_grid(int nchunks) { const int g = num_sms() * GRID_MULT; return nchunks < g ? nchunks : g; }
 // blocks of the kernels that split the rows into equal contiguous shares
-inline int bal_grid(int nchunks) { return nchunks < NUM_SMS * 4 ? nchunks : NUM_SMS * 4; }
+inline int bal_grid(int nchunks) { const int g = num_sms() * 4; return nchunks < g ? nchunks : g; }
 inline unsigned nb(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, NTHREADS); }
 
 // ---------------------------------------------------------------- operator
@@ -787,7 +787,7 @@ struct Op {
 inline int sell_split(const SellMat &S)
 {
     if (S.force_split) return S.force_split;
-    return S.nslices < NUM_SMS * 16 ? 4 : 1;
+    return S.nslices < num_sms() * 16 ? 4 : 1;
 }
 
 inline int sell_grid(const SellMat &S)
@@ -1267,7 +1267,7 @@ template <class X, class V>
 int launch_prec_diag(ogb_mtrx *m, const Op &op, const V *val, X *dinv, PcgScal *sc)
 {
     if (m->precond == 0) {
-        k_fill_one<X><<<NUM_SMS * 8, NTHREADS, 0, m->ctx->stream>>>(op.n, dinv);
+        k_fill_one<X><<<num_sms() * 8, NTHREADS, 0, m->ctx->stream>>>(op.n, dinv);
         count_launch(m->ctx);
         OGB_CUDA(cudaGetLastError());
         return OGB_OK;
@@ -1716,7 +1716,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
         if constexpr (F32) {
             if (!ctx->mixed_x64) {
                 // fold the FP32 increment into the FP64 solution
-                k_fold_increment<<<NUM_SMS * 8, NTHREADS, 0, s>>>(n, x, d);
+                k_fold_increment<<<num_sms() * 8, NTHREADS, 0, s>>>(n, x, d);
                 count_launch(ctx);
             }
         }
@@ -1847,7 +1847,7 @@ int pcg_mixed(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, o
         const int64_t ntot = m->nnz + (m->npad - m->neq);
         if (m->val32_version != m->version) {
             OGB_CHECK(m->val32.alloc(ntot));
-            k_to_float<<<NUM_SMS * 8, NTHREADS, 0, ctx->stream>>>(ntot, m->val.p, m->val32.p);
+            k_to_float<<<num_sms() * 8, NTHREADS, 0, ctx->stream>>>(ntot, m->val.p, m->val32.p);
             count_launch(ctx);
             m->val32_version = m->version;
         }
@@ -1901,7 +1901,7 @@ namespace ogb {
 namespace {
 
 constexpr int NOALLOC_MAX_ROWS = 1 << 17;           // 131,072 equations
-constexpr int NOALLOC_GRID = NUM_SMS * 2;           // fixed grid: deterministic reductions
+constexpr int NOALLOC_GRID = 304;                   // fixed grid (2 x 152 SMs of a GB300): sizes the static partials
 constexpr size_t NOALLOC_DOUBLES = (size_t)5 * NOALLOC_MAX_ROWS + 4 * NOALLOC_GRID + 16;
 
 // r, z, p, q, dinv (NOALLOC_MAX_ROWS each), reduction partials, the PcgScal
