@@ -243,54 +243,121 @@ __device__ void mises_tangent(const double *mat, const double *st, const double 
         }
 }
 
-// Symmetric 3x3 eigenvalues/vectors by cyclic Jacobi rotations, sorted descending
-// (StructuralMaterial::computePrincipalValDir, structuralmaterial.C:1337-1470).
-__device__ void sym3_eig(const double (&S)[3][3], double (&w)[3], double (&V)[3][3])
+// Principal strains of a 3-D strain vector (engineering shears) as
+// StructuralMaterial::computePrincipalValues gives them (structuralmaterial.C:1107-1262):
+// zeros unless a component exceeds 1e-20 in magnitude; the invariants of the
+// tensor with halved shears; the roots of -x^3 + I1 x^2 - I2 x + I3 in the
+// trigonometric form of cubic3r (mathfem.C:155-240: triple root when q and r
+// vanish below 1e-100, cosine argument clamped to [-1, 1]); sorted descending.
+__device__ void principal_strains(const double (&e)[6], double (&w)[3])
 {
-    double A[3][3], Q[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    bool nonzero = false;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) A[i][j] = S[i][j];
-    for (int sweep = 0; sweep < 50; ++sweep) {
-        double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-        double scale = fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]);
-        if (off <= 1e-300 || off <= 1e-17 * scale) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                if (A[p][q] == 0.0) continue;
-                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k) {
-                    double akp = A[k][p], akq = A[k][q];
-                    A[k][p] = c * akp - s * akq;
-                    A[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double apk = A[p][k], aqk = A[q][k];
-                    A[p][k] = c * apk - s * aqk;
-                    A[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double qkp = Q[k][p], qkq = Q[k][q];
-                    Q[k][p] = c * qkp - s * qkq;
-                    Q[k][q] = s * qkp + c * qkq;
-                }
-            }
+    for (int i = 0; i < 6; ++i) nonzero |= fabs(e[i]) > 1.e-20;
+    w[0] = w[1] = w[2] = 0.0;
+    if (!nonzero) return;
+    const double I1 = e[0] + e[1] + e[2];
+    const double I2 = e[0] * e[1] + e[1] * e[2] + e[2] * e[0] - 0.25 * (e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
+    const double I3 = e[0] * e[1] * e[2] +
+                      0.25 * (e[3] * e[4] * e[5] - e[0] * e[3] * e[3] - e[1] * e[4] * e[4] - e[2] * e[5] * e[5]);
+    // monic form x^3 + a x^2 + b x + c of the cubic with leading coefficient -1
+    const double a = I1 / -1.0, b = -I2 / -1.0, c = I3 / -1.0;
+    const double q = (a * a - 3.0 * b) / 9.0;
+    const double r = (2.0 * a * a * a - 9.0 * a * b + 27.0 * c) / 54.0;
+    if (fabs(q) < 1.0e-100 && fabs(r) < 1.0e-100) {
+        w[0] = w[1] = w[2] = -a / 3.0;
+    } else {
+        double h = r / sqrt(q * q * q);
+        if (fabs(h) > 1.0) h = h > 0 ? 1.0 : -1.0;
+        const double phi = acos(h), p = sqrt(q);
+        const double pi = 3.14159265358979323846;
+        w[0] = -2.0 * p * cos(phi / 3.0) - a / 3.0;
+        w[1] = -2.0 * p * cos((phi + 2.0 * pi) / 3.0) - a / 3.0;
+        w[2] = -2.0 * p * cos((phi - 2.0 * pi) / 3.0) - a / 3.0;
     }
-    int idx[3] = {0, 1, 2};
-    double ev[3] = {A[0][0], A[1][1], A[2][2]};
-    for (int ii = 0; ii < 2; ++ii)
-        for (int jj = 0; jj < 2; ++jj)
-            if (ev[idx[jj + 1]] > ev[idx[jj]]) { int t = idx[jj]; idx[jj] = idx[jj + 1]; idx[jj + 1] = t; }
-    for (int k = 0; k < 3; ++k) {
-        w[k] = ev[idx[k]];
-        for (int i = 0; i < 3; ++i) V[i][k] = Q[i][idx[k]];
-    }
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            if (w[j + 1] > w[j]) { double t = w[j]; w[j] = w[j + 1]; w[j + 1] = t; }
 }
 
-// IsotropicDamageMaterial1: Mazars equivalent strain (idm1.C:436-470), exponential
+// Principal values and directions of a symmetric 3x3 matrix as
+// StructuralMaterial::computePrincipalValDir obtains them (structuralmaterial.C:1337-1470,
+// FloatMatrix::jaco_ to 10 significant figures, floatmatrix.C:1953-2120): threshold
+// Jacobi rotations over the pairs (0,1), (0,2), (1,2) in that order; a pair is
+// rotated when |a_pq| exceeds 1e-10 of the sum of the absolute input entries, by
+// half of atan2(2 a_pq, a_pp - a_qq); sweeps stop once the rotated entries of a
+// sweep sum to no more than that fraction (51 sweeps at most). The loose stopping
+// rule is part of the result: the crack normal of a damaged point carries it.
+// Values sorted descending with their vectors (columns of V).
+__device__ void principal_dirs(const double (&S)[3][3], double (&w)[3], double (&V)[3][3])
+{
+    double u[3][3];   // the upper triangle is the working matrix, as in jaco_
+    double ev[3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            u[i][j] = S[i][j];
+            V[i][j] = i == j ? 1.0 : 0.0;
+        }
+    for (int i = 0; i < 3; ++i) ev[i] = u[i][i];
+    const double tol = 1.0e-10;   // 0.1^10
+    double sum = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sum += fabs(u[i][j]);
+    if (sum > 0.0) {
+        int sweeps = 0;
+        double ssum;
+        do {
+            ssum = 0.0;
+            for (int j = 1; j < 3; ++j)
+                for (int i = 0; i < j; ++i) {
+                    if (!(fabs(u[i][j]) / sum > tol)) continue;
+                    ssum += fabs(u[i][j]);
+                    const double ang = atan2(u[i][j] * 2.0, ev[i] - ev[j]) / 2.0;
+                    const double si = sin(ang), co = cos(ang);
+                    double t;
+                    for (int k = 0; k < i; ++k) {
+                        t = u[k][i];
+                        u[k][i] = co * t + si * u[k][j];
+                        u[k][j] = -si * t + co * u[k][j];
+                    }
+                    t = ev[i];
+                    ev[i] = co * t + si * u[i][j];
+                    const double aij = -si * t + co * u[i][j];
+                    for (int k = i + 1; k < j; ++k) {
+                        t = u[i][k];
+                        u[i][k] = co * t + si * u[k][j];
+                        u[k][j] = -si * t + co * u[k][j];
+                    }
+                    t = u[i][j];
+                    const double aji = co * t + si * ev[j];
+                    ev[j] = -si * t + co * ev[j];
+                    for (int k = j + 1; k < 3; ++k) {
+                        t = u[i][k];
+                        u[i][k] = co * t + si * u[j][k];
+                        u[j][k] = -si * t + co * u[j][k];
+                    }
+                    for (int k = 0; k < 3; ++k) {
+                        t = V[k][i];
+                        V[k][i] = co * t + si * V[k][j];
+                        V[k][j] = -si * t + co * V[k][j];
+                    }
+                    ev[i] = co * ev[i] + si * aji;
+                    ev[j] = -si * aij + co * ev[j];
+                    u[i][j] = 0.0;
+                }
+        } while (++sweeps <= 50 && fabs(ssum) / sum > tol);
+    }
+    for (int ii = 0; ii < 2; ++ii)
+        for (int jj = 0; jj < 2; ++jj)
+            if (ev[jj + 1] > ev[jj]) {
+                double t = ev[jj]; ev[jj] = ev[jj + 1]; ev[jj + 1] = t;
+                for (int k = 0; k < 3; ++k) { t = V[k][jj]; V[k][jj] = V[k][jj + 1]; V[k][jj + 1] = t; }
+            }
+    for (int i = 0; i < 3; ++i) w[i] = ev[i];
+}
+
+// IsotropicDamageMaterial1: Mazars equivalent strain (idm1.C:436-470) from the
+// principal strains above, exponential
 // cohesive crack (idm1.C:808-911, wf = gf/(E e0), ef = wf/Le, Newton until
 // |R| < e0*1e-9, at most 40 steps), crack band on first damage (initDamaged
 // idm1.C:1168-1322, Element::giveLengthInDir element.C:1162-1183), strain-level
@@ -305,7 +372,7 @@ __device__ void idm1_stress(const double *mat, const double (&eps)[6], double *s
                       {0.5 * eps[5], eps[1], 0.5 * eps[3]},
                       {0.5 * eps[4], 0.5 * eps[3], eps[2]}};
     double w[3], V[3][3];
-    sym3_eig(T, w, V);
+    principal_strains(eps, w);
     double pos = 0;
     for (int i = 0; i < 3; ++i)
         if (w[i] > 0.0) pos += w[i] * w[i];
@@ -318,6 +385,7 @@ __device__ void idm1_stress(const double *mat, const double (&eps)[6], double *s
     } else {
         tempKappa = equiv;
         if (tempKappa > e0 && (omega0 == 0.0 || le == 0.0)) {
+            principal_dirs(T, w, V);
             int indx = 0;
             for (int i = 1; i < 3; ++i)
                 if (w[i] > w[indx]) indx = i;

@@ -18,6 +18,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#define ORO_PI 3.14159265358979323846
+
 /* 2-point Gauss abscissa exactly as the reference writes it
  * (src/core/gaussintegrationrule.C:1436-1452): a 15-digit literal, not 1/sqrt(3). */
 static const double GP2 = 0.577350269189626;
@@ -593,50 +595,118 @@ static void mises_tangent_3d(const double *mat, const double *st, double *D)
     for (int i = 0; i < 36; ++i) D[i] += factor2 * Idev[i];
 }
 
-/* Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations; values sorted
- * descending with their vectors (columns of V), as
- * StructuralMaterial::computePrincipalValDir (structuralmaterial.C:1337-1470). */
-static void sym3_eig(const double *Sin, double *w, double *V)
+/* Principal strains of a 3-D strain vector (engineering shears) as
+ * StructuralMaterial::computePrincipalValues (structuralmaterial.C:1107-1262) gives
+ * them: zeros unless some component exceeds 1e-20 in magnitude; the invariants
+ * I1, I2, I3 of the tensor with halved shears; the real roots of
+ * -x^3 + I1 x^2 - I2 x + I3 by the trigonometric form of cubic3r
+ * (mathfem.C:155-240: a triple root when q and r vanish below 1e-100, the cosine
+ * argument clamped to [-1, 1]); sorted in descending order. */
+static void principal_strains(const double *e, double *w)
 {
-    double A[3][3], Q[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) A[i][j] = Sin[i * 3 + j];
-    for (int sweep = 0; sweep < 50; ++sweep) {
-        double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-        double scale = fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]);
-        if (off <= 1e-300 || off <= 1e-17 * scale) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                if (A[p][q] == 0.0) continue;
-                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k) {
-                    double akp = A[k][p], akq = A[k][q];
-                    A[k][p] = c * akp - s * akq;
-                    A[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double apk = A[p][k], aqk = A[q][k];
-                    A[p][k] = c * apk - s * aqk;
-                    A[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double qkp = Q[k][p], qkq = Q[k][q];
-                    Q[k][p] = c * qkp - s * qkq;
-                    Q[k][q] = s * qkp + c * qkq;
-                }
-            }
+    int nonzero = 0;
+    for (int i = 0; i < 6; ++i)
+        if (fabs(e[i]) > 1.e-20) nonzero = 1;
+    w[0] = w[1] = w[2] = 0.0;
+    if (!nonzero) return;
+    double I1 = e[0] + e[1] + e[2];
+    double I2 = e[0] * e[1] + e[1] * e[2] + e[2] * e[0] - 0.25 * (e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
+    double I3 = e[0] * e[1] * e[2] + 0.25 * (e[3] * e[4] * e[5] - e[0] * e[3] * e[3] - e[1] * e[4] * e[4] -
+                                             e[2] * e[5] * e[5]);
+    /* monic form x^3 + a x^2 + b x + c of the cubic with leading coefficient -1 */
+    double a = I1 / -1.0, b = -I2 / -1.0, c = I3 / -1.0;
+    double q = (a * a - 3.0 * b) / 9.0;
+    double r = (2.0 * a * a * a - 9.0 * a * b + 27.0 * c) / 54.0;
+    if (fabs(q) < 1.0e-100 && fabs(r) < 1.0e-100) {
+        w[0] = w[1] = w[2] = -a / 3.0;
+    } else {
+        double h = r / sqrt(q * q * q);
+        if (fabs(h) > 1.0) h = h > 0 ? 1.0 : -1.0;
+        double phi = acos(h), p = sqrt(q);
+        w[0] = -2.0 * p * cos(phi / 3.0) - a / 3.0;
+        w[1] = -2.0 * p * cos((phi + 2.0 * ORO_PI) / 3.0) - a / 3.0;
+        w[2] = -2.0 * p * cos((phi - 2.0 * ORO_PI) / 3.0) - a / 3.0;
     }
-    int idx[3] = {0, 1, 2};
-    double ev[3] = {A[0][0], A[1][1], A[2][2]};
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            if (w[j + 1] > w[j]) { double t = w[j]; w[j] = w[j + 1]; w[j + 1] = t; }
+}
+
+/* Principal values and directions of a symmetric 3x3 matrix as
+ * StructuralMaterial::computePrincipalValDir obtains them (structuralmaterial.C:1337-1470
+ * with FloatMatrix::jaco_ to 10 significant figures, floatmatrix.C:1953-2120):
+ * threshold Jacobi rotations over the pairs (0,1), (0,2), (1,2) in that order; a
+ * pair is rotated when |a_pq| exceeds 1e-10 of the sum of the absolute entries of
+ * the input, by half of atan2(2 a_pq, a_pp - a_qq); sweeps stop once the rotated
+ * entries of a sweep sum to no more than that fraction (51 sweeps at most). The
+ * loose stopping rule is part of the result (the crack normal of a damaged point
+ * carries it). Values sorted descending with their vectors (columns of V). */
+static void principal_dirs(const double *S, double *w, double *V)
+{
+    double u[3][3];   /* upper triangle is the working matrix, as in jaco_ */
+    double ev[3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            u[i][j] = S[i * 3 + j];
+            V[i * 3 + j] = i == j ? 1.0 : 0.0;
+        }
+    for (int i = 0; i < 3; ++i) ev[i] = u[i][i];
+    const double tol = pow(0.1, 10);
+    double sum = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sum += fabs(u[i][j]);
+    if (sum > 0.0) {
+        int sweeps = 0;
+        double ssum;
+        do {
+            ssum = 0.0;
+            for (int j = 1; j < 3; ++j)
+                for (int i = 0; i < j; ++i) {
+                    if (!(fabs(u[i][j]) / sum > tol)) continue;
+                    ssum += fabs(u[i][j]);
+                    double ang = atan2(u[i][j] * 2.0, ev[i] - ev[j]) / 2.0;
+                    double si = sin(ang), co = cos(ang), t;
+                    for (int k = 0; k < i; ++k) {
+                        t = u[k][i];
+                        u[k][i] = co * t + si * u[k][j];
+                        u[k][j] = -si * t + co * u[k][j];
+                    }
+                    t = ev[i];
+                    ev[i] = co * t + si * u[i][j];
+                    double aij = -si * t + co * u[i][j];
+                    for (int k = i + 1; k < j; ++k) {
+                        t = u[i][k];
+                        u[i][k] = co * t + si * u[k][j];
+                        u[k][j] = -si * t + co * u[k][j];
+                    }
+                    t = u[i][j];
+                    double aji = co * t + si * ev[j];
+                    ev[j] = -si * t + co * ev[j];
+                    for (int k = j + 1; k < 3; ++k) {
+                        t = u[i][k];
+                        u[i][k] = co * t + si * u[j][k];
+                        u[j][k] = -si * t + co * u[j][k];
+                    }
+                    for (int k = 0; k < 3; ++k) {
+                        t = V[k * 3 + i];
+                        V[k * 3 + i] = co * t + si * V[k * 3 + j];
+                        V[k * 3 + j] = -si * t + co * V[k * 3 + j];
+                    }
+                    ev[i] = co * ev[i] + si * aji;
+                    ev[j] = -si * aij + co * ev[j];
+                    u[i][j] = 0.0;
+                }
+        } while (++sweeps <= 50 && fabs(ssum) / sum > tol);
+    }
     for (int ii = 0; ii < 2; ++ii)
         for (int jj = 0; jj < 2; ++jj)
-            if (ev[idx[jj + 1]] > ev[idx[jj]]) { int t = idx[jj]; idx[jj] = idx[jj + 1]; idx[jj + 1] = t; }
-    for (int k = 0; k < 3; ++k) {
-        w[k] = ev[idx[k]];
-        for (int i = 0; i < 3; ++i) V[i * 3 + k] = Q[i][idx[k]];
-    }
+            if (ev[jj + 1] > ev[jj]) {
+                double t = ev[jj]; ev[jj] = ev[jj + 1]; ev[jj + 1] = t;
+                for (int k = 0; k < 3; ++k) {
+                    t = V[k * 3 + jj]; V[k * 3 + jj] = V[k * 3 + jj + 1]; V[k * 3 + jj + 1] = t;
+                }
+            }
+    for (int i = 0; i < 3; ++i) w[i] = ev[i];
 }
 
 /* a13: IsotropicDamageMaterial1 with Mazars equivalent strain (idm1.C:436-470,
@@ -656,7 +726,7 @@ static void idm1_stress_3d(const double *mat, const double *eps, double *st,
                    0.5 * eps[5], eps[1], 0.5 * eps[3],
                    0.5 * eps[4], 0.5 * eps[3], eps[2]};
     double w[3], V[9];
-    sym3_eig(T, w, V);
+    principal_strains(eps, w);
     double pos = 0;
     for (int i = 0; i < 3; ++i)
         if (w[i] > 0.0) pos += w[i] * w[i];
@@ -669,6 +739,7 @@ static void idm1_stress_3d(const double *mat, const double *eps, double *st,
     } else {
         tempKappa = equiv;
         if (tempKappa > e0 && (omega0 == 0.0 || le == 0.0)) {
+            principal_dirs(T, w, V);
             int indx = 0;
             for (int i = 1; i < 3; ++i)
                 if (w[i] > w[indx]) indx = i;
