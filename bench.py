@@ -650,6 +650,51 @@ def run_gpu_idm1_batch(args):
     print(json.dumps(out))
 
 
+SWEEP_FORMS = {1: "plain loop", 2: "prefetch 1", 3: "prefetch 4", 4: "TMA-staged", 5: "2 warps per slice",
+               6: "4 warps per slice", 0: "library choice", 8: "half-stored (mixed only)"}
+
+
+def run_spmv_forms(args):
+    """Every node-block SpMV form on this GPU (how the split rule and the
+    autotuner's candidate forms were chosen): for each cantilever of
+    --sweep-sizes and each precision, one warm-up LinearStatic solve to 1e-8 per
+    form (OGB_OPT_SPMV_VARIANT 1..6, 0 = the library's choice of the full-copy
+    form, 8 = the half-stored FP32 operator of mixed solves), then one timed solve
+    with kernel timing on; one JSON line per run (step time, PCG iterations, mean
+    device time and algorithmic bandwidth of the sampled SpMV launches)."""
+    import time as _t
+    from oofem_gb300 import meshgen as mg, native
+    sizes = [tuple(int(v) for v in sz.split("x")) for sz in args.sweep_sizes.split(",")]
+    for dims in sizes:
+        mesh = mg.hex_cantilever(*dims, h=WORKLOAD["h"], jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"])
+        ctx = native.Context(0)
+        model = native.GpuModel(ctx, mesh)
+        A = native.GpuCsrMtrx(ctx)
+        model.build_matrix(A)
+        for prec in (native.PREC_MIXED, native.PREC_FP64):
+            for v in (1, 2, 3, 4, 5, 6, 0, 8):
+                if v == 8 and prec != native.PREC_MIXED:
+                    continue
+                ctx.set_option(native.OPT_SPMV_VARIANT, 0 if v == 8 else v)
+                ctx.set_option(native.OPT_SPMV_HALF, 2 if v == 8 else 0)
+                model.linear_static(A, rtol=RTOL, maxit=200000, precision=prec)
+                ctx.profile(True)
+                ctx.profile_read()
+                t0 = _t.perf_counter()
+                _, _, info = model.linear_static(A, rtol=RTOL, maxit=200000, precision=prec)
+                dt = _t.perf_counter() - t0
+                ms, n, by = ctx.profile_read()
+                ctx.profile(False)
+                print(json.dumps(dict(mesh="x".join(map(str, dims)), precision="mixed" if prec else "fp64",
+                                      form=SWEEP_FORMS[v], variant=v, step_ms=round(dt * 1e3, 3),
+                                      iterations=info.iterations, spmv_us=round(1e3 * ms / max(n, 1), 2),
+                                      spmv_gbs=round((by / n) / (ms / n * 1e-3) / 1e9, 1) if n else None)),
+                      flush=True)
+        A.close()
+        model.close()
+        ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -662,7 +707,9 @@ def main():
     ap.add_argument("--ny", type=int, default=0)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--workload", default="cantilever",
-                    choices=["cantilever", "rve_batch", "mises_block", "idm1_batch"])
+                    choices=["cantilever", "rve_batch", "mises_block", "idm1_batch", "spmv_forms"])
+    ap.add_argument("--sweep-sizes", default="100x20x20,200x40x40,290x58x58",
+                    help="spmv_forms: cantilevers to sweep")
     ap.add_argument("--cube-n", type=int, default=40)
     ap.add_argument("--seeds", type=int, default=8)
     ap.add_argument("--idm-steps", type=int, default=16)
@@ -687,6 +734,8 @@ def main():
         run_gpu_newton(args)
     elif args.workload == "idm1_batch":
         run_gpu_idm1_batch(args)
+    elif args.workload == "spmv_forms":
+        run_spmv_forms(args)
     else:
         run_gpu(args)
 

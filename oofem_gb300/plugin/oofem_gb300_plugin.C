@@ -7,7 +7,7 @@
 // Build this file together with an OOFEM build (it includes the reference's
 // headers and links liboofem and liboofem_gb300); load it after liboofem so its
 // registrations are the ones in force (link it into the oofem executable with
-// --no-as-needed, or LD_PRELOAD it). See INTEGRATION.md.
+// --no-as-needed, or LD_PRELOAD it).
 //
 // Interfaces mirrored:
 //   SparseMtrx            src/core/sparsemtrx.h:62-303
@@ -74,10 +74,20 @@ static void gb300_check(int code, const char *what)
     }
 }
 
-// Set while a GpuCsrMtrx assembles its elements on the device (the GPU element
-// classes then hand an empty matrix to the host loop, which EngngModel::assemble
-// skips, engngm.C:913-915).
-static bool g_device_elements = false;
+class GpuCsrMtrx;
+// The GpuCsrMtrx whose element loop is in progress and whose elements are
+// evaluated on the device, or null. Only inside that window do the GPU element
+// classes hand an empty stiffness to the host loop (EngngModel::assemble skips
+// it, engngm.C:913-915); every other caller of the element stiffness -- the
+// extrapolated-force loops of the IG_Tangent initial guess
+// (EngngModel::assemblePrescribedExtrapolatedForces / assembleExtrapolatedForces,
+// engngm.C:1536-1666), other matrices, output -- gets the real matrix. The window
+// opens where the drivers start an assembly of this matrix (zero() before
+// NonLinearStatic / StaticStructural re-assemble it, nlinearstatic.C:621-641,
+// staticstructural.C:418-437; buildInternalStructure() under LinearStatic, which
+// assembles right after it, linearstatic.C:197-199) and closes in assembleEnd()
+// (engngm.C:1035-1036) or when the matrix is destroyed.
+static const GpuCsrMtrx *g_device_assembly = nullptr;
 
 /// SparseMtrx whose storage lives on the GPU: the full-pattern CSR (== CompCol),
 /// plus the node-block copy used by the solver when built from a mesh.
@@ -86,7 +96,8 @@ class GpuCsrMtrx : public SparseMtrx
 protected:
     ogb_mtrx *m = nullptr;
     ogb_model *model = nullptr;
-    std::vector< double >bcMaskDummy;
+    EngngModel *emodel = nullptr;   // model and domain the device elements mirror
+    int domainIndex = 1;
     // writes through at(i,j) are kept on the host and flushed before any device use
     mutable std::map< std::pair< int, int >, double >pending;
 
@@ -98,8 +109,65 @@ protected:
         pending.clear();
     }
 
+    // Equation numbers of the device model against OOFEM's own (default numbering,
+    // EngngModel::forceEquationNumbering engngm.C:469-530): the same count, and for
+    // every node the same DOFs (D_u, D_v[, D_w], master DOFs only) with the same
+    // number (free > 0, prescribed 0). Any difference -- renumber 1 (Sloan), slave
+    // or extra DOFs, a boundary condition whose activity changed -- means the
+    // device pattern and OOFEM's vectors would not line up.
+    bool numberingMatches(EngngModel *eModel, int di) const
+    {
+        if ( !model ) {
+            return false;
+        }
+        Domain *d = eModel->giveDomain(di);
+        EModelDefaultEquationNumbering dn;
+        int neq = 0, npeq = 0;
+        if ( ogb_model_neq(model, & neq, & npeq) != OGB_OK || neq != eModel->giveNumberOfDomainEquations(di, dn) ) {
+            return false;
+        }
+        const int nn = d->giveNumberOfDofManagers();
+        const int ndofpn = ( int ) ( eqCache.size() / ( nn > 0 ? nn : 1 ) );
+        if ( ( size_t ) nn * ndofpn != eqCache.size() ) {
+            return false;
+        }
+        for ( int i = 1; i <= nn; i++ ) {
+            DofManager *dm = d->giveDofManager(i);
+            if ( dm->giveNumberOfDofs() != ndofpn ) {
+                return false;
+            }
+            int k = 0;
+            for ( Dof *dof : *dm ) {
+                if ( !dof->isPrimaryDof() || ( int ) dof->giveDofID() != k + 1 ) {
+                    return false;
+                }
+                const int mine = eqCache [ ( size_t ) ( i - 1 ) * ndofpn + k ];
+                if ( dof->giveEquationNumber(dn) != ( mine > 0 ? mine : 0 ) ) {
+                    return false;
+                }
+                k++;
+            }
+        }
+        return true;
+    }
+    std::vector< int >eqCache;   // device equation numbers (nnodes x ndofpn, +free / -prescribed)
+
+    void dropDeviceElements()
+    {
+        if ( g_device_assembly == this ) {
+            g_device_assembly = nullptr;
+        }
+        if ( model ) {
+            ogb_model_destroy(model);
+            model = nullptr;
+        }
+        eqCache.clear();
+    }
+
     // Mesh of LSpace / LTRSpace / PlaneStress2d elements with isotropic linear
-    // elastic materials: build the device element backend (K1 + gather assembly).
+    // elastic materials whose numbering the device reproduces: build the device
+    // element backend (K1 + gather assembly). False (host element loop and
+    // location arrays) for anything else.
     bool tryDeviceElements(EngngModel *eModel, int di)
     {
         Domain *d = eModel->giveDomain(di);
@@ -164,7 +232,16 @@ protected:
         }
         gb300_check(ogb_model_create(gb300_context(), etype, nn, coords.data(), ne, conn.data(), emat.data(),
                                      ( int ) matIndex.size(), mats.data(), thickness, bc.data(), & model), "ogb_model_create");
+        eqCache.assign( ( size_t ) nn * ndofpn, 0 );
+        gb300_check(ogb_model_equations(model, eqCache.data() ), "ogb_model_equations");
+        if ( !numberingMatches(eModel, di) ) {
+            OOFEM_LOG_INFO("GpuCsrMtrx: equation numbering differs from the device's, host element loop used\n");
+            dropDeviceElements();
+            return false;
+        }
         gb300_check(ogb_model_build_matrix(model, m), "ogb_model_build_matrix");
+        emodel = eModel;
+        domainIndex = di;
         return true;
     }
 
@@ -172,13 +249,12 @@ public:
     GpuCsrMtrx() : SparseMtrx() { gb300_check(ogb_mtrx_create(gb300_context(), & m), "ogb_mtrx_create"); }
     ~GpuCsrMtrx() override
     {
-        if ( model ) {
-            ogb_model_destroy(model);
-        }
+        dropDeviceElements();
         ogb_mtrx_destroy(m);
     }
 
     ogb_mtrx *handle() const { flush(); return m; }
+    bool deviceElements() const { return model != nullptr; }
 
     // SparseMtrx::buildInternalStructure (sparsemtrx.h:198; CompCol compcol.C:174-272)
     int buildInternalStructure(EngngModel *eModel, int di, const UnknownNumberingScheme &s) override
@@ -187,12 +263,12 @@ public:
         int neq = eModel->giveNumberOfDomainEquations(di, s);
         nRows = nColumns = neq;
         pending.clear();
-        if ( model ) {
-            ogb_model_destroy(model);
-            model = nullptr;
-        }
-        g_device_elements = s.isDefault() && tryDeviceElements(eModel, di);
-        if ( g_device_elements ) {
+        dropDeviceElements();
+        if ( s.isDefault() && tryDeviceElements(eModel, di) ) {
+            // LinearStatic assembles right after building the structure
+            if ( std::string(eModel->giveClassName() ) == "LinearStatic" ) {
+                g_device_assembly = this;
+            }
             this->version++;
             return 1;
         }
@@ -237,7 +313,25 @@ public:
     // EngngModel::assemble (engngm.C:1035-1036): the device launch hook.
     int assembleEnd() override
     {
-        int r = model ? ogb_model_assemble_stiffness(model, m) : ogb_mtrx_assemble_end(m);
+        const bool device = model && g_device_assembly == this;
+        if ( g_device_assembly == this ) {
+            g_device_assembly = nullptr;
+        }
+        int r;
+        if ( device ) {
+            // the numbering may have moved since the structure was built (a boundary
+            // condition switched on or off): rebuild the device mesh from the current
+            // state, and refuse to go on if it still does not match OOFEM's
+            if ( !numberingMatches(emodel, domainIndex) ) {
+                dropDeviceElements();
+                if ( !tryDeviceElements(emodel, domainIndex) ) {
+                    OOFEM_ERROR("GpuCsrMtrx: equation numbering changed and the device mesh cannot follow it");
+                }
+            }
+            r = ogb_model_assemble_stiffness(model, m);
+        } else {
+            r = ogb_mtrx_assemble_end(m);
+        }
         gb300_check(r, "assembleEnd");
         this->version++;
         return 1;
@@ -247,12 +341,20 @@ public:
     {
         pending.clear();
         gb300_check(ogb_mtrx_zero(m), "zero");
+        if ( model ) {
+            g_device_assembly = this;   // the drivers zero the matrix right before assembling it
+        }
         this->version++;
     }
 
     void times(const FloatArray &x, FloatArray &answer) const override
     {
         flush();
+        int neq = 0;
+        gb300_check(ogb_mtrx_neq(m, & neq), "times");
+        if ( x.giveSize() != nRows || neq != nRows ) {
+            OOFEM_ERROR("GpuCsrMtrx::times: size mismatch");
+        }
         answer.resize(nRows);
         gb300_check(ogb_mtrx_times(m, x.givePointer(), answer.givePointer() ), "times");
     }
@@ -319,8 +421,14 @@ public:
         if ( !g ) {
             OOFEM_ERROR("GpuPcgSolver needs a GpuCsrMtrx (smtype 11)");
         }
+        int neq = 0;
+        if ( ogb_mtrx_neq(g->handle(), & neq) != OGB_OK || b.giveSize() != A.giveNumberOfRows() || neq != b.giveSize() ) {
+            OOFEM_ERROR("GpuPcgSolver: right-hand side of %d entries for a matrix of %d equations",
+                        b.giveSize(), A.giveNumberOfRows() );
+        }
         if ( x.giveSize() != b.giveSize() ) {
-            OOFEM_ERROR("size mismatch");
+            x.resize(b.giveSize() );
+            x.zero();
         }
         ogb_solve_info info;
         if ( ogb_mtrx_set_preconditioner(g->handle(), precond) != OGB_OK ) {
@@ -383,9 +491,10 @@ REGISTER_SparseLinSolver(GpuPcgSolver, ST_GpuPcg);
 
 // GPU element backend: the same keywords as the reference elements, registered
 // after them so they take over for an unchanged input file (classfactory.C:128-133
-// stores the latest creator). While a GpuCsrMtrx assembles on the device the
-// stiffness handed to the host loop is empty; everything else (internal forces,
-// output, context) is the reference element's.
+// stores the latest creator). While a GpuCsrMtrx assembles on the device (the
+// window of g_device_assembly) the stiffness handed to the host loop is empty;
+// everything else (internal forces, the extrapolated forces of IG_Tangent, output,
+// context) is the reference element's.
 #define GB300_DEVICE_ELEMENT(NAME, BASE, KEYWORD)                                              \
     class NAME : public BASE                                                                    \
     {                                                                                           \
@@ -393,7 +502,7 @@ REGISTER_SparseLinSolver(GpuPcgSolver, ST_GpuPcg);
         NAME(int n, Domain *d) : BASE(n, d) { }                                                 \
         void computeStiffnessMatrix(FloatMatrix &answer, MatResponseMode rMode, TimeStep *tStep) override \
         {                                                                                       \
-            if ( g_device_elements ) {                                                          \
+            if ( g_device_assembly ) {                                                          \
                 answer.clear();                                                                 \
                 return;                                                                         \
             }                                                                                   \

@@ -186,7 +186,7 @@ def reference_patch_decks(ref_src):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference")
+    ap.add_argument("--ref-src", required=True, help="reference source tree (its tests/sm decks)")
     ap.add_argument("--work", default=os.path.join(ROOT, "_work", "golden"))
     ap.add_argument("--only", default="")
     args = ap.parse_args()

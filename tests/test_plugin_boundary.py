@@ -2,8 +2,8 @@
 against the reference's headers, links against a reference build, and takes
 over the class factory: the reference executable run on an unchanged deck with
 `smtype 11 lstype 9` constructs GpuCsrMtrx (without a GPU it then stops at
-context creation, which is what this CPU test checks). Skipped where no
-reference source tree and build are available."""
+context creation, which is what this CPU test checks). Skipped unless
+OOFEM_REF_SRC and OOFEM_REF_BUILD name a reference source tree and build."""
 import os
 import subprocess
 
@@ -11,12 +11,13 @@ import pytest
 
 from conftest import ROOT
 
-REF_SRC = os.environ.get("OOFEM_REF_SRC", "/root/reference")
-REF_BUILD = os.environ.get("OOFEM_REF_BUILD", "/tmp/oofem_probe")
+REF_SRC = os.environ.get("OOFEM_REF_SRC", "")
+REF_BUILD = os.environ.get("OOFEM_REF_BUILD", "")
 
 pytestmark = pytest.mark.skipif(
-    not (os.path.isdir(os.path.join(REF_SRC, "src")) and os.path.exists(os.path.join(REF_BUILD, "liboofem.so"))),
-    reason="needs the reference source tree and a reference build")
+    not (REF_SRC and REF_BUILD and os.path.isdir(os.path.join(REF_SRC, "src"))
+         and os.path.exists(os.path.join(REF_BUILD, "liboofem.so"))),
+    reason="needs OOFEM_REF_SRC (reference source tree) and OOFEM_REF_BUILD (a reference build)")
 
 
 def test_plugin_registers_through_the_class_factory(tmp_path, native_lib):
