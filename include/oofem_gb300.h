@@ -112,10 +112,17 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   copy. The sum order differs from the full copy's (results agree to FP32
  *   rounding of the operator, not bitwise). */
 #define OGB_OPT_SPMV_HALF 8
+/*   OGB_OPT_MIXED_BLOCK_JACOBI (0/1, default 1): mixed solves on a matrix
+ *   assembled from a model precondition with the FP32 inverses of the node
+ *   ND x ND diagonal blocks (block Jacobi) where the diagonal preconditioner
+ *   (lsprecond 1) is selected; 0 keeps the scalar diagonal. FP64 solves always
+ *   use the reference's scalar DiagPreconditioner. */
+#define OGB_OPT_MIXED_BLOCK_JACOBI 9
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
- * graphs, the ninth of each replayed 16-iteration batch inside them; ogb_ctx_profile_read
+ * graphs, the ninth of each replayed 16-iteration batch inside them, not the FP64
+ * residual products of mixed solves; ogb_ctx_profile_read
  * returns the summed device time (ms), the launch count and the algorithmic
  * bytes of those launches (values + column indices + row pointers + x + y),
  * and resets the counters. No reference counterpart (instrumentation). */
@@ -173,6 +180,10 @@ OGB_API int ogb_mtrx_set_preconditioner(ogb_mtrx *m, int type);
  * used the half-stored copy (OGB_OPT_SPMV_HALF). Instrumentation, no reference
  * counterpart. */
 OGB_API int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_per_slice);
+/* 1 when the last mixed solve on this matrix preconditioned with the block-Jacobi
+ * inverses (OGB_OPT_MIXED_BLOCK_JACOBI), else 0. Instrumentation, no reference
+ * counterpart. */
+OGB_API int ogb_mtrx_mixed_block_jacobi(ogb_mtrx *m, int *used);
 /* SparseMtrx::giveVersion (sparsemtrx.h:82): bumped on every mutation. */
 OGB_API int ogb_mtrx_version(ogb_mtrx *m, int64_t *version);
 

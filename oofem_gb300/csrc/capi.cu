@@ -380,6 +380,7 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         if (value < 0 || value > 2) return fail(OGB_E_ARG, "half-stored SpMV option must be 0, 1 or 2");
         ctx->spmv_half = (int)value;
         return OGB_OK;
+    case OGB_OPT_MIXED_BLOCK_JACOBI: ctx->mixed_bj = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
         ctx->mixed_drop = value * 1e-6;
@@ -600,6 +601,13 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
     if (fp32_form) *fp32_form = sell ? (m->last_half ? 8 : m->sell.group[1]) : 0;
     if (warps_per_slice) *warps_per_slice = sell ? (m->sell.force_split ? m->sell.force_split
                                                     : (m->sell.nslices < num_sms() * 16 ? 4 : 1)) : 0;
+    return OGB_OK;
+}
+
+int ogb_mtrx_mixed_block_jacobi(ogb_mtrx *m, int *used)
+{
+    if (!m || !used) return fail(OGB_E_ARG, "null argument");
+    *used = m->last_bj ? 1 : 0;
     return OGB_OK;
 }
 

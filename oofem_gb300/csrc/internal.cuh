@@ -231,6 +231,7 @@ struct ogb_ctx {
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
+    bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;
 };
@@ -256,6 +257,8 @@ struct ogb_mtrx {
     // solver workspace
     ogb::DBuf<double> w_r, w_z, w_p, w_q, w_dinv, w_x, w_b, w_part, w_d;
     ogb::DBuf<float> w_r32, w_z32, w_p32, w_q32, w_dinv32, w_x32;
+    ogb::DBuf<float> w_binv32;   // block-Jacobi inverses of the node diagonal blocks (ND*ND planes)
+    bool last_bj = false;        // the last mixed solve used the block-Jacobi preconditioner
     ogb::DBuf<ogb::PcgScal> w_scal;
     ogb::HBuf<ogb::PcgScal> h_scal;
     ogb::DBuf<unsigned int> w_count;

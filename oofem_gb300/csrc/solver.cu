@@ -452,26 +452,11 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__res
 }
 
 // Residual replacement: r32 = r64, z = D^-1 r32, beta = r.z / rho (0 at the start).
-template <class X, class P>
-__global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const double *__restrict__ r64,
-                                                            X *__restrict__ r, X *__restrict__ z,
-                                                            const P *__restrict__ p, const X *__restrict__ dinv,
-                                                            double *part, unsigned int *count, PcgScal *sc, int first,
-                                                            int orth, int cycle_cap)
+// Epilogue of the replacement kernels: ||r64||^2, r.z, r.p -> rho, beta, the
+// coefficient of z in the next p update and the end of the new cycle.
+__device__ __forceinline__ void finish_replace(double (&v)[3], double *part, unsigned int *count, PcgScal *sc,
+                                               int first, int orth, int cycle_cap)
 {
-    double v[3] = {0, 0, 0};
-    for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
-        for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
-            int row = c * CHUNK + i;
-            double r6 = r64[row];
-            X rr = (X)r6;
-            X zz = rr * dinv[row];
-            r[row] = rr;
-            z[row] = zz;
-            v[0] += r6 * r6;
-            v[1] += (double)rr * (double)zz;
-            v[2] += (double)rr * (double)p[row];
-        }
     block_sum<3>(v);
     if (publish_partials<3>(v, part, count)) {
         double t[3];
@@ -495,6 +480,108 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const d
         // after cycle_cap iterations, so the FP64 residual is looked at again
         sc->cycle_end = sc->iters + cycle_cap;
     }
+}
+
+template <class X, class P>
+__global__ void __launch_bounds__(NTHREADS) k_mixed_replace(int nchunks, const double *__restrict__ r64,
+                                                            X *__restrict__ r, X *__restrict__ z,
+                                                            const P *__restrict__ p, const X *__restrict__ dinv,
+                                                            double *part, unsigned int *count, PcgScal *sc, int first,
+                                                            int orth, int cycle_cap)
+{
+    double v[3] = {0, 0, 0};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
+        for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
+            int row = c * CHUNK + i;
+            double r6 = r64[row];
+            X rr = (X)r6;
+            X zz = rr * dinv[row];
+            r[row] = rr;
+            z[row] = zz;
+            v[0] += r6 * r6;
+            v[1] += (double)rr * (double)zz;
+            v[2] += (double)rr * (double)p[row];
+        }
+    finish_replace(v, part, count, sc, first, orth, cycle_cap);
+}
+
+// Block-Jacobi form of k_mixed_replace: z_A = B_A^-1 r_A per node (FP32 vectors).
+template <int ND, class P>
+__global__ void __launch_bounds__(NTHREADS) k_mixed_replace_bj(int64_t nnodes, const double *__restrict__ r64,
+                                                               float *__restrict__ r, float *__restrict__ z,
+                                                               const P *__restrict__ p, const float *__restrict__ binv,
+                                                               double *part, unsigned int *count, PcgScal *sc,
+                                                               int first, int orth, int cycle_cap)
+{
+    double v[3] = {0, 0, 0};
+    int64_t lo, hi;
+    block_range(nnodes, lo, hi);
+    for (int64_t a = lo + threadIdx.x; a < hi; a += NTHREADS) {
+        float rr[ND];
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const double r6 = r64[a * ND + d];
+            rr[d] = (float)r6;
+            r[a * ND + d] = rr[d];
+            v[0] += r6 * r6;
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            float zz = 0.f;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) zz = fmaf(binv[(d * ND + j) * nnodes + a], rr[j], zz);
+            z[a * ND + d] = zz;
+            v[1] += (double)rr[d] * (double)zz;
+            v[2] += (double)rr[d] * (double)p[a * ND + d];
+        }
+    }
+    finish_replace(v, part, count, sc, first, orth, cycle_cap);
+}
+
+// Inverse of every node's ND x ND diagonal block of the FP64 node-block copy
+// (prescribed rows and columns are zero there with a unit diagonal, padding rows
+// hold an identity block), stored FP32 as ND*ND planes binv[e * nrows + a].
+// Cofactor formula in FP64; a singular block reports a zero pivot (done = 3).
+template <int ND>
+__global__ void k_block_inv_sell(int nrows, const int64_t *__restrict__ diag, const double *__restrict__ val,
+                                 float *__restrict__ binv, PcgScal *sc)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nrows) return;
+    const int64_t slot = diag[a];
+    const int r = (int)(slot & 31);
+    const double *vb = val + (slot - r) * (ND * ND) + r;
+    double B[ND][ND], C[ND][ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) B[i][j] = vb[32 * (i * ND + j)];
+    double det;
+    if constexpr (ND == 3) {
+        C[0][0] = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+        C[0][1] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+        C[0][2] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+        C[1][0] = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+        C[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+        C[1][2] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+        C[2][0] = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+        C[2][1] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+        C[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+        det = B[0][0] * C[0][0] + B[0][1] * C[1][0] + B[0][2] * C[2][0];
+    } else {
+        C[0][0] = B[1][1];
+        C[0][1] = -B[0][1];
+        C[1][0] = -B[1][0];
+        C[1][1] = B[0][0];
+        det = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+    }
+    const bool ok = det != 0.0 && isfinite(det);
+    if (!ok) sc->done = 3;
+    const double inv = ok ? 1.0 / det : 0.0;
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) binv[(int64_t)(i * ND + j) * nrows + a] = (float)(C[i][j] * inv);
 }
 
 template <class X, class P = X>
@@ -580,6 +667,33 @@ __global__ void __launch_bounds__(NTHREADS) k_pupdate4(int64_t n, const double *
     for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) p[row] = (P)(zc * z[row] + beta * (double)p[row]);
 }
 
+// Epilogue of the mixed update kernels: block sums of r.r and r.z, and in the
+// last block the convergence / replacement decision and beta.
+__device__ __forceinline__ void finish_update32(double (&v)[2], double *part, unsigned int *count, PcgScal *sc,
+                                                int maxit)
+{
+    block_sum<2>(v);
+    if (publish_partials<2>(v, part, count)) {
+        double t[2];
+        final_sums<2>(part, t);
+        if (threadIdx.x != 0) return;
+        *count = 0;
+        sc->rnorm2 = t[0];
+        sc->iters += 1;
+        if (!isfinite(t[0]) || !isfinite(t[1])) {
+            sc->done = 2;
+        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
+                       sc->iters >= sc->cycle_end) {
+            sc->reliable = 1;
+        } else {
+            sc->beta = t[1] / sc->rho;
+            sc->rho_old = sc->rho;
+            sc->rho = t[1];
+            sc->zcoef = 1.0;
+        }
+    }
+}
+
 // Mixed update with FP32 r, z, dinv, p, q and the FP64 solution x: the FP64
 // arithmetic per row is x += alpha p and a quarter of the dot-product sums.
 // Each block owns one contiguous, equal share of the rows (no tail of partly
@@ -634,26 +748,57 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
         v[0] += (double)(rr * rr);
         v[1] += (double)(rr * zz);
     }
-    block_sum<2>(v);
-    if (publish_partials<2>(v, part, count)) {
-        double t[2];
-        final_sums<2>(part, t);
-        if (threadIdx.x != 0) return;
-        *count = 0;
-        sc->rnorm2 = t[0];
-        sc->iters += 1;
-        if (!isfinite(t[0]) || !isfinite(t[1])) {
-            sc->done = 2;
-        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
-                       sc->iters >= sc->cycle_end) {
-            sc->reliable = 1;
-        } else {
-            sc->beta = t[1] / sc->rho;
-            sc->rho_old = sc->rho;
-            sc->rho = t[1];
-            sc->zcoef = 1.0;
+    finish_update32(v, part, count, sc, maxit);
+}
+
+// Block-Jacobi form of k_update_rz32 (node-space vectors, ND rows per node):
+// z_A = B_A^-1 r_A with the FP32 inverse of node A's ND x ND diagonal block,
+// stored as ND*ND planes binv[e * nnodes + A] (coalesced loads). One node per
+// thread per pass, the block's node range as in k_update_rz32.
+template <int ND>
+__global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double *__restrict__ x,
+                                                          float *__restrict__ r, float *__restrict__ z,
+                                                          const float *__restrict__ p, const float *__restrict__ q,
+                                                          const float *__restrict__ binv, double *part,
+                                                          unsigned int *count, PcgScal *sc, int maxit)
+{
+    if (halted(sc)) return;
+    const double alpha = sc->alpha;
+    const float af = (float)alpha;
+    int64_t lo, hi;
+    block_range(nnodes, lo, hi);
+    double v[2] = {0.0, 0.0};
+#pragma unroll 2
+    for (int64_t a = lo + threadIdx.x; a < hi; a += NTHREADS) {
+        float rr[ND], bb[ND * ND];
+        double xx[ND];
+        float pp[ND];
+#pragma unroll
+        for (int e = 0; e < ND * ND; ++e) bb[e] = binv[e * nnodes + a];
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const int64_t i = a * ND + d;
+            rr[d] = fmaf(-af, q[i], r[i]);
+            xx[d] = x[i];
+            pp[d] = p[i];
         }
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const int64_t i = a * ND + d;
+            float zz = 0.f;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) zz = fmaf(bb[d * ND + j], rr[j], zz);
+            x[i] = xx[d] + alpha * (double)pp[d];
+            r[i] = rr[d];
+            z[i] = zz;
+            s0 = fmaf(rr[d], rr[d], s0);
+            s1 = fmaf(rr[d], zz, s1);
+        }
+        v[0] += (double)s0;
+        v[1] += (double)s1;
     }
+    finish_update32(v, part, count, sc, maxit);
 }
 
 // p = zcoef z + beta p in FP32, same block ranges.
@@ -1589,6 +1734,21 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     OGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(P), s));
     // Jacobi from the FP64 diagonal blocks (the FP32 copy may hold row sums there)
     OGB_CHECK((launch_prec_diag<X, double>(m, op, v64, dinv, sc)));
+    // block Jacobi (FP32 inverses of the node diagonal blocks) in place of the
+    // scalar one for node-block operators with FP32 vectors
+    const bool bj = F32 && ctx->mixed_x64 && ctx->mixed_bj && op.sell && m->precond == 1;
+    const int nd = op.sell ? op.S->nd : 1;
+    const int64_t nnodes = op.n / nd;
+    float *binv = nullptr;
+    if (bj) {
+        OGB_CHECK(m->w_binv32.alloc((size_t)op.n * nd));
+        binv = m->w_binv32.p;
+        const int nrows = (int)nnodes;
+        if (nd == 3) k_block_inv_sell<3><<<nb(nrows), NTHREADS, 0, s>>>(nrows, op.S->diag.p, v64, binv, sc);
+        else k_block_inv_sell<2><<<nb(nrows), NTHREADS, 0, s>>>(nrows, op.S->diag.p, v64, binv, sc);
+        count_launch(ctx);
+    }
+    m->last_bj = bj;
     const bool diff = op.sell && ctx->mixed_diff;
     // the half-stored FP32 copy for large node-block matrices (one warp per slice)
     bool half = false;
@@ -1632,7 +1792,15 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             }
             ctx->prof_sample = true;
             if constexpr (F32) {
-                if (ctx->mixed_x64) {
+                if (bj) {
+                    if (nd == 3)
+                        k_update_bj32<3><<<gb, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
+                                                                 m->w_count.p, sc, maxit);
+                    else
+                        k_update_bj32<2><<<gb, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
+                                                                 m->w_count.p, sc, maxit);
+                    k_pupdate_f32<<<gb, NTHREADS, 0, s>>>(op.n, z, p, sc);
+                } else if (ctx->mixed_x64) {
                     k_update_rz32<<<gb, NTHREADS, 0, s>>>(op.n, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
                                                            maxit);
                     k_pupdate_f32<<<gb, NTHREADS, 0, s>>>(op.n, z, p, sc);
@@ -1654,8 +1822,12 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     IterGraph graph;
     if (ctx->use_graphs) OGB_CHECK(graph.capture(ctx, batch));
     for (;;) {
-        // FP64 residual of the current x64
-        OGB_CHECK((apply_op<double, double, false>(ctx, op, v64, x, q64, nullptr, nullptr, nullptr)));
+        // FP64 residual of the current x64 (not sampled by the kernel timing, which
+        // measures the FP32 operator of the iterations)
+        ctx->prof_sample = false;
+        const int rres = apply_op<double, double, false>(ctx, op, v64, x, q64, nullptr, nullptr, nullptr);
+        ctx->prof_sample = true;
+        OGB_CHECK(rres);
         k_residual64<<<g, NTHREADS, 0, s>>>(nch, b, q64, r64, m->w_part.p, m->w_count.p, m->w_d.p);
         count_launch(ctx);
         double h2[2];
@@ -1688,8 +1860,21 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
         // replacement: r = r64, z = D^-1 r, beta; then p = z + beta p
         // cycle cap: unbounded for the first cycle, then twice the longest cycle so far (at least 512)
         const int cap = first ? (maxit < (1 << 29) ? maxit : (1 << 29)) : (2 * longest > 512 ? 2 * longest : 512);
-        k_mixed_replace<X, P><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
-                                                     first ? 1 : 0, ctx->mixed_orth ? 1 : 0, cap);
+        if constexpr (F32) {
+            if (bj) {
+                if (nd == 3)
+                    k_mixed_replace_bj<3, P><<<g, NTHREADS, 0, s>>>(nnodes, r64, r, z, p, binv, m->w_part.p,
+                                                                     m->w_count.p, sc, first ? 1 : 0,
+                                                                     ctx->mixed_orth ? 1 : 0, cap);
+                else
+                    k_mixed_replace_bj<2, P><<<g, NTHREADS, 0, s>>>(nnodes, r64, r, z, p, binv, m->w_part.p,
+                                                                     m->w_count.p, sc, first ? 1 : 0,
+                                                                     ctx->mixed_orth ? 1 : 0, cap);
+            }
+        }
+        if (!bj)
+            k_mixed_replace<X, P><<<g, NTHREADS, 0, s>>>(nch, r64, r, z, p, dinv, m->w_part.p, m->w_count.p, sc,
+                                                         first ? 1 : 0, ctx->mixed_orth ? 1 : 0, cap);
         k_pcg_pupdate<X, P><<<g, NTHREADS, 0, s>>>(n, z, p, sc);
         count_launch(ctx, 2);
         first = false;

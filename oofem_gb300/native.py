@@ -35,6 +35,7 @@ OPT_MIXED_P32 = 5
 OPT_MIXED_X64 = 6
 OPT_SPMV_VARIANT = 7
 OPT_SPMV_HALF = 8
+OPT_MIXED_BLOCK_JACOBI = 9
 # linear solver types (the reference's lstype numbers)
 LS_DIRECT = 0
 LS_IML = 1
@@ -103,6 +104,7 @@ SIGNATURES = {
     "ogb_model_set_nr_mode": (_i, [_vp, _i]),
     "ogb_mtrx_set_preconditioner": (_i, [_vp, _i]),
     "ogb_mtrx_set_solver": (_i, [_vp, _i]),
+    "ogb_mtrx_mixed_block_jacobi": (_i, [_vp, _pi]),
     "ogb_ldlt_factorize": (_i, [_vp]),
     "ogb_ldlt_bandwidth": (_i, [_vp, _pi]),
     "ogb_ldlt_solve": (_i, [_vp, _vp, _vp]),
@@ -284,6 +286,12 @@ class GpuCsrMtrx:
         x = np.zeros(self.neq)
         _check(self.lib.ogb_ldlt_solve(self.h, _ptr(b), _ptr(x)))
         return x
+
+    def last_block_jacobi(self) -> bool:
+        """Whether the last mixed solve on this matrix used the block-Jacobi preconditioner."""
+        v = C.c_int()
+        _check(self.lib.ogb_mtrx_mixed_block_jacobi(self.h, C.byref(v)))
+        return bool(v.value)
 
     def spmv_forms(self):
         """(FP64 form, FP32 form, warps per slice) of the node-block SpMV."""
