@@ -118,6 +118,8 @@ def apply_options(ctx):
         ctx.set_option(native.OPT_MIXED_X64, ARGS.mixed_x64)
     if ARGS is not None and ARGS.block_jacobi >= 0:
         ctx.set_option(native.OPT_MIXED_BLOCK_JACOBI, ARGS.block_jacobi)
+    if ARGS is not None and ARGS.tangent_tc >= 0:
+        ctx.set_option(native.OPT_TANGENT_TC, ARGS.tangent_tc)
 
 
 def profile_traffic(form: int):
@@ -389,6 +391,8 @@ def run_gpu(args):
     achieved = (sp_bytes / sp_n) / (sp_ms / sp_n * 1e-3) / 1e9 if sp_n else None
     f32_form = A.spmv_forms()[1]
     traffic = profile_traffic(f32_form)
+    nblocks = nnz / (mesh.ndofpn ** 2)
+    full_bytes = nnz * 4 + nblocks * 4 + 2 * 4 * nfree
     info = infos[-1]
     cb = None
     if ws == 1 and not args.no_cpu:
@@ -418,7 +422,14 @@ def run_gpu(args):
                      "peak_kind": peak_kind,
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "spmv_launches_per_step": sp_n / args.steps if sp_n else 0,
-                     "spmv_ms_per_step": sp_ms / args.steps if sp_n else 0},
+                     "spmv_ms_per_step": sp_ms / args.steps if sp_n else 0,
+                     # the same operator applied from the full FP32 node-block copy moves every stored
+                     # block once: values + block columns + x + y (what a plain SpMV of K needs)
+                     "full_copy_bytes": full_bytes,
+                     "effective_frac": (full_bytes / (sp_ms / sp_n * 1e-3) / 1e9 / peak) if sp_n else None,
+                     "effective_frac_note": "bytes of the full-copy SpMV of the same operator / measured time / "
+                                            "peak: the half-stored form applies K at this fraction of the "
+                                            "copy-bound time of a full-copy SpMV; frac counts its own bytes"},
         "elements": elements,
         "clocks": clk,
         "gpu_launches": int(launches),
@@ -577,6 +588,30 @@ def run_gpu_newton(args):
 
     analysis(native.PREC_MIXED)   # warm-up: autotuning, graph capture, allocations
     torch.cuda.synchronize()
+    used_tc = model.tangent_kernel()[0]
+    # element tangent kernels of this state, CUDA events on the library stream
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def tangent_ms(prec, reps=3):
+        model.assemble_tangent(A, prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                model.assemble_tangent(A, prec)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    ms64 = tangent_ms(native.PREC_FP64)
+    ctx.set_option(native.OPT_TANGENT_TC, 1)
+    ms_tc = tangent_ms(native.PREC_MIXED)
+    ctx.set_option(native.OPT_TANGENT_TC, args.tangent_tc if args.tangent_tc >= 0 else 0)
+    tangent = {"assembly_ms_fp64_kernel": ms64, "assembly_ms_tensor_core_kernel": ms_tc,
+               "mixed_steps_used": "tensor cores (split-BF16 tcgen05)" if used_tc else "FP64 CUDA cores",
+               "note": "tangent assembly of the converged state (element kernel + deterministic gather into the "
+                       "CSR and node-block copies), CUDA events; the tensor-core kernel is FP32-accurate and off "
+                       "by default in mixed steps (OGB_OPT_TANGENT_TC)"}
     clocks = ClockSampler(local)
     clocks.start()
     l0 = ctx.kernel_launches()
@@ -612,6 +647,7 @@ def run_gpu_newton(args):
         "fp64": {"value": nfree * nsteps / secs64, "seconds": secs64, "newton_iterations": nites64,
                  "linear_solves": lin64[0], "pcg_iterations": lin64[1]},
         "mixed_over_fp64": secs64 / secs, "clocks": clk, "gpu_launches": int(launches),
+        "tangent": tangent,
         "timing": "host wall clock around the 10-step analysis (device synchronized)",
         "cpu_baseline": cb,
     }
@@ -760,6 +796,9 @@ def main():
     ap.add_argument("--block-jacobi", type=int, default=-1, choices=(-1, 0, 1),
                     help="mixed solves: 1 block-Jacobi, 0 scalar Jacobi preconditioner "
                          "(OGB_OPT_MIXED_BLOCK_JACOBI; -1 = library default)")
+    ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
+                    help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
+                         "(OGB_OPT_TANGENT_TC; -1 = library default)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()

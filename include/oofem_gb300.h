@@ -118,6 +118,17 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   (lsprecond 1) is selected; 0 keeps the scalar diagonal. FP64 solves always
  *   use the reference's scalar DiagPreconditioner. */
 #define OGB_OPT_MIXED_BLOCK_JACOBI 9
+/*   OGB_OPT_TANGENT_TC (0/1/2, default 0): element tangents of mixed-precision
+ *   Newton steps (ogb_nonlinear_step, ogb_batch_nonlinear_step with
+ *   OGB_PREC_MIXED) on the tensor cores: K_e = sum B^T D B dV as split-BF16
+ *   products accumulated in FP32, the upper triangle mirrored (FP32 accuracy);
+ *   0 = FP64 CUDA cores, 1 = tensor cores, 2 = whichever kernel the first such
+ *   assembly of the model timed faster. An FP32-accurate tangent annihilates the
+ *   element rigid-body modes only to about 1e-7 of its entries: on meshes whose
+ *   stiffness spans more than about seven decades that perturbs the tangent
+ *   beyond what the Newton iteration and the CG solve tolerate, hence off by
+ *   default. FP64 steps and LinearStatic always use the FP64 element kernels. */
+#define OGB_OPT_TANGENT_TC 11
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA
@@ -218,7 +229,8 @@ OGB_API int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b_dev, double *x_dev, d
  * that array's device address (do it before any stream capture). All calls
  * share the array: each call clears the parts that must start at zero, and
  * calls that overlap on the GPU race on it. It calls no cudaMalloc, cudaFree
- * or allocating library routine. */
+ * or allocating library routine. The call returns when the solve has finished:
+ * it reads the solver's scalars from the device after every 16 iterations. */
 OGB_API int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr_dev, const int *colind_dev, const double *val_dev,
                                   const double *b_dev, double *x_dev, double rtol, int maxit, void *stream,
                                   ogb_solve_info *info);
@@ -284,6 +296,10 @@ OGB_API int ogb_model_build_matrix(ogb_model *md, ogb_mtrx *m);
  * deterministic gather assembly). Uses the material state of the last stress
  * evaluation (temp values), like TangentAssembler after InternalRhs. */
 OGB_API int ogb_model_assemble_stiffness(ogb_model *md, ogb_mtrx *m);
+/* The tangent a Newton step of the given precision assembles: OGB_PREC_FP64 as
+ * ogb_model_assemble_stiffness; OGB_PREC_MIXED with the element kernel of mixed
+ * steps (split-BF16 tensor cores per OGB_OPT_TANGENT_TC, FP32 accuracy). */
+OGB_API int ogb_model_assemble_tangent(ogb_model *md, ogb_mtrx *m, int precision);
 /* Internal forces f = sum_e sum_gp B^T sigma dV for the total node displacement
  * field u_node (nnodes x ndofpn, prescribed values included); node-indexed
  * output, deterministic. Updates the temp material state. */
@@ -344,6 +360,11 @@ OGB_API int ogb_model_restore_state(ogb_model *md, const void *buf, size_t bytes
 OGB_API int ogb_deck_parse_block(const char *path, int64_t offset, int64_t count, const char *keyword,
                                  const char *field, int maxvals, int64_t *ids, double *vals, int32_t *nvals,
                                  uint8_t *other, int64_t *next_offset, int64_t *lines);
+/* Element tangent kernel of the model's last assembly: *tensor_cores = 1 when it
+ * was the split-BF16 tensor-core kernel (OGB_OPT_TANGENT_TC), and the device
+ * times (ms) of the FP64 and tensor-core kernels measured when the choice was
+ * timed (0 before). Instrumentation, no reference counterpart. */
+OGB_API int ogb_model_tangent_kernel(ogb_model *md, int *tensor_cores, double *ms_fp64, double *ms_tc);
 /* Linear solves of the Newton drivers since the model was created or reset, and
  * their PCG iterations (summed over instances for batched steps). Instrumentation,
  * no reference counterpart. */

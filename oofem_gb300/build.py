@@ -36,7 +36,7 @@ def _stale(target: str, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "internal.cuh"), os.path.join(CSRC, "reduce.cuh"),
+    headers = [os.path.join(CSRC, "internal.cuh"), os.path.join(CSRC, "reduce.cuh"), os.path.join(CSRC, "tcgen05.cuh"),
                os.path.join(os.path.dirname(HERE), "include", "oofem_gb300.h")]
     cc = nvcc()
     jobs = []

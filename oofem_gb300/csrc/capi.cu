@@ -381,6 +381,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->spmv_half = (int)value;
         return OGB_OK;
     case OGB_OPT_MIXED_BLOCK_JACOBI: ctx->mixed_bj = value != 0; return OGB_OK;
+    case OGB_OPT_TANGENT_TC:
+        if (value < 0 || value > 2) return fail(OGB_E_ARG, "tensor-core tangent option must be 0, 1 or 2");
+        ctx->tangent_tc = (int)value;
+        return OGB_OK;
     case OGB_OPT_MIXED_DROP_PPM:
         if (value <= 0 || value >= 1000000) return fail(OGB_E_ARG, "drop factor must be in (0,1)");
         ctx->mixed_drop = value * 1e-6;
@@ -830,13 +834,67 @@ int ogb_model_build_matrix(ogb_model *md, ogb_mtrx *m)
     return OGB_OK;
 }
 
+// Element tangents of a mixed-precision Newton step (md->mixed_tangent) may run
+// on the tensor cores (split BF16, FP32 accuracy) instead of the FP64 CUDA cores:
+// OGB_OPT_TANGENT_TC 1 always, 2 when the first such assembly of the model timed
+// the tensor-core kernel faster (each kernel once after a warm-up launch, CUDA
+// events), 0 (default) never. FP64 solves always use the FP64 kernel.
+static int element_tangents(ogb_model *md)
+{
+    ogb_ctx *ctx = md->ctx;
+    const bool isotropic_hex = md->etype == OGB_LSPACE && !md->nonlinear;   // the cheaper isotropic FP64 form
+    if (!md->mixed_tangent || ctx->tangent_tc == 0 || isotropic_hex) {
+        md->last_tangent_tc = false;
+        return launch_elem_stiffness(md);
+    }
+    if (ctx->tangent_tc == 2 && md->tc_choice == 0) {
+        cudaStream_t s = ctx->stream;
+        cudaEvent_t ev[4];
+        for (auto &e : ev) OGB_CUDA(cudaEventCreate(&e));
+        OGB_CHECK(launch_elem_stiffness(md));
+        OGB_CHECK(launch_elem_stiffness_tc(md));
+        OGB_CUDA(cudaEventRecord(ev[0], s));
+        OGB_CHECK(launch_elem_stiffness(md));
+        OGB_CUDA(cudaEventRecord(ev[1], s));
+        OGB_CHECK(launch_elem_stiffness_tc(md));
+        OGB_CUDA(cudaEventRecord(ev[2], s));
+        OGB_CUDA(cudaEventSynchronize(ev[2]));
+        float t64 = 0.f, ttc = 0.f;
+        OGB_CUDA(cudaEventElapsedTime(&t64, ev[0], ev[1]));
+        OGB_CUDA(cudaEventElapsedTime(&ttc, ev[1], ev[2]));
+        for (auto &e : ev) cudaEventDestroy(e);
+        OGB_CHECK(check_device_status(ctx, "tensor-core element stiffness"));
+        md->tc_ms[0] = t64;
+        md->tc_ms[1] = ttc;
+        md->tc_choice = ttc < t64 ? 1 : 2;
+        md->last_tangent_tc = md->tc_choice == 1;
+        // the last launch was the tensor-core one: its element matrices are current
+        return md->tc_choice == 1 ? OGB_OK : launch_elem_stiffness(md);
+    }
+    const bool tc = ctx->tangent_tc == 1 || md->tc_choice == 1;
+    md->last_tangent_tc = tc;
+    return tc ? launch_elem_stiffness_tc(md) : launch_elem_stiffness(md);
+}
+
 static int assemble_stiffness_async(ogb_model *md, ogb_mtrx *m)
 {
     if (md->bound != m || !m->has_structure)
         return fail(OGB_E_STATE, "matrix was not built from this model (ogb_model_build_matrix)");
-    OGB_CHECK(launch_elem_stiffness(md));
+    OGB_CHECK(element_tangents(md));
     OGB_CHECK(launch_gather_matrix(md, m));
     return OGB_OK;
+}
+
+int ogb_model_assemble_tangent(ogb_model *md, ogb_mtrx *m, int precision)
+{
+    if (!md || !m) return fail(OGB_E_ARG, "null argument");
+    if (precision != OGB_PREC_FP64 && precision != OGB_PREC_MIXED) return fail(OGB_E_ARG, "unknown precision");
+    OGB_CUDA(cudaSetDevice(md->ctx->device));
+    md->mixed_tangent = precision == OGB_PREC_MIXED;
+    const int r = assemble_stiffness_async(md, m);
+    md->mixed_tangent = false;
+    OGB_CHECK(r);
+    return check_device_status(md->ctx, "assemble tangent");
 }
 
 int ogb_model_assemble_stiffness(ogb_model *md, ogb_mtrx *m)
@@ -1038,6 +1096,15 @@ int ogb_model_restore_state(ogb_model *md, const void *buf, size_t bytes)
     return OGB_OK;
 }
 
+int ogb_model_tangent_kernel(ogb_model *md, int *tensor_cores, double *ms_fp64, double *ms_tc)
+{
+    if (!md) return fail(OGB_E_ARG, "null argument");
+    if (tensor_cores) *tensor_cores = md->last_tangent_tc ? 1 : 0;
+    if (ms_fp64) *ms_fp64 = md->tc_ms[0];
+    if (ms_tc) *ms_tc = md->tc_ms[1];
+    return OGB_OK;
+}
+
 int ogb_model_solver_stats(ogb_model *md, int64_t *solves, int64_t *iterations)
 {
     if (!md) return fail(OGB_E_ARG, "null argument");
@@ -1069,8 +1136,11 @@ int ogb_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bcval, cons
     if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
     if (!md->inc.p)
         OGB_CHECK(build_incidence(md->ctx, md->nnodes, md->nelem, md->nnpe, md->conn.p, md->inc_ptr, md->inc));
-    return nonlinear_step(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac, iterations, nullptr,
-                          nr_assemble, nr_forces, nr_solve);
+    md->mixed_tangent = precision == OGB_PREC_MIXED;
+    const int r = nonlinear_step(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac, iterations,
+                                 nullptr, nr_assemble, nr_forces, nr_solve);
+    md->mixed_tangent = false;
+    return r;
 }
 
 int ogb_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf, int maxiter,
@@ -1140,8 +1210,11 @@ int ogb_batch_nonlinear_step_dev(ogb_model *md, ogb_mtrx *m, const double *bcval
     if (md->bound != m) OGB_CHECK(ogb_model_build_matrix(md, m));
     if (!md->inc.p)
         OGB_CHECK(build_incidence(md->ctx, md->nnodes, md->nelem, md->nnpe, md->conn.p, md->inc_ptr, md->inc));
-    return nonlinear_step_batch(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac, iterations,
-                                nr_assemble, nr_forces);
+    md->mixed_tangent = precision == OGB_PREC_MIXED;
+    const int r = nonlinear_step_batch(md, m, bcval, load, rtolf, maxiter, lin_rtol, precision, u_node, reac,
+                                       iterations, nr_assemble, nr_forces);
+    md->mixed_tangent = false;
+    return r;
 }
 
 int ogb_batch_nonlinear_step(ogb_model *md, ogb_mtrx *m, const double *bcval, const double *load, double rtolf,

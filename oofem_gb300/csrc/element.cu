@@ -7,7 +7,10 @@
 // tangents or weighted stresses) in shared memory; phase 2 runs one thread per
 // (element, node a) and produces the a-th block row of the element matrix or
 // vector, so no thread holds more than NPE*ND*ND accumulators.
+#include <cuda_bf16.h>
+
 #include "internal.cuh"
+#include "tcgen05.cuh"
 
 namespace ogb {
 
@@ -803,6 +806,256 @@ static int run_forces(ogb_model *md, const double *u_node)
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
     return OGB_OK;
+}
+
+// ------------------------------------------------------------------ K1 on tensor cores
+// Element stiffness of the mixed-precision tangent on the 5th-generation tensor
+// cores: K_e = G^T H with G[(gp, s)][(a, i)] = B_gp[s][(a, i)] and
+// H[(gp, s)][(b, j)] = dV_gp (D_gp B_gp)[s][(b, j)] (the sum over Gauss points
+// and strain components is the K dimension of one MMA chain,
+// NLStructuralElement::computeStiffnessMatrix nlstructuralelement.C:345-376).
+// EPT elements share one 128 x 128 tile: element le owns rows and columns
+// le*NDOF .. le*NDOF+NDOF-1, and only its diagonal block of the product is read
+// back. Split BF16: each FP32 operand is the sum of three BF16 pieces
+// (v = v0 + v1 + v2, exact to about 2^-24 |v|); the six products v_i w_j with
+// i + j <= 2 are accumulated in FP32 in tensor memory, which gives K_e to FP32
+// accuracy. Per CTA (128 threads, persistent over tiles): gradients, dV and the
+// material tangent per (element, GP) on the CUDA cores; the split operands in
+// shared memory (canonical K-major layout without swizzle); 6 MMAs per 16 of K
+// issued by one thread, completion through an mbarrier (bounded wait: a timeout
+// sets DS_TIMEOUT and the kernel stops); each warp reads its 32 tensor-memory
+// lanes (rows) and writes the element rows in the layout of k_elem_stiffness.
+template <int ET>
+struct TcTile {
+    using T = ET_<ET>;
+    static constexpr int NDOF = T::NPE * T::ND;        // 24 hex, 8 quad, 12 tet
+    static constexpr int KDIM = T::NGP * T::NS;        // 48, 12, 6
+    static constexpr int KP = (KDIM + 15) / 16 * 16;   // K padded to whole MMAs: 48, 16, 16
+    static constexpr int EPT = 128 / NDOF;             // elements per tile: 5, 16, 10
+    static constexpr int PIECE = 128 * KP * 2;         // bytes of one BF16 operand piece (128 rows)
+    static constexpr int OPER = 6 * PIECE;             // A0 A1 A2 (G pieces) B0 B1 B2 (H pieces)
+    static constexpr int NGPT = EPT * T::NGP;          // (element, GP) pairs of a tile
+    static constexpr int GPF = 2 * T::NPE * T::NDIM + 1 + T::NS * T::NS;   // g, gs, dV, D (FP32)
+    static constexpr size_t SMEM = 1024 + OPER + (size_t)NGPT * GPF * 4 + 16;
+};
+
+// Store v as three BF16 pieces at (row, k) of pieces p0, p0+1, p0+2.
+template <int KP>
+__device__ __forceinline__ void store_split3(unsigned char *oper, int piece_bytes, int p0, int row, int k, float v)
+{
+    const int off = ((((row >> 3) * (KP / 8)) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1);
+    const __nv_bfloat16 h0 = __float2bfloat16_rn(v);
+    float rem = v - __bfloat162float(h0);
+    const __nv_bfloat16 h1 = __float2bfloat16_rn(rem);
+    rem -= __bfloat162float(h1);
+    const __nv_bfloat16 h2 = __float2bfloat16_rn(rem);
+    *reinterpret_cast<__nv_bfloat16 *>(oper + (p0 + 0) * piece_bytes + off) = h0;
+    *reinterpret_cast<__nv_bfloat16 *>(oper + (p0 + 1) * piece_bytes + off) = h1;
+    *reinterpret_cast<__nv_bfloat16 *>(oper + (p0 + 2) * piece_bytes + off) = h2;
+}
+
+template <int ET>
+__global__ void __launch_bounds__(128) k_elem_stiffness_tc(
+    int nelem, const double *__restrict__ coords, const int *__restrict__ conn, const int *__restrict__ emat,
+    const double *__restrict__ mats, const double *__restrict__ Dmat, const double *__restrict__ state,
+    double thickness, double *__restrict__ ke, int *status)
+{
+    using T = ET_<ET>;
+    using L = TcTile<ET>;
+    constexpr int NPE = T::NPE, NGP = T::NGP, ND = T::ND, NDIM = T::NDIM, NS = T::NS;
+    extern __shared__ unsigned char tc_smem[];
+    __shared__ int s_ok;
+    const uint32_t raw = tc::smem_u32(tc_smem);
+    unsigned char *oper = tc_smem + (((raw + 1023u) & ~1023u) - raw);
+    float *gpd = reinterpret_cast<float *>(oper + L::OPER);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(gpd + L::NGPT * L::GPF);   // 8-byte aligned: OPER, 4*count even
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // zero the operands: padding rows and K beyond KDIM stay zero for every tile
+    for (int i = tid; i < L::OPER / 16; i += 128) reinterpret_cast<uint4 *>(oper)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) tc::tmem_alloc(slot, 128);
+    if (tid == 0) tc::mbar_init(bar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t abase = tc::smem_u32(oper);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(128, 128);
+    constexpr uint32_t LBO = 128, SBO = (L::KP / 8) * 128;
+    constexpr long long WAIT_CYCLES = 2000000000LL;   // about a second
+    uint32_t phase = 0;
+    bool failed = false;
+    const int ntiles = (nelem + L::EPT - 1) / L::EPT;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int e0 = tile * L::EPT;
+        // (1) gradients, dV and the material tangent of every (element, GP)
+        for (int t = tid; t < L::NGPT; t += 128) {
+            const int le = t / NGP, gp = t % NGP, e = e0 + le;
+            float *q = gpd + t * L::GPF;
+            if (e >= nelem) {
+                for (int i = 0; i < L::GPF; ++i) q[i] = 0.f;
+                continue;
+            }
+            double x[NPE][NDIM], g[NPE][NDIM], gs[NPE][NDIM], dV;
+            gather_xe<ET>(coords, conn, e, x);
+            if (!gp_grad<ET>(x, gp, thickness, g, gs, dV)) atomicCAS(status, DS_OK, DS_NEGVOL);
+            for (int a = 0; a < NPE; ++a)
+                for (int d = 0; d < NDIM; ++d) {
+                    q[a * NDIM + d] = (float)g[a][d];
+                    q[NPE * NDIM + a * NDIM + d] = (float)gs[a][d];
+                }
+            q[2 * NPE * NDIM] = (float)dV;
+            float *Dq = q + 2 * NPE * NDIM + 1;
+            const int m = emat[e];
+            const double *mat = mats + 8 * m;
+            const double *Del = Dmat + 36 * m;
+            const int kind = (int)mat[0];
+            if (kind == OGB_MAT_MISES && state) {
+                double D[6][6];
+                mises_tangent(mat, state + ((size_t)e * NGP + gp) * NSTATE, Del, D);
+                for (int i = 0; i < NS; ++i)
+                    for (int j = 0; j < NS; ++j) Dq[i * NS + j] = (float)D[i][j];
+            } else {
+                double f = 1.0;
+                if (kind == OGB_MAT_IDM1 && state) {
+                    // secant (1 - min(omega, 0.999999)) D (isodamagemodel.C:63-81)
+                    const double om = state[((size_t)e * NGP + gp) * NSTATE + 9];
+                    f = 1.0 - (om < 0.999999 ? om : 0.999999);
+                }
+                for (int i = 0; i < NS; ++i)
+                    for (int j = 0; j < NS; ++j) Dq[i * NS + j] = (float)(f * Del[i * NS + j]);
+            }
+        }
+        __syncthreads();
+        // (2) split operands, one thread per (element, GP, node a): the ND columns
+        // (a, i) of B_gp (sparse: gradients of node a) and of dV D_gp B_gp
+        for (int t = tid; t < L::NGPT * NPE; t += 128) {
+            const int pair = t / NPE, a = t % NPE, le = pair / NGP, gp = pair % NGP;
+            const float *q = gpd + pair * L::GPF;
+            const float *ga = q + a * NDIM, *gsa = q + NPE * NDIM + a * NDIM;
+            const float dv = q[2 * NPE * NDIM];
+            const float *Dq = q + 2 * NPE * NDIM + 1;
+            float Bc[ND][NS];
+            if constexpr (NDIM == 3) {
+                // Voigt xx, yy, zz, yz, zx, xy (structural3delement.C:63-85)
+                const float gx = ga[0], gy = ga[1], gz = ga[2];
+                const float c0[6] = {gx, 0.f, 0.f, 0.f, gz, gy}, c1[6] = {0.f, gy, 0.f, gz, 0.f, gx},
+                            c2[6] = {0.f, 0.f, gz, gy, gx, 0.f};
+                for (int s = 0; s < 6; ++s) {
+                    Bc[0][s] = c0[s];
+                    Bc[1][s] = c1[s];
+                    Bc[2][s] = c2[s];
+                }
+            } else {
+                // xx, yy, xy with the shear row at the element centre (planstrss.C:78-106)
+                Bc[0][0] = ga[0]; Bc[0][1] = 0.f; Bc[0][2] = gsa[1];
+                Bc[1][0] = 0.f; Bc[1][1] = ga[1]; Bc[1][2] = gsa[0];
+            }
+            for (int i = 0; i < ND; ++i) {
+                const int row = le * L::NDOF + a * ND + i;
+                for (int s = 0; s < NS; ++s) {
+                    float h = 0.f;
+                    for (int u = 0; u < NS; ++u) h = fmaf(Dq[s * NS + u], Bc[i][u], h);
+                    const int k = gp * NS + s;
+                    store_split3<L::KP>(oper, L::PIECE, 0, row, k, Bc[i][s]);
+                    store_split3<L::KP>(oper, L::PIECE, 3, row, k, h * dv);
+                }
+            }
+        }
+        tc::fence_smem_async();
+        __syncthreads();
+        // (3) one thread issues the split products: A_i B_j with i + j <= 2
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+            uint32_t acc = 0;
+            for (int ks = 0; ks < L::KP / 16; ++ks)
+                for (int pr = 0; pr < 6; ++pr) {
+                    const uint64_t ad = tc::smem_desc(abase + pa[pr] * L::PIECE + ks * 256, LBO, SBO);
+                    const uint64_t bd = tc::smem_desc(abase + (3 + pb[pr]) * L::PIECE + ks * 256, LBO, SBO);
+                    tc::mma_bf16(tmem, ad, bd, idesc, acc);
+                    acc = 1;
+                }
+            tc::mma_commit(bar);
+            s_ok = tc::mbar_wait_bounded(bar, phase, WAIT_CYCLES) ? 1 : 0;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (!s_ok) {
+            failed = true;
+            if (tid == 0) atomicCAS(status, DS_OK, DS_TIMEOUT);
+            break;
+        }
+        tc::fence_after_sync();
+        // (4) each warp reads its 32 lanes; thread = row rr = (a, i) of element le.
+        // The upper triangle (column >= row) is written to both (rr, c) and (c, rr):
+        // B^T D B is symmetric for these materials, and the split products of an
+        // entry and of its transpose round differently, so the element matrix is
+        // made exactly symmetric as the FP32 operator of the solve assumes (the
+        // reference likewise fills the upper triangle and mirrors it,
+        // plusProductSymmUpper + symmetrized, nlstructuralelement.C:365-376).
+        {
+            const int le = tid / L::NDOF, rr = tid % L::NDOF, e = e0 + le;
+            const bool valid = le < L::EPT && e < nelem;
+            const int a = rr / ND, i = rr % ND;
+            const int lo_e = (32 * warp) / L::NDOF;
+            const int hi_e = min(L::EPT - 1, (32 * warp + 31) / L::NDOF);
+            const int c_lo = (lo_e * L::NDOF) & ~7;
+            const int c_hi = min(128, (hi_e + 1) * L::NDOF);
+            double *eb = valid ? ke + (size_t)e * NPE * NPE * ND * ND : nullptr;
+            for (int c0 = c_lo; c0 < c_hi; c0 += 8) {
+                float v[8];
+                tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+#pragma unroll
+                for (int qq = 0; qq < 8; ++qq) {
+                    const int c = c0 + qq - le * L::NDOF;
+                    if (valid && c >= rr && c < L::NDOF) {
+                        const int b = c / ND, j = c % ND;
+                        const double val = (double)v[qq];
+                        eb[((a * NPE + b) * ND + i) * ND + j] = val;   // (rr, c)
+                        eb[((b * NPE + a) * ND + j) * ND + i] = val;   // (c, rr)
+                    }
+                }
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    // a failed tile's MMAs get one more bounded wait before the tensor memory is freed
+    if (failed && tid == 0) tc::mbar_wait_bounded(bar, phase ^ 1u, WAIT_CYCLES);
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+}
+
+template <int ET>
+static int run_stiffness_tc(ogb_model *md)
+{
+    ogb_ctx *ctx = md->ctx;
+    constexpr size_t smem = TcTile<ET>::SMEM;
+    static bool attr_set[64] = {};
+    OGB_CUDA(set_smem_limit_once((const void *)k_elem_stiffness_tc<ET>, (int)smem, attr_set));
+    const int ntiles = (int)ceil_div(md->nelem, TcTile<ET>::EPT);
+    const int grid = ntiles < num_sms() * 2 ? ntiles : num_sms() * 2;
+    if (grid > 0)
+        k_elem_stiffness_tc<ET><<<grid, 128, smem, ctx->stream>>>(md->nelem, md->coords.p, md->conn.p, md->emat.p,
+                                                                  md->mats.p, md->Dmat.p,
+                                                                  md->nonlinear ? md->state.p : nullptr,
+                                                                  md->thickness, md->ke.p, ctx->status.p);
+    count_launch(ctx);
+    OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+int launch_elem_stiffness_tc(ogb_model *md)
+{
+    switch (md->etype) {
+    case OGB_LSPACE: return run_stiffness_tc<OGB_LSPACE>(md);
+    case OGB_PLANESTRESS2D: return run_stiffness_tc<OGB_PLANESTRESS2D>(md);
+    case OGB_LTRSPACE: return run_stiffness_tc<OGB_LTRSPACE>(md);
+    }
+    return fail(OGB_E_ARG, "unknown element type");
 }
 
 int launch_elem_stiffness(ogb_model *md)

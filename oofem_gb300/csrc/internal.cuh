@@ -232,6 +232,7 @@ struct ogb_ctx {
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner
+    int tangent_tc = 0;         // mixed Newton tangents on tensor cores: 0 never, 1 always, 2 when timed faster
     ogb::DBuf<int> status;           // device status word
     ogb::HBuf<int> h_status;
 };
@@ -319,6 +320,10 @@ struct ogb_model {
     int initial_guess = 0;                 // NonLinearStatic initialGuess: 0 IG_None, 1 IG_Tangent
     int nr_manrm = 1;                      // NRSolver manrmsteps: 0 modified Newton, k re-assembles when nite % k == 0
     int64_t lin_solves = 0, lin_iters = 0;  // linear solves of the Newton drivers and their PCG iterations
+    bool mixed_tangent = false;   // inside a mixed-precision Newton step: tangents may run on tensor cores
+    int tc_choice = 0;            // tensor-core tangent timing: 0 not yet, 1 tensor cores faster, 2 FP64 faster
+    bool last_tangent_tc = false; // the last element tangents came from the tensor-core kernel
+    float tc_ms[2] = {0.f, 0.f};  // timed FP64 and tensor-core element stiffness (ms)
     ogb::DBuf<unsigned int> nr_count;
     ogb::HBuf<double> h_nr_out;
 };
@@ -365,6 +370,8 @@ int refresh_half(ogb_ctx *ctx, SellMat &S);
 
 // element.cu
 int launch_elem_stiffness(ogb_model *md);
+// Split-BF16 tensor-core element stiffness (FP32 accuracy) for mixed-precision tangents.
+int launch_elem_stiffness_tc(ogb_model *md);
 int launch_elem_internal_forces(ogb_model *md, const double *u_node);
 int launch_isotropic_tables(ogb_model *md);
 

@@ -218,6 +218,11 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
     if (halted(sc)) return;
     const int s = blockIdx.x * (NTHREADS / 32) + (threadIdx.x >> 5);
     const int r = threadIdx.x & 31;
+    // node c's ND entries of x
+    auto gather = [&](int c, float (&v)[ND]) {
+#pragma unroll
+        for (int j = 0; j < ND; ++j) v[j] = (float)__ldg(x + (int64_t)c * ND + j);
+    };
     double dot = 0.0;
     if (s < nslices) {
         const int arow = s * 32 + r;
@@ -244,12 +249,12 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
                 }
                 float xb[G][ND];
 #pragma unroll
-                for (int g = 0; g < G; ++g)
+                for (int g = 0; g < G; ++g) {
+                    gather(cc[g], xb[g]);
 #pragma unroll
-                    for (int j = 0; j < ND; ++j) {
-                        xb[g][j] = (float)__ldg(x + (int64_t)cc[g] * ND + j);
+                    for (int j = 0; j < ND; ++j)
                         if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
-                    }
+                }
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
                     if (k0 + g < w) {
@@ -283,11 +288,10 @@ __global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64
                     const int c = e[g] >= 0 ? (e[g] >> 6) : arow;
                     const int kk = e[g] >= 0 ? (e[g] & 63) : 0;
                     vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + (c & 31);
+                    gather(c, xb[g]);
 #pragma unroll
-                    for (int j = 0; j < ND; ++j) {
-                        xb[g][j] = (float)__ldg(x + (int64_t)c * ND + j);
+                    for (int j = 0; j < ND; ++j)
                         if (DIFF) xb[g][j] -= xa[j];
-                    }
                 }
 #pragma unroll
                 for (int g = 0; g < G; ++g) {

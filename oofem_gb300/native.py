@@ -36,6 +36,7 @@ OPT_MIXED_X64 = 6
 OPT_SPMV_VARIANT = 7
 OPT_SPMV_HALF = 8
 OPT_MIXED_BLOCK_JACOBI = 9
+OPT_TANGENT_TC = 11
 # linear solver types (the reference's lstype numbers)
 LS_DIRECT = 0
 LS_IML = 1
@@ -94,6 +95,7 @@ SIGNATURES = {
     "ogb_model_equations": (_i, [_vp, _vp]),
     "ogb_model_build_matrix": (_i, [_vp, _vp]),
     "ogb_model_assemble_stiffness": (_i, [_vp, _vp]),
+    "ogb_model_assemble_tangent": (_i, [_vp, _vp, _i]),
     "ogb_model_internal_forces": (_i, [_vp, _vp, _vp]),
     "ogb_model_internal_forces_dev": (_i, [_vp, _vp, _vp]),
     "ogb_model_gp_stress": (_i, [_vp, _vp, _vp]),
@@ -115,6 +117,7 @@ SIGNATURES = {
     "ogb_model_save_state": (_i, [_vp, _vp, C.c_size_t]),
     "ogb_model_restore_state": (_i, [_vp, _vp, C.c_size_t]),
     "ogb_model_solver_stats": (_i, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "ogb_model_tangent_kernel": (_i, [_vp, _pi, _pd, _pd]),
     "ogb_batch_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_batch_nonlinear_step_dev": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, _vp]),
     "ogb_nonlinear_step": (_i, [_vp, _vp, _vp, _vp, _d, _i, _d, _i, _vp, _vp, C.POINTER(C.c_int)]),
@@ -436,6 +439,10 @@ class GpuModel:
     def build_matrix(self, A: GpuCsrMtrx):
         _check(self.lib.ogb_model_build_matrix(self.h, A.h))
 
+    def assemble_tangent(self, A: GpuCsrMtrx, precision: int = PREC_FP64):
+        """The tangent a Newton step of this precision assembles (mixed: tensor-core element kernel)."""
+        _check(self.lib.ogb_model_assemble_tangent(self.h, A.h, int(precision)))
+
     def assemble_stiffness(self, A: GpuCsrMtrx):
         _check(self.lib.ogb_model_assemble_stiffness(self.h, A.h))
 
@@ -560,6 +567,12 @@ class GpuModel:
         off = self._STATE_HEADER.size
         blob[off:off + 8 * state_len] = st.tobytes()
         self.restore_state(bytes(blob))
+
+    def tangent_kernel(self):
+        """(tensor cores used by the last tangent assembly, timed FP64 ms, timed tensor-core ms)."""
+        k, a, b = C.c_int(), C.c_double(), C.c_double()
+        _check(self.lib.ogb_model_tangent_kernel(self.h, C.byref(k), C.byref(a), C.byref(b)))
+        return bool(k.value), a.value, b.value
 
     def set_nr_mode(self, manrmsteps: int):
         """NRSolver manrmsteps: 0 modified Newton, k > 0 re-assembles the tangent

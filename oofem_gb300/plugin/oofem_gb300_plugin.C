@@ -246,7 +246,11 @@ protected:
     }
 
 public:
-    GpuCsrMtrx() : SparseMtrx() { gb300_check(ogb_mtrx_create(gb300_context(), & m), "ogb_mtrx_create"); }
+    GpuCsrMtrx() : SparseMtrx()
+    {
+        OOFEM_LOG_INFO("GpuCsrMtrx: constructed by the class factory (smtype 11)\n");
+        gb300_check(ogb_mtrx_create(gb300_context(), & m), "ogb_mtrx_create");
+    }
     ~GpuCsrMtrx() override
     {
         dropDeviceElements();
@@ -383,7 +387,25 @@ public:
         return v;
     }
 
-    bool canBeFactorized() const override { return false; }
+    // LDLTFactorization (lstype 0, ldltfact.C:50-63) on this matrix: the device
+    // L D L^T of the upper triangle (as Skyline::factorized, skyline.C:429-491),
+    // kept until the next mutation; backSubstitutionWith solves with it.
+    bool canBeFactorized() const override { return true; }
+    SparseMtrx *factorized() override
+    {
+        gb300_check(ogb_ldlt_factorize(handle() ), "GpuCsrMtrx::factorized");
+        return this;
+    }
+    FloatArray *backSubstitutionWith(FloatArray &y) const override
+    {
+        if ( y.giveSize() != nRows ) {
+            OOFEM_ERROR("GpuCsrMtrx::backSubstitutionWith: size mismatch");
+        }
+        FloatArray x(nRows);
+        gb300_check(ogb_ldlt_solve(handle(), y.givePointer(), x.givePointer() ), "GpuCsrMtrx::backSubstitutionWith");
+        y = x;
+        return & y;
+    }
     SparseMtrxType giveType() const override { return SMT_GpuCsr; }
     bool isAsymmetric() const override { return false; }
     const char *giveClassName() const override { return "GpuCsrMtrx"; }

@@ -372,3 +372,4 @@ def test_block_jacobi_mixed_solve(kind, native_lib, oracle):
     A = native_lib.GpuCsrMtrx(c)
     model.linear_static(A, rtol=1e-10, precision=native_lib.PREC_FP64)
     assert not A.last_block_jacobi()
+
