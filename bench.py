@@ -38,6 +38,8 @@ sys.path.insert(0, ROOT)
 METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
 SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged",
               8: "half-stored: upper blocks streamed, lower blocks applied as transposes"}
+HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers capped for 6 blocks per SM (40)",
+              3: "registers for 2 blocks per SM (128)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -120,11 +122,13 @@ def apply_options(ctx):
         ctx.set_option(native.OPT_MIXED_BLOCK_JACOBI, ARGS.block_jacobi)
     if ARGS is not None and ARGS.tangent_tc >= 0:
         ctx.set_option(native.OPT_TANGENT_TC, ARGS.tangent_tc)
+    if ARGS is not None and ARGS.half_form >= 0:
+        ctx.set_option(native.OPT_HALF_FORM, ARGS.half_form)
 
 
 def profile_traffic(form: int):
     """DRAM bytes per SpMV launch of this form from the committed ncu summary (if any)."""
-    p = os.path.join(ROOT, "profiles", "spmv_half_traffic.json" if form == 8 else "spmv_traffic.json")
+    p = os.path.join(ROOT, "profiles", "spmv_half_traffic.json" if form % 10 == 8 else "spmv_traffic.json")
     if os.path.exists(p):
         try:
             return json.load(open(p))
@@ -414,9 +418,10 @@ def run_gpu(args):
         "mixed_over_fp64": ms64 / ms,
         "mixed_vs_fp64_accuracy": accuracy,
         "preconditioner": "block Jacobi (FP32 3x3 node blocks)" if A.last_block_jacobi() else "Jacobi (diagonal)",
-        "roofline": {"bound": "hbm", "kernel": ("k_half_spmv" if f32_form == 8 else "k_sell_spmv") +
+        "roofline": {"bound": "hbm", "kernel": ("k_half_spmv" if f32_form % 10 == 8 else "k_sell_spmv") +
                      " (node-block SELL-32, FP32 values, difference form, fused p.q; form %s)" %
-                     SPMV_FORMS.get(f32_form, "?"),
+                     (SPMV_FORMS[8] + ", " + HALF_FORMS.get(f32_form // 10, "?") if f32_form % 10 == 8
+                      else SPMV_FORMS.get(f32_form, "?")),
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind,
@@ -799,6 +804,8 @@ def main():
     ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
+    ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
+                    help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()

@@ -118,6 +118,11 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   (lsprecond 1) is selected; 0 keeps the scalar diagonal. FP64 solves always
  *   use the reference's scalar DiagPreconditioner. */
 #define OGB_OPT_MIXED_BLOCK_JACOBI 9
+/*   OGB_OPT_HALF_FORM (0..3, default 0): loop form of the half-stored SpMV: the
+ *   registers per thread bounded for 4 (1), 6 (2) or 2 (3) resident blocks of
+ *   256 threads per SM; 0 = timed once per matrix by the built-in autotuner. The
+ *   forms give bitwise equal results. */
+#define OGB_OPT_HALF_FORM 12
 /*   OGB_OPT_TANGENT_TC (0/1/2, default 0): element tangents of mixed-precision
  *   Newton steps (ogb_nonlinear_step, ogb_batch_nonlinear_step with
  *   OGB_PREC_MIXED) on the tensor cores: K_e = sum B^T D B dV as split-BF16
@@ -187,9 +192,9 @@ OGB_API int ogb_mtrx_set_at(ogb_mtrx *m, int i, int j, double value);
 OGB_API int ogb_mtrx_set_preconditioner(ogb_mtrx *m, int type);
 /* Node-block SpMV forms in use for this matrix (0 = not tuned yet, or no
  * node-block copy): the OGB_OPT_SPMV_VARIANT numbers 1..4 chosen for FP64 and
- * FP32 values, and the warps per slice; fp32_form is 8 when the last mixed solve
- * used the half-stored copy (OGB_OPT_SPMV_HALF). Instrumentation, no reference
- * counterpart. */
+ * FP32 values, and the warps per slice; when the last mixed solve used the
+ * half-stored copy (OGB_OPT_SPMV_HALF) fp32_form is 8 + 10 f, f its loop form
+ * (OGB_OPT_HALF_FORM). Instrumentation, no reference counterpart. */
 OGB_API int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_per_slice);
 /* 1 when the last mixed solve on this matrix preconditioned with the block-Jacobi
  * inverses (OGB_OPT_MIXED_BLOCK_JACOBI), else 0. Instrumentation, no reference

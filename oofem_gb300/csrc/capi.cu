@@ -381,6 +381,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->spmv_half = (int)value;
         return OGB_OK;
     case OGB_OPT_MIXED_BLOCK_JACOBI: ctx->mixed_bj = value != 0; return OGB_OK;
+    case OGB_OPT_HALF_FORM:
+        if (value < 0 || value > 3) return fail(OGB_E_ARG, "half-stored SpMV form must be 0 (timed) or 1..3");
+        ctx->half_form = (int)value;
+        return OGB_OK;
     case OGB_OPT_TANGENT_TC:
         if (value < 0 || value > 2) return fail(OGB_E_ARG, "tensor-core tangent option must be 0, 1 or 2");
         ctx->tangent_tc = (int)value;
@@ -602,7 +606,10 @@ int ogb_mtrx_spmv_forms(ogb_mtrx *m, int *fp64_form, int *fp32_form, int *warps_
     if (!m) return fail(OGB_E_ARG, "null argument");
     const bool sell = m->has_sell;
     if (fp64_form) *fp64_form = sell ? m->sell.group[0] : 0;
-    if (fp32_form) *fp32_form = sell ? (m->last_half ? 8 : m->sell.group[1]) : 0;
+    if (fp32_form)
+        *fp32_form = sell ? (m->last_half ? 8 + 10 * (m->ctx->half_form ? m->ctx->half_form : m->sell.half.form)
+                                          : m->sell.group[1])
+                          : 0;
     if (warps_per_slice) *warps_per_slice = sell ? (m->sell.force_split ? m->sell.force_split
                                                     : (m->sell.nslices < num_sms() * 16 ? 4 : 1)) : 0;
     return OGB_OK;

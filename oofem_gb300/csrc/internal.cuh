@@ -145,10 +145,12 @@ struct HalfSell {
     DBuf<int> low;                    // nslotsL: c << 6 | k (-1: padding)
     DBuf<float> v32;                  // nslotsU * ND*ND
     int64_t version = -1;             // full-copy v32_version these values were taken from
+    int form = 0;                     // SpMV form chosen by the autotuner (0 = not yet)
     void reset()
     {
         ok = tried = false;
         version = -1;
+        form = 0;
     }
 };
 
@@ -229,6 +231,7 @@ struct ogb_ctx {
     bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
     int spmv_group = 0;         // SELL SpMV loop variant forced (1..4) or 0 = tuned per matrix
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
+    int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner

@@ -207,8 +207,12 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // the lower passes of later rows read them a second and last time (evict-first).
 // DIFF: the diagonal slot holds the block row sum and the off-diagonal blocks
 // act on x_c - x_a. The sum order is fixed (upper list, then lower list).
-template <int ND, class X, bool DIFF, int G>
-__global__ void __launch_bounds__(NTHREADS) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
+// MINB: minimum resident blocks of 256 threads per SM asked of the compiler, which
+// bounds the registers per thread (4: 64, the allocation it picks unasked; 6: 40;
+// 2: 128, more loads in flight per warp). The loop and its sum order do not depend
+// on MINB: the forms give bitwise equal results.
+template <int ND, class X, bool DIFF, int G, int MINB = 4>
+__global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
                                                         const float *__restrict__ val, const int64_t *__restrict__ ptrL,
                                                         const int *__restrict__ wL, const int *__restrict__ low,
@@ -1360,22 +1364,76 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
 }
 
 // q = K p through the half-stored FP32 copy, fused p.q (mixed solves).
+// Half-stored SpMV forms: 1 = 4 resident blocks per SM (64 registers), 2 = 6
+// blocks (40 registers), 3 = 2 blocks (128 registers).
+constexpr int HALF_FORMS = 3;
+
+template <int ND, class X, bool DIFF>
+void launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, double *part, unsigned int *count,
+                 PcgScal *sc)
+{
+    const HalfSell &H = S.half;
+    const int grid = (int)ceil_div(S.nslices, NTHREADS / 32);
+#define OGB_HALF_ARGS S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p, H.sl_ptrL.p, H.sl_widthL.p, H.low.p, \
+                      x, y, part, count, sc
+    if (form == 2) k_half_spmv<ND, X, DIFF, 8, 6><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+#undef OGB_HALF_ARGS
+}
+
+// Time the half-stored forms once per matrix (scratch scalars; three launches
+// each after a warm-up launch); a later form must be 2 % faster to be chosen.
+template <class X, bool DIFF>
+int half_autotune(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, unsigned int *count, PcgScal *sc)
+{
+    SellMat &S = const_cast<SellMat &>(*op.S);
+    if (S.half.form) return OGB_OK;
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t e0, e1;
+    OGB_CUDA(cudaEventCreate(&e0));
+    OGB_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_f = 1;
+    for (int f = 1; f <= HALF_FORMS; ++f) {
+        auto launch = [&]() {
+            cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
+            if (S.nd == 3) launch_half<3, X, DIFF>(s, f, S, x, y, part, count, sc);
+            else launch_half<2, X, DIFF>(s, f, S, x, y, part, count, sc);
+        };
+        launch();
+        cudaEventRecord(e0, s);
+        for (int k = 0; k < 3; ++k) launch();
+        cudaEventRecord(e1, s);
+        count_launch(ctx, 4);
+        cudaError_t e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(e, "half-stored SpMV autotune");
+        }
+        if (f == 1 || ms < 0.98f * best) {
+            best = ms;
+            best_f = f;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    S.half.form = best_f;
+    return OGB_OK;
+}
+
 template <class X, bool DIFF>
 int apply_half(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, unsigned int *count, PcgScal *sc)
 {
     const SellMat &S = *op.S;
-    const HalfSell &H = S.half;
-    const int grid = (int)ceil_div(S.nslices, NTHREADS / 32);
+    const int form = ctx->half_form ? ctx->half_form : (S.half.form ? S.half.form : 1);
     cudaStream_t s = ctx->stream;
     prof_begin(ctx);
-    if (S.nd == 3)
-        k_half_spmv<3, X, DIFF, 8><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
-                                                             H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
-                                                             sc);
-    else
-        k_half_spmv<2, X, DIFF, 8><<<grid, NTHREADS, 0, s>>>(S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p,
-                                                             H.sl_ptrL.p, H.sl_widthL.p, H.low.p, x, y, part, count,
-                                                             sc);
+    if (S.nd == 3) launch_half<3, X, DIFF>(s, form, S, x, y, part, count, sc);
+    else launch_half<2, X, DIFF>(s, form, S, x, y, part, count, sc);
     // algorithmic bytes: the upper values (the diagonal blocks and half of the
     // off-diagonal ones) with their block columns, one 4-byte entry per lower
     // block, x once and y once; padding slots not counted
@@ -1769,7 +1827,12 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     }
     m->last_half = half;
     if (half) {
-        // no loop variants to tune
+        if constexpr (sizeof(P) == 4) {
+            if (!ctx->half_form) {
+                if (diff) OGB_CHECK((half_autotune<P, true>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+                else OGB_CHECK((half_autotune<P, false>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc + 1)));
+            }
+        }
     } else if (diff) {
         OGB_CHECK((sell_autotune<float, P, float, true>(ctx, op, v32, p, q, m->w_part.p, m->w_count.p, sc + 1)));
     } else {
