@@ -124,6 +124,8 @@ def apply_options(ctx):
         ctx.set_option(native.OPT_TANGENT_TC, ARGS.tangent_tc)
     if ARGS is not None and ARGS.half_form >= 0:
         ctx.set_option(native.OPT_HALF_FORM, ARGS.half_form)
+    if ARGS is not None and ARGS.update_blocks >= 0:
+        ctx.set_option(native.OPT_UPDATE_BLOCKS, ARGS.update_blocks)
 
 
 def profile_traffic(form: int):
@@ -549,8 +551,6 @@ def run_gpu_batch(args):
         "fp64": {"value": nfree * nrhs / (ms64 * 1e-3), "ms_per_step": ms64, "max_iterations": int(its64.max()),
                  "mean_iterations": float(its64.mean()), "all_converged": bool((st64 == 0).all())},
         "mixed_over_fp64": ms64 / ms,
-        "mixed_vs_fp64_accuracy": accuracy,
-        "preconditioner": "block Jacobi (FP32 3x3 node blocks)" if A.last_block_jacobi() else "Jacobi (diagonal)",
         "clocks": clk, "gpu_launches": int(launches),
         "e2e": {"value": nfree * nrhs / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "seconds": e2e_s},
@@ -774,6 +774,37 @@ def run_spmv_forms(args):
         ctx.close()
 
 
+def run_solvers(args):
+    """Linear solvers of the reference on one cantilever (--nx/--ny/--nz, default
+    60x12x12), FP64: IML CG with lsprecond 1 (diagonal), 4 (incomplete Cholesky),
+    2 (ILU by columns), 0 (none), each to 1e-8, and the direct L D L^T (lstype 0).
+    One warm-up solve, then one timed LinearStatic step per solver (host wall
+    clock, device synchronized); one JSON line per solver."""
+    from oofem_gb300 import meshgen as mg, native
+    nx, ny, nz = args.nx or 60, args.ny or 12, args.nz or 12
+    mesh = mg.hex_cantilever(nx, ny, nz, h=WORKLOAD["h"], jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"])
+    for name, lstype, prec in (("CG + diagonal (lsprecond 1)", 1, 1), ("CG + incomplete Cholesky (lsprecond 4)", 1, 4),
+                               ("CG + ILU by columns (lsprecond 2)", 1, 2), ("CG, no preconditioner (lsprecond 0)", 1, 0),
+                               ("direct L D L^T (lstype 0)", 0, 1)):
+        ctx = native.Context(0)
+        model = native.GpuModel(ctx, mesh)
+        A = native.GpuCsrMtrx(ctx)
+        A.set_solver(native.LS_DIRECT if lstype == 0 else native.LS_IML)
+        A.set_preconditioner(prec)
+        model.linear_static(A, rtol=RTOL, maxit=1000000)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        u, reac, info = model.linear_static(A, rtol=RTOL, maxit=1000000)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        print(json.dumps({"mesh": f"{nx}x{ny}x{nz}", "free_dofs": mesh.nfree, "solver": name, "step_ms": 1e3 * dt,
+                          "iterations": info.iterations, "achieved": info.achieved, "status": info.status}),
+              flush=True)
+        A.close()
+        model.close()
+        ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -786,7 +817,7 @@ def main():
     ap.add_argument("--ny", type=int, default=0)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--workload", default="cantilever",
-                    choices=["cantilever", "rve_batch", "mises_block", "idm1_batch", "spmv_forms"])
+                    choices=["cantilever", "rve_batch", "mises_block", "idm1_batch", "spmv_forms", "solvers"])
     ap.add_argument("--sweep-sizes", default="100x20x20,200x40x40,290x58x58",
                     help="spmv_forms: cantilevers to sweep")
     ap.add_argument("--cube-n", type=int, default=40)
@@ -806,6 +837,7 @@ def main():
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
     ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
+    ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()
@@ -823,6 +855,8 @@ def main():
         run_gpu_idm1_batch(args)
     elif args.workload == "spmv_forms":
         run_spmv_forms(args)
+    elif args.workload == "solvers":
+        run_solvers(args)
     else:
         run_gpu(args)
 

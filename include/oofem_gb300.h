@@ -123,6 +123,10 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   256 threads per SM; 0 = timed once per matrix by the built-in autotuner. The
  *   forms give bitwise equal results. */
 #define OGB_OPT_HALF_FORM 12
+/*   OGB_OPT_UPDATE_BLOCKS (0..8, default 0): blocks per SM of the block-Jacobi
+ *   vector update of mixed solves; 0 = one wave of the kernel's resident blocks
+ *   (its occupancy). */
+#define OGB_OPT_UPDATE_BLOCKS 13
 /*   OGB_OPT_TANGENT_TC (0/1/2, default 0): element tangents of mixed-precision
  *   Newton steps (ogb_nonlinear_step, ogb_batch_nonlinear_step with
  *   OGB_PREC_MIXED) on the tensor cores: K_e = sum B^T D B dV as split-BF16

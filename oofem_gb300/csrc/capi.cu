@@ -381,6 +381,10 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->spmv_half = (int)value;
         return OGB_OK;
     case OGB_OPT_MIXED_BLOCK_JACOBI: ctx->mixed_bj = value != 0; return OGB_OK;
+    case OGB_OPT_UPDATE_BLOCKS:
+        if (value < 0 || value > 8) return fail(OGB_E_ARG, "update blocks per SM must be 0 (default) or 1..8");
+        ctx->upd_bps = (int)value;
+        return OGB_OK;
     case OGB_OPT_HALF_FORM:
         if (value < 0 || value > 3) return fail(OGB_E_ARG, "half-stored SpMV form must be 0 (timed) or 1..3");
         ctx->half_form = (int)value;

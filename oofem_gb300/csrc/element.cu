@@ -25,33 +25,34 @@ template <> struct ET_<OGB_LTRSPACE> { static constexpr int NPE = 4, NGP = 1, ND
 // ------------------------------------------------------------------ gradients
 // FEI3dHexaLin::evaldNdxi / evaldNdx (fei3dhexalin.C:126-205); GP order i-j-k
 // (gaussintegrationrule.C:190-213); dV = |detJ| (structural3delement.C:330-342).
-__device__ void hex_grad(const double (&x)[8][3], int gp, double (&g)[8][3], double &dV)
+template <class R>
+__device__ void hex_grad(const R (&x)[8][3], int gp, R (&g)[8][3], R &dV)
 {
-    double u = c_gp2[gp >> 2], v = c_gp2[(gp >> 1) & 1], w = c_gp2[gp & 1];
-    double dN[8][3] = {
-        {-0.125 * (1. - v) * (1. + w), -0.125 * (1. - u) * (1. + w), 0.125 * (1. - u) * (1. - v)},
-        {-0.125 * (1. + v) * (1. + w), 0.125 * (1. - u) * (1. + w), 0.125 * (1. - u) * (1. + v)},
-        {0.125 * (1. + v) * (1. + w), 0.125 * (1. + u) * (1. + w), 0.125 * (1. + u) * (1. + v)},
-        {0.125 * (1. - v) * (1. + w), -0.125 * (1. + u) * (1. + w), 0.125 * (1. + u) * (1. - v)},
-        {-0.125 * (1. - v) * (1. - w), -0.125 * (1. - u) * (1. - w), -0.125 * (1. - u) * (1. - v)},
-        {-0.125 * (1. + v) * (1. - w), 0.125 * (1. - u) * (1. - w), -0.125 * (1. - u) * (1. + v)},
-        {0.125 * (1. + v) * (1. - w), 0.125 * (1. + u) * (1. - w), -0.125 * (1. + u) * (1. + v)},
-        {0.125 * (1. - v) * (1. - w), -0.125 * (1. + u) * (1. - w), -0.125 * (1. + u) * (1. - v)}};
-    double J[3][3];
+    const R u = (R)c_gp2[gp >> 2], v = (R)c_gp2[(gp >> 1) & 1], w = (R)c_gp2[gp & 1];
+    const R dN[8][3] = {
+        {-R(0.125) * (R(1) - v) * (R(1) + w), -R(0.125) * (R(1) - u) * (R(1) + w), R(0.125) * (R(1) - u) * (R(1) - v)},
+        {-R(0.125) * (R(1) + v) * (R(1) + w), R(0.125) * (R(1) - u) * (R(1) + w), R(0.125) * (R(1) - u) * (R(1) + v)},
+        {R(0.125) * (R(1) + v) * (R(1) + w), R(0.125) * (R(1) + u) * (R(1) + w), R(0.125) * (R(1) + u) * (R(1) + v)},
+        {R(0.125) * (R(1) - v) * (R(1) + w), -R(0.125) * (R(1) + u) * (R(1) + w), R(0.125) * (R(1) + u) * (R(1) - v)},
+        {-R(0.125) * (R(1) - v) * (R(1) - w), -R(0.125) * (R(1) - u) * (R(1) - w), -R(0.125) * (R(1) - u) * (R(1) - v)},
+        {-R(0.125) * (R(1) + v) * (R(1) - w), R(0.125) * (R(1) - u) * (R(1) - w), -R(0.125) * (R(1) - u) * (R(1) + v)},
+        {R(0.125) * (R(1) + v) * (R(1) - w), R(0.125) * (R(1) + u) * (R(1) - w), -R(0.125) * (R(1) + u) * (R(1) + v)},
+        {R(0.125) * (R(1) - v) * (R(1) - w), -R(0.125) * (R(1) + u) * (R(1) - w), -R(0.125) * (R(1) + u) * (R(1) - v)}};
+    R J[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            double s = 0;
+            R s = 0;
 #pragma unroll
             for (int k = 0; k < 8; ++k) s += x[k][i] * dN[k][j];
             J[i][j] = s;
         }
-    double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-    double c01 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
-    double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    double det = J[0][0] * c00 - J[0][1] * c01 + J[0][2] * c02;
-    double Ji[3][3];
+    R c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    R c01 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
+    R c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    R det = J[0][0] * c00 - J[0][1] * c01 + J[0][2] * c02;
+    R Ji[3][3];
     Ji[0][0] = c00 / det;
     Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
     Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
@@ -70,18 +71,20 @@ __device__ void hex_grad(const double (&x)[8][3], int gp, double (&g)[8][3], dou
 }
 
 // FEI2dQuadLin::evaldNdxi / evaldNdx (fei2dquadlin.C:80-104, 345-363).
-__device__ void quad_grad_at(const double (&x)[4][2], double ksi, double eta, double (&g)[4][2], double &det)
+template <class R>
+__device__ void quad_grad_at(const R (&x)[4][2], R ksi, R eta, R (&g)[4][2], R &det)
 {
-    double dn0[4] = {0.25 * (1. + eta), -0.25 * (1. + eta), -0.25 * (1. - eta), 0.25 * (1. - eta)};
-    double dn1[4] = {0.25 * (1. + ksi), 0.25 * (1. - ksi), -0.25 * (1. - ksi), -0.25 * (1. + ksi)};
-    double j00 = 0, j01 = 0, j10 = 0, j11 = 0;
+    const R q = R(0.25), one = R(1);
+    const R dn0[4] = {q * (one + eta), -q * (one + eta), -q * (one - eta), q * (one - eta)};
+    const R dn1[4] = {q * (one + ksi), q * (one - ksi), -q * (one - ksi), -q * (one + ksi)};
+    R j00 = 0, j01 = 0, j10 = 0, j11 = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         j00 += dn0[i] * x[i][0]; j01 += dn0[i] * x[i][1];
         j10 += dn1[i] * x[i][0]; j11 += dn1[i] * x[i][1];
     }
     det = j00 * j11 - j01 * j10;
-    double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
+    const R i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         g[i][0] = i00 * dn0[i] + i01 * dn1[i];
@@ -91,15 +94,16 @@ __device__ void quad_grad_at(const double (&x)[4][2], double ksi, double eta, do
 
 // FEI3dTetLin::evaldNdx closed form (fei3dtetlin.C:115-164); w = 1/6.
 // Returns false for detJ <= 0 ("negative volume" in the reference).
-__device__ bool tet_grad(const double (&x)[4][3], double (&g)[4][3], double &dV)
+template <class R>
+__device__ bool tet_grad(const R (&x)[4][3], R (&g)[4][3], R &dV)
 {
-    double x1 = x[0][0], x2 = x[1][0], x3 = x[2][0], x4 = x[3][0];
-    double y1 = x[0][1], y2 = x[1][1], y3 = x[2][1], y4 = x[3][1];
-    double z1 = x[0][2], z2 = x[1][2], z3 = x[2][2], z4 = x[3][2];
-    double detJ = ((x4 - x1) * (y2 - y1) * (z3 - z1) - (x4 - x1) * (y3 - y1) * (z2 - z1) +
+    const R x1 = x[0][0], x2 = x[1][0], x3 = x[2][0], x4 = x[3][0];
+    const R y1 = x[0][1], y2 = x[1][1], y3 = x[2][1], y4 = x[3][1];
+    const R z1 = x[0][2], z2 = x[1][2], z3 = x[2][2], z4 = x[3][2];
+    const R detJ = ((x4 - x1) * (y2 - y1) * (z3 - z1) - (x4 - x1) * (y3 - y1) * (z2 - z1) +
                    (x3 - x1) * (y4 - y1) * (z2 - z1) - (x2 - x1) * (y4 - y1) * (z3 - z1) +
                    (x2 - x1) * (y3 - y1) * (z4 - z1) - (x3 - x1) * (y2 - y1) * (z4 - z1));
-    double s = 1. / detJ;
+    const R s = R(1) / detJ;
     g[0][0] = -((y3 - y2) * (z4 - z2) - (y4 - y2) * (z3 - z2)) * s;
     g[1][0] = ((y4 - y3) * (z1 - z3) - (y1 - y3) * (z4 - z3)) * s;
     g[2][0] = -((y1 - y4) * (z2 - z4) - (y2 - y4) * (z1 - z4)) * s;
@@ -112,8 +116,8 @@ __device__ bool tet_grad(const double (&x)[4][3], double (&g)[4][3], double &dV)
     g[1][2] = ((x4 - x3) * (y1 - y3) - (x1 - x3) * (y4 - y3)) * s;
     g[2][2] = -((x1 - x4) * (y2 - y4) - (x2 - x4) * (y1 - y4)) * s;
     g[3][2] = ((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)) * s;
-    dV = fabs(detJ) * (1.0 / 6.0);
-    return detJ > 0.0;
+    dV = fabs(detJ) * (R(1) / R(6));
+    return detJ > R(0);
 }
 
 template <int ET>
@@ -131,10 +135,10 @@ __device__ __forceinline__ void gather_xe(const double *coords, const int *conn,
 
 // Gradients of one Gauss point: g (NPE x NDIM), shear-row gradients gs (quad
 // only: element centre, planstrss.h:51 / planstrss.C:98-105), dV.
-template <int ET>
-__device__ __forceinline__ bool gp_grad(const double (&x)[ET_<ET>::NPE][ET_<ET>::NDIM], int gp,
-                                        double thickness, double (&g)[ET_<ET>::NPE][ET_<ET>::NDIM],
-                                        double (&gs)[ET_<ET>::NPE][ET_<ET>::NDIM], double &dV)
+template <int ET, class R = double>
+__device__ __forceinline__ bool gp_grad(const R (&x)[ET_<ET>::NPE][ET_<ET>::NDIM], int gp,
+                                        R thickness, R (&g)[ET_<ET>::NPE][ET_<ET>::NDIM],
+                                        R (&gs)[ET_<ET>::NPE][ET_<ET>::NDIM], R &dV)
 {
     if constexpr (ET == OGB_LSPACE) {
         hex_grad(x, gp, g, dV);
@@ -144,9 +148,9 @@ __device__ __forceinline__ bool gp_grad(const double (&x)[ET_<ET>::NPE][ET_<ET>:
             for (int d = 0; d < 3; ++d) gs[a][d] = g[a][d];
         return true;
     } else if constexpr (ET == OGB_PLANESTRESS2D) {
-        double det, det0;
-        quad_grad_at(x, c_gp2[gp >> 1], c_gp2[gp & 1], g, det);
-        quad_grad_at(x, 0.0, 0.0, gs, det0);
+        R det, det0;
+        quad_grad_at<R>(x, (R)c_gp2[gp >> 1], (R)c_gp2[gp & 1], g, det);
+        quad_grad_at<R>(x, R(0), R(0), gs, det0);
         dV = fabs(det) * thickness;
         return true;
     } else {
@@ -897,15 +901,21 @@ __global__ void __launch_bounds__(128) k_elem_stiffness_tc(
                 for (int i = 0; i < L::GPF; ++i) q[i] = 0.f;
                 continue;
             }
-            double x[NPE][NDIM], g[NPE][NDIM], gs[NPE][NDIM], dV;
+            // FP32 gradients (this tangent is FP32-accurate) from coordinates relative
+            // to the element's first node, which keeps the Jacobian exact to FP32
+            // whatever the distance of the element from the origin
+            double x[NPE][NDIM];
             gather_xe<ET>(coords, conn, e, x);
-            if (!gp_grad<ET>(x, gp, thickness, g, gs, dV)) atomicCAS(status, DS_OK, DS_NEGVOL);
+            float xl[NPE][NDIM], g[NPE][NDIM], gs[NPE][NDIM], dV;
+            for (int a = 0; a < NPE; ++a)
+                for (int d = 0; d < NDIM; ++d) xl[a][d] = (float)(x[a][d] - x[0][d]);
+            if (!gp_grad<ET, float>(xl, gp, (float)thickness, g, gs, dV)) atomicCAS(status, DS_OK, DS_NEGVOL);
             for (int a = 0; a < NPE; ++a)
                 for (int d = 0; d < NDIM; ++d) {
-                    q[a * NDIM + d] = (float)g[a][d];
-                    q[NPE * NDIM + a * NDIM + d] = (float)gs[a][d];
+                    q[a * NDIM + d] = g[a][d];
+                    q[NPE * NDIM + a * NDIM + d] = gs[a][d];
                 }
-            q[2 * NPE * NDIM] = (float)dV;
+            q[2 * NPE * NDIM] = dV;
             float *Dq = q + 2 * NPE * NDIM + 1;
             const int m = emat[e];
             const double *mat = mats + 8 * m;

@@ -232,6 +232,7 @@ struct ogb_ctx {
     int spmv_group = 0;         // SELL SpMV loop variant forced (1..4) or 0 = tuned per matrix
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix
+    int upd_bps = 0;            // blocks per SM of the block-Jacobi update and p update (0 = its occupancy)
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner
@@ -261,7 +262,7 @@ struct ogb_mtrx {
     // solver workspace
     ogb::DBuf<double> w_r, w_z, w_p, w_q, w_dinv, w_x, w_b, w_part, w_d;
     ogb::DBuf<float> w_r32, w_z32, w_p32, w_q32, w_dinv32, w_x32;
-    ogb::DBuf<float> w_binv32;   // block-Jacobi inverses of the node diagonal blocks (ND*ND planes)
+    ogb::DBuf<float> w_binv32;   // block-Jacobi inverses of the node diagonal blocks (upper-triangle planes)
     bool last_bj = false;        // the last mixed solve used the block-Jacobi preconditioner
     ogb::DBuf<ogb::PcgScal> w_scal;
     ogb::HBuf<ogb::PcgScal> h_scal;

@@ -460,6 +460,14 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__res
 }
 
 // Residual replacement: r32 = r64, z = D^-1 r32, beta = r.z / rho (0 at the start).
+// Plane of entry (i, j) of a symmetric ND x ND block stored as its upper
+// triangle, row by row (ND = 3: 00 01 02 11 12 22; ND = 2: 00 01 11).
+template <int ND>
+__host__ __device__ constexpr int sym_plane(int i, int j)
+{
+    return i <= j ? i * ND - i * (i - 1) / 2 + (j - i) : j * ND - j * (j - 1) / 2 + (i - j);
+}
+
 // Epilogue of the replacement kernels: ||r64||^2, r.z, r.p -> rho, beta, the
 // coefficient of z in the next p update and the end of the new cycle.
 __device__ __forceinline__ void finish_replace(double (&v)[3], double *part, unsigned int *count, PcgScal *sc,
@@ -537,7 +545,7 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace_bj(int64_t nnodes, c
         for (int d = 0; d < ND; ++d) {
             float zz = 0.f;
 #pragma unroll
-            for (int j = 0; j < ND; ++j) zz = fmaf(binv[(d * ND + j) * nnodes + a], rr[j], zz);
+            for (int j = 0; j < ND; ++j) zz = fmaf(binv[sym_plane<ND>(d, j) * nnodes + a], rr[j], zz);
             z[a * ND + d] = zz;
             v[1] += (double)rr[d] * (double)zz;
             v[2] += (double)rr[d] * (double)p[a * ND + d];
@@ -548,8 +556,10 @@ __global__ void __launch_bounds__(NTHREADS) k_mixed_replace_bj(int64_t nnodes, c
 
 // Inverse of every node's ND x ND diagonal block of the FP64 node-block copy
 // (prescribed rows and columns are zero there with a unit diagonal, padding rows
-// hold an identity block), stored FP32 as ND*ND planes binv[e * nrows + a].
-// Cofactor formula in FP64; a singular block reports a zero pivot (done = 3).
+// hold an identity block), stored FP32 as the ND(ND+1)/2 planes of its upper
+// triangle, binv[sym_plane(i, j) * nrows + a] (the inverse of a symmetric block
+// is symmetric). Cofactor formula in FP64; a singular block reports a zero pivot
+// (done = 3).
 template <int ND>
 __global__ void k_block_inv_sell(int nrows, const int64_t *__restrict__ diag, const double *__restrict__ val,
                                  float *__restrict__ binv, PcgScal *sc)
@@ -589,7 +599,7 @@ __global__ void k_block_inv_sell(int nrows, const int64_t *__restrict__ diag, co
 #pragma unroll
     for (int i = 0; i < ND; ++i)
 #pragma unroll
-        for (int j = 0; j < ND; ++j) binv[(int64_t)(i * ND + j) * nrows + a] = (float)(C[i][j] * inv);
+        for (int j = i; j < ND; ++j) binv[(int64_t)sym_plane<ND>(i, j) * nrows + a] = (float)(C[i][j] * inv);
 }
 
 template <class X, class P = X>
@@ -761,9 +771,10 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
 
 // Block-Jacobi form of k_update_rz32 (node-space vectors, ND rows per node):
 // z_A = B_A^-1 r_A with the FP32 inverse of node A's ND x ND diagonal block,
-// stored as ND*ND planes binv[e * nnodes + A] (coalesced loads). One node per
-// thread per pass, the block's node range as in k_update_rz32.
-template <int ND>
+// stored as the planes of its upper triangle (coalesced loads). A thread takes
+// UNR nodes of the block's node range per pass (nodes a, a + 256, ...), all their
+// loads issued before the arithmetic; the grid is one wave of resident blocks.
+template <int ND, int UNR = 2>
 __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double *__restrict__ x,
                                                           float *__restrict__ r, float *__restrict__ z,
                                                           const float *__restrict__ p, const float *__restrict__ q,
@@ -771,40 +782,49 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double
                                                           unsigned int *count, PcgScal *sc, int maxit)
 {
     if (halted(sc)) return;
+    constexpr int NSYM = ND * (ND + 1) / 2;
     const double alpha = sc->alpha;
     const float af = (float)alpha;
     int64_t lo, hi;
     block_range(nnodes, lo, hi);
     double v[2] = {0.0, 0.0};
-#pragma unroll 2
-    for (int64_t a = lo + threadIdx.x; a < hi; a += NTHREADS) {
-        float rr[ND], bb[ND * ND];
-        double xx[ND];
-        float pp[ND];
+    for (int64_t a0 = lo + threadIdx.x; a0 < hi; a0 += (int64_t)UNR * NTHREADS) {
+        float rr[UNR][ND], bb[UNR][NSYM], pp[UNR][ND];
+        double xx[UNR][ND];
 #pragma unroll
-        for (int e = 0; e < ND * ND; ++e) bb[e] = binv[e * nnodes + a];
+        for (int u = 0; u < UNR; ++u) {
+            const int64_t a = a0 + (int64_t)u * NTHREADS;
+            if (a >= hi) continue;
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
-            const int64_t i = a * ND + d;
-            rr[d] = fmaf(-af, q[i], r[i]);
-            xx[d] = x[i];
-            pp[d] = p[i];
+            for (int e = 0; e < NSYM; ++e) bb[u][e] = binv[e * nnodes + a];
+#pragma unroll
+            for (int d = 0; d < ND; ++d) {
+                const int64_t i = a * ND + d;
+                rr[u][d] = fmaf(-af, q[i], r[i]);
+                xx[u][d] = x[i];
+                pp[u][d] = p[i];
+            }
         }
-        float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
-            const int64_t i = a * ND + d;
-            float zz = 0.f;
+        for (int u = 0; u < UNR; ++u) {
+            const int64_t a = a0 + (int64_t)u * NTHREADS;
+            if (a >= hi) continue;
+            float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-            for (int j = 0; j < ND; ++j) zz = fmaf(bb[d * ND + j], rr[j], zz);
-            x[i] = xx[d] + alpha * (double)pp[d];
-            r[i] = rr[d];
-            z[i] = zz;
-            s0 = fmaf(rr[d], rr[d], s0);
-            s1 = fmaf(rr[d], zz, s1);
+            for (int d = 0; d < ND; ++d) {
+                const int64_t i = a * ND + d;
+                float zz = 0.f;
+#pragma unroll
+                for (int j = 0; j < ND; ++j) zz = fmaf(bb[u][sym_plane<ND>(d, j)], rr[u][j], zz);
+                x[i] = xx[u][d] + alpha * (double)pp[u][d];
+                r[i] = rr[u][d];
+                z[i] = zz;
+                s0 = fmaf(rr[u][d], rr[u][d], s0);
+                s1 = fmaf(rr[u][d], zz, s1);
+            }
+            v[0] += (double)s0;
+            v[1] += (double)s1;
         }
-        v[0] += (double)s0;
-        v[1] += (double)s1;
     }
     finish_update32(v, part, count, sc, maxit);
 }
@@ -1775,6 +1795,19 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     ogb_ctx *ctx = m->ctx;
     cudaStream_t s = ctx->stream;
     const int nch = op.nchunks(), g = vec_grid(nch), gb = bal_grid(nch);
+    // grid of the block-Jacobi update and p update: one wave of the update kernel's
+    // resident blocks per SM (its occupancy, queried once), or the option's count;
+    // each block takes an equal contiguous share of the nodes
+    int upd_bps = ctx->upd_bps;
+    if (!upd_bps && op.sell) {
+        int occ = 0;
+        const cudaError_t oe = op.S->nd == 3
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update_bj32<3>, NTHREADS, 0)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update_bj32<2>, NTHREADS, 0);
+        if (oe != cudaSuccess) return cuda_fail(oe, "occupancy of the block-Jacobi update");
+        upd_bps = occ < 1 ? 1 : (occ > 8 ? 8 : occ);
+    }
+    const int gu = upd_bps ? (nch < num_sms() * upd_bps ? nch : num_sms() * upd_bps) : gb;
     const int n = (int)op.n;
     constexpr bool F32 = sizeof(X) == 4;
     PcgScal *sc = m->w_scal.p;
@@ -1803,7 +1836,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     const int64_t nnodes = op.n / nd;
     float *binv = nullptr;
     if (bj) {
-        OGB_CHECK(m->w_binv32.alloc((size_t)op.n * nd));
+        OGB_CHECK(m->w_binv32.alloc((size_t)nnodes * (nd * (nd + 1) / 2)));
         binv = m->w_binv32.p;
         const int nrows = (int)nnodes;
         if (nd == 3) k_block_inv_sell<3><<<nb(nrows), NTHREADS, 0, s>>>(nrows, op.S->diag.p, v64, binv, sc);
@@ -1861,12 +1894,12 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             if constexpr (F32) {
                 if (bj) {
                     if (nd == 3)
-                        k_update_bj32<3><<<gb, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
+                        k_update_bj32<3><<<gu, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
                                                                  m->w_count.p, sc, maxit);
                     else
-                        k_update_bj32<2><<<gb, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
+                        k_update_bj32<2><<<gu, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
                                                                  m->w_count.p, sc, maxit);
-                    k_pupdate_f32<<<gb, NTHREADS, 0, s>>>(op.n, z, p, sc);
+                    k_pupdate_f32<<<gu, NTHREADS, 0, s>>>(op.n, z, p, sc);
                 } else if (ctx->mixed_x64) {
                     k_update_rz32<<<gb, NTHREADS, 0, s>>>(op.n, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
                                                            maxit);

@@ -37,6 +37,7 @@ OPT_SPMV_VARIANT = 7
 OPT_SPMV_HALF = 8
 OPT_MIXED_BLOCK_JACOBI = 9
 OPT_HALF_FORM = 12
+OPT_UPDATE_BLOCKS = 13
 OPT_TANGENT_TC = 11
 # linear solver types (the reference's lstype numbers)
 LS_DIRECT = 0
