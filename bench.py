@@ -126,6 +126,8 @@ def apply_options(ctx):
         ctx.set_option(native.OPT_HALF_FORM, ARGS.half_form)
     if ARGS is not None and ARGS.update_blocks >= 0:
         ctx.set_option(native.OPT_UPDATE_BLOCKS, ARGS.update_blocks)
+    if ARGS is not None and ARGS.fused_update >= 0:
+        ctx.set_option(native.OPT_FUSED_UPDATE, ARGS.fused_update)
 
 
 def profile_traffic(form: int):
@@ -777,24 +779,30 @@ def run_spmv_forms(args):
 def run_solvers(args):
     """Linear solvers of the reference on one cantilever (--nx/--ny/--nz, default
     60x12x12), FP64: IML CG with lsprecond 1 (diagonal), 4 (incomplete Cholesky),
-    2 (ILU by columns), 0 (none), each to 1e-8, and the direct L D L^T (lstype 0).
+    2 (ILU by columns), 0 (none), each to 1e-8, the direct L D L^T (lstype 0) and
+    the mixed-precision solve of this library.
     One warm-up solve, then one timed LinearStatic step per solver (host wall
     clock, device synchronized); one JSON line per solver."""
     from oofem_gb300 import meshgen as mg, native
     nx, ny, nz = args.nx or 60, args.ny or 12, args.nz or 12
     mesh = mg.hex_cantilever(nx, ny, nz, h=WORKLOAD["h"], jitter=WORKLOAD["jitter"], seed=WORKLOAD["seed"])
-    for name, lstype, prec in (("CG + diagonal (lsprecond 1)", 1, 1), ("CG + incomplete Cholesky (lsprecond 4)", 1, 4),
-                               ("CG + ILU by columns (lsprecond 2)", 1, 2), ("CG, no preconditioner (lsprecond 0)", 1, 0),
-                               ("direct L D L^T (lstype 0)", 0, 1)):
+    for name, lstype, prec, pr in (("CG + diagonal (lsprecond 1)", 1, 1, native.PREC_FP64),
+                                   ("CG + incomplete Cholesky (lsprecond 4)", 1, 4, native.PREC_FP64),
+                                   ("CG + ILU by columns (lsprecond 2)", 1, 2, native.PREC_FP64),
+                                   ("CG, no preconditioner (lsprecond 0)", 1, 0, native.PREC_FP64),
+                                   ("direct L D L^T (lstype 0)", 0, 1, native.PREC_FP64),
+                                   ("mixed: FP32 block-Jacobi PCG + FP64 residual replacement", 1, 1,
+                                    native.PREC_MIXED)):
         ctx = native.Context(0)
+        apply_options(ctx)
         model = native.GpuModel(ctx, mesh)
         A = native.GpuCsrMtrx(ctx)
         A.set_solver(native.LS_DIRECT if lstype == 0 else native.LS_IML)
         A.set_preconditioner(prec)
-        model.linear_static(A, rtol=RTOL, maxit=1000000)
+        model.linear_static(A, rtol=RTOL, maxit=1000000, precision=pr)
         ctx.synchronize()
         t0 = time.perf_counter()
-        u, reac, info = model.linear_static(A, rtol=RTOL, maxit=1000000)
+        u, reac, info = model.linear_static(A, rtol=RTOL, maxit=1000000, precision=pr)
         ctx.synchronize()
         dt = time.perf_counter() - t0
         print(json.dumps({"mesh": f"{nx}x{ny}x{nz}", "free_dofs": mesh.nfree, "solver": name, "step_ms": 1e3 * dt,
@@ -838,6 +846,9 @@ def main():
     ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
+    ap.add_argument("--fused-update", type=int, default=-1, choices=(-1, 0, 1),
+                    help="block-Jacobi update and p update in one cooperative launch "
+                         "(OGB_OPT_FUSED_UPDATE; -1 = library default)")
     ap.add_argument("--spmv-half", type=int, default=1, choices=(0, 1, 2),
                     help="half-stored FP32 operator in mixed solves (OGB_OPT_SPMV_HALF; 1 = default rule)")
     args = ap.parse_args()

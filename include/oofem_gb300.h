@@ -138,6 +138,12 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   beyond what the Newton iteration and the CG solve tolerate, hence off by
  *   default. FP64 steps and LinearStatic always use the FP64 element kernels. */
 #define OGB_OPT_TANGENT_TC 11
+/*   OGB_OPT_FUSED_UPDATE (0/1, default 0): mixed solves with the block-Jacobi
+ *   preconditioner run the vector update and the p update of an iteration as
+ *   one cooperative launch (z stays in shared memory; the blocks wait for the
+ *   iteration's beta with a bounded wait). Same arithmetic and sum order as the
+ *   two-launch form: bitwise equal iterates. */
+#define OGB_OPT_FUSED_UPDATE 14
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA

@@ -114,7 +114,8 @@ struct PcgScal {
     double tol2;      // (rtol ||b||)^2 (mixed)
     double drop2;     // replacement threshold: ||r||^2 <= drop2 * rmax2 (mixed)
     double zcoef;     // p = zcoef z + beta p (1 except right after a replacement)
-    int done;         // 1 converged, 2 breakdown, 3 zero diagonal, 4 max iterations
+    int done;         // 1 converged, 2 breakdown, 3 zero diagonal, 4 max iterations,
+                      // 5 a device-wide wait of a fused update timed out
     int iters;
     int reliable;     // mixed: an FP64 residual replacement is due
     int cycle_end;    // mixed: iteration count at which the current cycle ends at the latest
@@ -233,6 +234,7 @@ struct ogb_ctx {
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix
     int upd_bps = 0;            // blocks per SM of the block-Jacobi update and p update (0 = its occupancy)
+    bool fused_update = false;  // block-Jacobi update and p update in one cooperative launch
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner
@@ -267,6 +269,7 @@ struct ogb_mtrx {
     ogb::DBuf<ogb::PcgScal> w_scal;
     ogb::HBuf<ogb::PcgScal> h_scal;
     ogb::DBuf<unsigned int> w_count;
+    ogb::DBuf<unsigned int> w_epoch;             // fused update: advanced once per iteration by its last block
     int spmv_tpr = 8;    // threads per row of the CSR SpMV (autotuned)
     // node-block copy used by the solver when the matrix was built from a model
     bool has_sell = false;

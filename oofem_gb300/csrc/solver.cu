@@ -687,29 +687,38 @@ __global__ void __launch_bounds__(NTHREADS) k_pupdate4(int64_t n, const double *
 
 // Epilogue of the mixed update kernels: block sums of r.r and r.z, and in the
 // last block the convergence / replacement decision and beta.
+__device__ __forceinline__ bool publish_after_sum(double (&v)[2], double *part, unsigned int *count)
+{
+    block_sum<2>(v);
+    return publish_partials<2>(v, part, count);
+}
+
+// Run by every thread of the last block; thread 0 writes the scalars.
+__device__ __forceinline__ void finish_update32_last(double *part, unsigned int *count, PcgScal *sc, int maxit)
+{
+    double t[2];
+    final_sums<2>(part, t);
+    if (threadIdx.x != 0) return;
+    *count = 0;
+    sc->rnorm2 = t[0];
+    sc->iters += 1;
+    if (!isfinite(t[0]) || !isfinite(t[1])) {
+        sc->done = 2;
+    } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
+               sc->iters >= sc->cycle_end) {
+        sc->reliable = 1;
+    } else {
+        sc->beta = t[1] / sc->rho;
+        sc->rho_old = sc->rho;
+        sc->rho = t[1];
+        sc->zcoef = 1.0;
+    }
+}
+
 __device__ __forceinline__ void finish_update32(double (&v)[2], double *part, unsigned int *count, PcgScal *sc,
                                                 int maxit)
 {
-    block_sum<2>(v);
-    if (publish_partials<2>(v, part, count)) {
-        double t[2];
-        final_sums<2>(part, t);
-        if (threadIdx.x != 0) return;
-        *count = 0;
-        sc->rnorm2 = t[0];
-        sc->iters += 1;
-        if (!isfinite(t[0]) || !isfinite(t[1])) {
-            sc->done = 2;
-        } else if (t[0] <= sc->drop2 * sc->rmax2 || t[0] <= sc->tol2 || !(t[1] > 0.0) || sc->iters >= maxit ||
-                       sc->iters >= sc->cycle_end) {
-            sc->reliable = 1;
-        } else {
-            sc->beta = t[1] / sc->rho;
-            sc->rho_old = sc->rho;
-            sc->rho = t[1];
-            sc->zcoef = 1.0;
-        }
-    }
+    if (publish_after_sum(v, part, count)) finish_update32_last(part, count, sc, maxit);
 }
 
 // Mixed update with FP32 r, z, dinv, p, q and the FP64 solution x: the FP64
@@ -774,23 +783,39 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
 // stored as the planes of its upper triangle (coalesced loads). A thread takes
 // UNR nodes of the block's node range per pass (nodes a, a + 256, ...), all their
 // loads issued before the arithmetic; the grid is one wave of resident blocks.
-template <int ND, int UNR = 2>
-__global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double *__restrict__ x,
+// XS: the solution accumulator, double (the FP64 solution, x += alpha p) or
+// float (the FP32 increment since the last residual replacement, folded into the
+// FP64 solution by the host loop).
+// FUSE: the p update of the same iteration follows in this kernel. The blocks
+// keep their z in shared memory (zcap nodes; a larger range writes z to memory
+// and reads it back), the last block publishes beta and advances *epoch, and
+// every other block waits for that advance before p = zcoef z + beta p over its
+// own rows. The launch is cooperative (all blocks resident), and the wait is
+// bounded: past about a second the block sets done = 5 and returns.
+constexpr int DONE_WAIT_TIMEOUT = 5;
+
+template <int ND, class XS, bool FUSE, int UNR = 2>
+__global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__restrict__ x,
                                                           float *__restrict__ r, float *__restrict__ z,
-                                                          const float *__restrict__ p, const float *__restrict__ q,
+                                                          float *__restrict__ p, const float *__restrict__ q,
                                                           const float *__restrict__ binv, double *part,
-                                                          unsigned int *count, PcgScal *sc, int maxit)
+                                                          unsigned int *count, unsigned int *epoch, int zcap,
+                                                          PcgScal *sc, int maxit)
 {
+    extern __shared__ float zs[];
     if (halted(sc)) return;
     constexpr int NSYM = ND * (ND + 1) / 2;
+    unsigned int e0 = 0;
+    if (FUSE && threadIdx.x == 0) e0 = *(volatile unsigned int *)epoch;
     const double alpha = sc->alpha;
     const float af = (float)alpha;
     int64_t lo, hi;
     block_range(nnodes, lo, hi);
+    const bool zsm = FUSE && hi - lo <= zcap;
     double v[2] = {0.0, 0.0};
     for (int64_t a0 = lo + threadIdx.x; a0 < hi; a0 += (int64_t)UNR * NTHREADS) {
         float rr[UNR][ND], bb[UNR][NSYM], pp[UNR][ND];
-        double xx[UNR][ND];
+        XS xx[UNR][ND];
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const int64_t a = a0 + (int64_t)u * NTHREADS;
@@ -816,9 +841,11 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double
                 float zz = 0.f;
 #pragma unroll
                 for (int j = 0; j < ND; ++j) zz = fmaf(bb[u][sym_plane<ND>(d, j)], rr[u][j], zz);
-                x[i] = xx[u][d] + alpha * (double)pp[u][d];
+                if constexpr (sizeof(XS) == 8) x[i] = xx[u][d] + alpha * (double)pp[u][d];
+                else x[i] = fmaf(af, pp[u][d], xx[u][d]);
                 r[i] = rr[u][d];
-                z[i] = zz;
+                if (zsm) zs[(a - lo) * ND + d] = zz;
+                else z[i] = zz;
                 s0 = fmaf(rr[u][d], rr[u][d], s0);
                 s1 = fmaf(rr[u][d], zz, s1);
             }
@@ -826,7 +853,34 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, double
             v[1] += (double)s1;
         }
     }
-    finish_update32(v, part, count, sc, maxit);
+    if constexpr (!FUSE) {
+        finish_update32(v, part, count, sc, maxit);
+    } else {
+        if (publish_after_sum(v, part, count)) {
+            finish_update32_last(part, count, sc, maxit);
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(epoch, 1u);
+            }
+        } else if (threadIdx.x == 0) {
+            const long long t0 = clock64();
+            while (*(volatile unsigned int *)epoch == e0) {
+                if (clock64() - t0 > 2000000000LL) {
+                    atomicCAS(&sc->done, 0, DONE_WAIT_TIMEOUT);
+                    break;
+                }
+                __nanosleep(100);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        // this iteration's scalars, from L2 (written by the last block)
+        if (__ldcg(&sc->done) || __ldcg(&sc->reliable)) return;
+        const float beta = (float)__ldcg(&sc->beta), zc = (float)__ldcg(&sc->zcoef);
+        const int64_t r0 = lo * ND, r1 = hi * ND;
+        for (int64_t i = r0 + threadIdx.x; i < r1; i += NTHREADS)
+            p[i] = fmaf(zc, zsm ? zs[i - r0] : __ldcg(z + i), beta * p[i]);
+    }
 }
 
 // p = zcoef z + beta p in FP32, same block ranges.
@@ -839,6 +893,32 @@ __global__ void __launch_bounds__(NTHREADS) k_pupdate_f32(int64_t n, const float
     block_range(n, lo, hi);
 #pragma unroll 4
     for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) p[row] = fmaf(zc, z[row], beta * p[row]);
+}
+
+// The block-Jacobi update of a node size, solution type and form.
+const void *bj_update_fn(int nd, bool x64, bool fuse)
+{
+    if (nd == 3) {
+        if (x64) return fuse ? (const void *)k_update_bj32<3, double, true> : (const void *)k_update_bj32<3, double, false>;
+        return fuse ? (const void *)k_update_bj32<3, float, true> : (const void *)k_update_bj32<3, float, false>;
+    }
+    if (x64) return fuse ? (const void *)k_update_bj32<2, double, true> : (const void *)k_update_bj32<2, double, false>;
+    return fuse ? (const void *)k_update_bj32<2, float, true> : (const void *)k_update_bj32<2, float, false>;
+}
+
+// Launch of bj_update_fn's kernel; xs is the FP64 solution or the FP32 increment
+// (the kernel's solution type). The fused form is a cooperative launch, which
+// fails instead of starting when the grid cannot be resident at once.
+int launch_bj_update(const void *fn, bool coop, int grid, size_t smem, cudaStream_t s, int64_t nnodes, void *xs,
+                     float *r, float *z, float *p, const float *q, const float *binv, double *part,
+                     unsigned int *count, unsigned int *epoch, int zcap, PcgScal *sc, int maxit)
+{
+    void *args[] = {&nnodes, &xs, &r, &z, &p, &q, &binv, &part, &count, &epoch, &zcap, &sc, &maxit};
+    const cudaError_t e = coop ? cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NTHREADS), args, smem, s)
+                               : cudaLaunchKernel(fn, dim3(grid), dim3(NTHREADS), args, smem, s);
+    if (e != cudaSuccess) return cuda_fail(e, coop ? "cooperative launch of the fused block-Jacobi update"
+                                                   : "launch of the block-Jacobi update");
+    return OGB_OK;
 }
 
 // r = b - Ax in FP64, ||r||^2 and ||b||^2 into out2.
@@ -1798,14 +1878,17 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // grid of the block-Jacobi update and p update: one wave of the update kernel's
     // resident blocks per SM (its occupancy, queried once), or the option's count;
     // each block takes an equal contiguous share of the nodes
+    // (the fused form is a cooperative launch: at most its occupancy per SM)
+    const bool fuse = ctx->fused_update && op.sell;
+    const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64, fuse) : nullptr;
     int upd_bps = ctx->upd_bps;
-    if (!upd_bps && op.sell) {
+    if (op.sell) {
         int occ = 0;
-        const cudaError_t oe = op.S->nd == 3
-            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update_bj32<3>, NTHREADS, 0)
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update_bj32<2>, NTHREADS, 0);
+        const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ufn, NTHREADS, 0);
         if (oe != cudaSuccess) return cuda_fail(oe, "occupancy of the block-Jacobi update");
-        upd_bps = occ < 1 ? 1 : (occ > 8 ? 8 : occ);
+        if (occ < 1) occ = 1;
+        if (!upd_bps) upd_bps = occ > 8 ? 8 : occ;
+        if (fuse && upd_bps > occ) upd_bps = occ;
     }
     const int gu = upd_bps ? (nch < num_sms() * upd_bps ? nch : num_sms() * upd_bps) : gb;
     const int n = (int)op.n;
@@ -1831,7 +1914,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     OGB_CHECK((launch_prec_diag<X, double>(m, op, v64, dinv, sc)));
     // block Jacobi (FP32 inverses of the node diagonal blocks) in place of the
     // scalar one for node-block operators with FP32 vectors
-    const bool bj = F32 && ctx->mixed_x64 && ctx->mixed_bj && op.sell && m->precond == 1;
+    const bool bj = F32 && ctx->mixed_bj && op.sell && m->precond == 1;
     const int nd = op.sell ? op.S->nd : 1;
     const int64_t nnodes = op.n / nd;
     float *binv = nullptr;
@@ -1844,6 +1927,27 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
         count_launch(ctx);
     }
     m->last_bj = bj;
+    // fused form: z of the block's nodes in shared memory when they fit in 48 KB
+    // without lowering the resident blocks below the grid
+    int zcap = 0;
+    size_t zbytes = 0;
+    if (bj && fuse) {
+        if (!m->w_epoch.p) {
+            OGB_CHECK(m->w_epoch.alloc(1));
+            OGB_CUDA(cudaMemsetAsync(m->w_epoch.p, 0, sizeof(unsigned int), s));
+        }
+        const int64_t share = (nnodes + gu - 1) / gu;
+        const int64_t per = (share + NTHREADS - 1) / NTHREADS * NTHREADS;
+        const size_t bytes = (size_t)per * nd * sizeof(float);
+        if (bytes <= 48 * 1024) {
+            int occz = 0;
+            OGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occz, ufn, NTHREADS, bytes));
+            if ((int64_t)occz * num_sms() >= gu) {
+                zcap = (int)per;
+                zbytes = bytes;
+            }
+        }
+    }
     const bool diff = op.sell && ctx->mixed_diff;
     // the half-stored FP32 copy for large node-block matrices (one warp per slice)
     bool half = false;
@@ -1893,13 +1997,10 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             ctx->prof_sample = true;
             if constexpr (F32) {
                 if (bj) {
-                    if (nd == 3)
-                        k_update_bj32<3><<<gu, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
-                                                                 m->w_count.p, sc, maxit);
-                    else
-                        k_update_bj32<2><<<gu, NTHREADS, 0, s>>>(nnodes, x, r, z, p, q, binv, m->w_part.p,
-                                                                 m->w_count.p, sc, maxit);
-                    k_pupdate_f32<<<gu, NTHREADS, 0, s>>>(op.n, z, p, sc);
+                    void *xs = ctx->mixed_x64 ? (void *)x : (void *)d;
+                    OGB_CHECK(launch_bj_update(ufn, fuse, gu, zbytes, s, nnodes, xs, r, z, p, q, binv, m->w_part.p,
+                                               m->w_count.p, m->w_epoch.p, zcap, sc, maxit));
+                    if (!fuse) k_pupdate_f32<<<gu, NTHREADS, 0, s>>>(op.n, z, p, sc);
                 } else if (ctx->mixed_x64) {
                     k_update_rz32<<<gb, NTHREADS, 0, s>>>(op.n, x, r, z, p, q, dinv, m->w_part.p, m->w_count.p, sc,
                                                            maxit);
@@ -1914,7 +2015,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
                                                           rtol, maxit);
                 k_pupdate4<P><<<gb, NTHREADS, 0, s>>>(op.n, z, p, sc);
             }
-            count_launch(ctx, 2);
+            count_launch(ctx, bj && fuse ? 1 : 2);
         }
         OGB_CUDA(cudaGetLastError());
         return OGB_OK;
@@ -1986,13 +2087,15 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             if (res.done || res.reliable) break;
             if (ctx->use_graphs) {
                 OGB_CHECK(graph.launch(ctx));
-                count_launch(ctx, 3 * BATCH);
+                count_launch(ctx, (bj && fuse ? 2 : 3) * BATCH);
             } else {
                 OGB_CHECK(batch());
             }
         }
         longest = res.iters - iters > longest ? res.iters - iters : longest;
         iters = res.iters;
+        if (res.done == DONE_WAIT_TIMEOUT)
+            return fail(OGB_E_CUDA, "fused block-Jacobi update: the blocks did not all arrive within the wait limit");
         if (res.done == 3) { status = OGB_E_ZERODIAG; break; }
         if (res.done == 2) {   // FP32 recurrences broke down: finish in FP64
             *stalled = true;

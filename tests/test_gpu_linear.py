@@ -374,6 +374,49 @@ def test_block_jacobi_mixed_solve(kind, native_lib, oracle):
     assert not A.last_block_jacobi()
 
 
+def mixed_solve(native_lib, mesh, rtol, **opts):
+    c = native_lib.Context(0)
+    for k, v in opts.items():
+        c.set_option(getattr(native_lib, "OPT_" + k.upper()), v)
+    model = native_lib.GpuModel(c, mesh)
+    A = native_lib.GpuCsrMtrx(c)
+    u, reac, info = model.linear_static(A, rtol=rtol, precision=native_lib.PREC_MIXED)
+    assert info.status == 0 and info.achieved <= rtol, (opts, info.status, info.achieved)
+    assert A.last_block_jacobi()
+    return info.iterations, u, c.kernel_launches()
+
+
+@pytest.mark.parametrize("kind", ["hex", "quad", "tet"])
+def test_fused_update_and_fp32_increment(kind, native_lib, oracle):
+    """The block-Jacobi update with the p update in the same cooperative launch
+    gives bitwise the iterates of the two-launch form (same sums, same order) in
+    one launch fewer per iteration; with the solution accumulated as an FP32
+    increment folded into the FP64 solution at each residual replacement the
+    solve still converges on the FP64 residual to the oracle's solution."""
+    from oofem_gb300 import meshgen as mg
+    mesh = {"hex": lambda: mg.hex_cantilever(30, 6, 6, jitter=0.2, seed=4),
+            "quad": lambda: mg.quad_rve(40, seed=6),
+            "tet": lambda: mg.tet_cube_linear(8, jitter=0.1, seed=2)}[kind]()
+    ref = oracle.linear_static(oracle.mesh_dict(mesh), rtol=1e-13)
+    for x64 in (1, 0):
+        it0, u0, l0 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=0)
+        it1, u1, l1 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=1)
+        assert it0 == it1 and np.array_equal(u0, u1), (x64, it0, it1)
+        assert l1 < l0
+        assert rel(u1, ref["u"]) < 1e-7, (x64, rel(u1, ref["u"]))
+
+
+def test_fused_update_with_z_in_memory(native_lib):
+    """A block range too long for shared memory (one block per SM on 741k active
+    nodes: 4,875 nodes of z, 60 KB on 152 SMs) keeps z in memory in the fused
+    form: still bitwise the two-launch form."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(150, 60, 80, jitter=0.2, seed=1)
+    a = mixed_solve(native_lib, mesh, 1e-6, update_blocks=1, fused_update=0)
+    b = mixed_solve(native_lib, mesh, 1e-6, update_blocks=1, fused_update=1)
+    assert a[0] == b[0] and np.array_equal(a[1], b[1])
+
+
 
 def test_half_stored_forms_are_bitwise_equal(native_lib):
     """The loop forms of the half-stored SpMV (registers bounded for 4, 6 or 2
