@@ -240,12 +240,12 @@ OGB_API int ogb_pcg_solve_dev(ogb_mtrx *m, const double *b_dev, double *x_dev, d
  * Same semantics and status codes as ogb_pcg_solve with OGB_PREC_FP64.
  * Limit: n <= 131072 equations (OGB_E_LIMIT beyond). The work vectors live in
  * one file-scope device array of about 5.2 MB that every GPU which loads the
- * library holds until the process exits; the first call on a device looks up
- * that array's device address (do it before any stream capture). All calls
- * share the array: each call clears the parts that must start at zero, and
- * calls that overlap on the GPU race on it. It calls no cudaMalloc, cudaFree
- * or allocating library routine. The call returns when the solve has finished:
- * it reads the solver's scalars from the device after every 16 iterations. */
+ * library holds until the process exits. All calls share the array: each call
+ * clears the parts that must start at zero, and calls that overlap on the GPU
+ * race on it. It calls no cudaMalloc, cudaFree or allocating library routine.
+ * The call is synchronous -- it reads the solver's scalars from the device
+ * after every 16 iterations and returns when the solve has finished -- so it
+ * cannot be captured into a CUDA graph. */
 OGB_API int ogb_pcg_solve_noalloc(int n, const int64_t *rowptr_dev, const int *colind_dev, const double *val_dev,
                                   const double *b_dev, double *x_dev, double rtol, int maxit, void *stream,
                                   ogb_solve_info *info);

@@ -2452,24 +2452,15 @@ __global__ void __launch_bounds__(NTHREADS) k_na_pupdate(int n, double *scratch)
         w.p[i] = w.z[i] + beta * w.p[i];
 }
 
-// Device address of g_noalloc_scratch, looked up once per device (with that
-// device current) because in host code the symbol's name is only a host-side
-// stand-in, not a device address.
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
-
+// Device address of g_noalloc_scratch on the current device, looked up on every
+// call (cheap; in host code the symbol's name is only a host-side stand-in, and
+// a cached address would go stale after a device reset).
 int noalloc_scratch(double **out)
 {
-    int dev = 0;
-    OGB_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(OGB_E_LIMIT, "device index beyond the supported range");
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_ptr[dev] = static_cast<double *>(p);
-    }
-    *out = g_noalloc_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *out = static_cast<double *>(p);
     return OGB_OK;
 }
 
