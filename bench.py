@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
 SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged",
               8: "half-stored: upper blocks streamed, lower blocks applied as transposes"}
-HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers capped for 6 blocks per SM (40)",
+HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers for 3 blocks per SM (80)",
               3: "registers for 2 blocks per SM (128)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8

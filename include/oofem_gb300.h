@@ -119,7 +119,7 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   use the reference's scalar DiagPreconditioner. */
 #define OGB_OPT_MIXED_BLOCK_JACOBI 9
 /*   OGB_OPT_HALF_FORM (0..3, default 0): loop form of the half-stored SpMV: the
- *   registers per thread bounded for 4 (1), 6 (2) or 2 (3) resident blocks of
+ *   registers per thread bounded for 4 (1), 3 (2) or 2 (3) resident blocks of
  *   256 threads per SM; 0 = timed once per matrix by the built-in autotuner. The
  *   forms give bitwise equal results. */
 #define OGB_OPT_HALF_FORM 12

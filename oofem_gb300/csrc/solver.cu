@@ -197,20 +197,37 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
     }
 }
 
+// Block of lane l from a group of the half copy's values (layout half_vidx):
+// two 16-byte loads and one 4-byte load for ND = 3, one 16-byte load for ND = 2.
+// STREAM: evict-first loads (the block's last use), else L2-only loads.
+template <int ND, bool STREAM>
+__device__ __forceinline__ void half_block(const float *grp, int l, float (&v)[ND * ND])
+{
+    const float4 *g4 = reinterpret_cast<const float4 *>(grp);
+    const float4 a = STREAM ? __ldcs(g4 + l) : __ldcg(g4 + l);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    if constexpr (ND == 3) {
+        const float4 b = STREAM ? __ldcs(g4 + 32 + l) : __ldcg(g4 + 32 + l);
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        v[8] = STREAM ? __ldcs(grp + 256 + l) : __ldcg(grp + 256 + l);
+    }
+}
+
 // q = K p from the half-stored FP32 copy (halfsell.cu), fused p.q and alpha.
 // Upper pass: the row's diagonal block and its blocks of columns b > a, streamed
 // like k_sell_spmv (block columns prefetched G ahead). Lower pass: for every
 // column c < a, the block K_ca that row c stored (slot ptrU[c / 32] + 32 k +
 // c % 32 of its upper list, the entry packing c << 6 | k) applied transposed,
-// K_ac = K_ca^T; the entries are prefetched G ahead.
+// K_ac = K_ca^T; the entries are prefetched G ahead. Each block is read as
+// 16-byte vectors (half_block: 3 loads per lane for a 3 x 3 block, not 9).
 // The upper values bypass L1 (no reuse within the block) and stay in L2, where
 // the lower passes of later rows read them a second and last time (evict-first).
 // DIFF: the diagonal slot holds the block row sum and the off-diagonal blocks
 // act on x_c - x_a. The sum order is fixed (upper list, then lower list).
 // MINB: minimum resident blocks of 256 threads per SM asked of the compiler, which
-// bounds the registers per thread (4: 64, the allocation it picks unasked; 6: 40;
-// 2: 128, more loads in flight per warp). The loop and its sum order do not depend
-// on MINB: the forms give bitwise equal results.
+// bounds the registers per thread (4: 64; 3: 80; 2: 128, more loads in flight per
+// warp). The loop and its sum order do not depend on MINB: the forms give
+// bitwise equal results.
 template <int ND, class X, bool DIFF, int G, int MINB = 4>
 __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
@@ -239,7 +256,7 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
         {   // upper pass
             const int64_t base = ptrU[s];
             const int w = wU[s];
-            const float *vp = val + base * (ND * ND) + r;
+            const float *vp = val + base * (ND * ND);
             const int *cp = colU + base + r;
             int cn[G];
 #pragma unroll
@@ -262,11 +279,12 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
                     if (k0 + g < w) {
-                        const float *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+                        float v[ND * ND];
+                        half_block<ND, false>(vp + (int64_t)(k0 + g) * (32 * ND * ND), r, v);
 #pragma unroll
                         for (int i = 0; i < ND; ++i)
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldcg(vk + 32 * (i * ND + j)) * xb[g][j];
+                            for (int j = 0; j < ND; ++j) yy[i] += v[i * ND + j] * xb[g][j];
                     }
                 }
             }
@@ -291,7 +309,7 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                 for (int g = 0; g < G; ++g) {
                     const int c = e[g] >= 0 ? (e[g] >> 6) : arow;
                     const int kk = e[g] >= 0 ? (e[g] & 63) : 0;
-                    vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + (c & 31);
+                    vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND);
                     gather(c, xb[g]);
 #pragma unroll
                     for (int j = 0; j < ND; ++j)
@@ -300,10 +318,12 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
                     if (e[g] >= 0) {
+                        float v[ND * ND];
+                        half_block<ND, true>(vk[g], (e[g] >> 6) & 31, v);   // lane c % 32 of row c
 #pragma unroll
                         for (int i = 0; i < ND; ++i)
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldcs(vk[g] + 32 * (j * ND + i)) * xb[g][j];
+                            for (int j = 0; j < ND; ++j) yy[i] += v[j * ND + i] * xb[g][j];
                     }
                 }
             }
@@ -1476,7 +1496,7 @@ void launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, d
     const int grid = (int)ceil_div(S.nslices, NTHREADS / 32);
 #define OGB_HALF_ARGS S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p, H.sl_ptrL.p, H.sl_widthL.p, H.low.p, \
                       x, y, part, count, sc
-    if (form == 2) k_half_spmv<ND, X, DIFF, 8, 6><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    if (form == 2) k_half_spmv<ND, X, DIFF, 8, 3><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
