@@ -14,9 +14,10 @@
 // What is GB300-native: the factor lives in a dense band of n x (bw+1) doubles
 // in HBM, column-major (column j holds L(j..j+bw, j), its diagonal slot holds
 // d_j), and is computed right-looking in panels of 32 columns -- one CTA
-// factors a panel (32 dependent steps, each a parallel rank-1 update of the
-// panel), then a 2-D grid of 32 x 32 tiles applies the panel's rank-32 update
-// to the trailing band (shared-memory staged, FP64 FMAs). The solves run in one
+// factors the panel's 32 x 32 diagonal block in shared memory, one thread per
+// row below it solves that row against the block (L21 = A21 L11^-T D^-1), then
+// a 2-D grid of 32 x 32 tiles applies the panel's rank-32 update to the trailing
+// band (shared-memory staged, FP64 FMAs). The solves run in one
 // CTA in blocks of 32 equations: one warp resolves the 32 x 32 triangle with
 // shuffles, the other warps apply the block to the rows below (forward) or
 // reduce the rows below into the block (backward). Every sum has a fixed order,
@@ -65,34 +66,79 @@ __global__ void k_ldl_fill(int n, int bw, const int64_t *__restrict__ rowptr, co
     }
 }
 
-// Factor panel columns [k0, k1): for each column j in order, d_j = A(j,j);
-// the columns j+1 .. k1-1 of the panel receive the rank-1 update
-// A(j+r, j+s) -= A(j+r, j) * (A(j+s, j) / d_j), then column j is scaled to
-// L(j+r, j) = A(j+r, j) / d_j. A zero or non-finite pivot sets *status to
-// the 1-based equation and stops this and every later launch.
-__global__ void __launch_bounds__(PANEL_THREADS) k_ldl_panel(int n, int bw, double *__restrict__ band, int k0, int k1,
-                                                             int *status)
+// Diagonal block of panel [k0, k1) (P = k1 - k0 <= 32 columns): its lower
+// triangle is loaded into shared memory (thread (r, s) of a 32 x 32 CTA owns
+// entry (r, s)) and factored in place, column by column: d_j = A(j,j), the
+// columns s > j receive A(r, s) -= l_rj A(s, j) (A(s, j) not yet scaled), then
+// column j is scaled to l_rj = A(r, j) / d_j. L11 and D go back to the band. A
+// zero or non-finite pivot sets *status to the 1-based equation and stops this
+// and every later launch.
+__global__ void __launch_bounds__(PANEL_THREADS) k_ldl_diag(int n, int bw, double *__restrict__ band, int k0, int k1,
+                                                            int *status)
 {
     if (*status) return;
+    __shared__ double A[PANEL][PANEL + 1];
+    __shared__ double lj[PANEL];
     const int64_t ld = (int64_t)bw + 1;
-    for (int j = k0; j < k1; ++j) {
-        double *cj = band + (int64_t)j * ld;
-        const double d = cj[0];
+    const int P = k1 - k0;
+    const int r = threadIdx.x >> 5, c = threadIdx.x & 31;
+    const bool own = r < P && c <= r && r - c <= bw;
+    A[r][c] = own ? band[(int64_t)(k0 + c) * ld + (r - c)] : 0.0;
+    __syncthreads();
+    for (int j = 0; j < P; ++j) {
+        const double d = A[j][j];
         if (!(d != 0.0) || !isfinite(d)) {
-            if (threadIdx.x == 0) *status = j + 1;
+            if (threadIdx.x == 0) *status = k0 + j + 1;
             return;   // every thread read the same d: a uniform exit
         }
-        const int rmax = min(bw, n - 1 - j);        // rows j+1 .. j+rmax of column j
-        const int smax = min(k1 - 1 - j, rmax);     // panel columns j+1 .. j+smax
-        const int64_t work = (int64_t)smax * rmax;
-        for (int64_t t = threadIdx.x; t < work; t += blockDim.x) {
-            const int s = 1 + (int)(t / rmax), r = 1 + (int)(t % rmax);
-            if (r < s) continue;
-            band[(int64_t)(j + s) * ld + (r - s)] -= cj[r] * (cj[s] / d);
-        }
+        if (c == j && r > j && r < P) lj[r] = A[r][j] / d;
         __syncthreads();
-        for (int r = 1 + threadIdx.x; r <= rmax; r += blockDim.x) cj[r] = cj[r] / d;
+        if (c > j && r >= c && r < P) A[r][c] -= lj[r] * A[c][j];
         __syncthreads();
+        if (c == j && r > j && r < P) A[r][j] = lj[r];
+        __syncthreads();
+    }
+    if (own) band[(int64_t)(k0 + c) * ld + (r - c)] = A[r][c];
+}
+
+// Rows below the diagonal block, one thread per row i in [k1, min(n, k1 + bw)):
+// y = a L11^-T by forward substitution over the panel columns in order
+// (y_j = a_j - sum_{p<j} y_p l_jp), then L(i, j) = y_j / d_j. Entries outside
+// the band (i - j > bw) are zero and stay unwritten.
+__global__ void __launch_bounds__(NTHREADS) k_ldl_subpanel(int n, int bw, double *__restrict__ band, int k0, int k1,
+                                                           const int *status)
+{
+    if (*status) return;
+    __shared__ double L[PANEL][PANEL + 1];
+    __shared__ double dd[PANEL];
+    const int64_t ld = (int64_t)bw + 1;
+    const int P = k1 - k0;
+    for (int t = threadIdx.x; t < PANEL * PANEL; t += blockDim.x) {
+        const int r = t >> 5, c = t & 31;
+        L[r][c] = (r < P && c < r && r - c <= bw) ? band[(int64_t)(k0 + c) * ld + (r - c)] : 0.0;
+        if (r == c) dd[r] = r < P ? band[(int64_t)(k0 + r) * ld] : 1.0;
+    }
+    __syncthreads();
+    const int64_t i = (int64_t)k1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t e = min((int64_t)n, (int64_t)k1 + bw);
+    if (i >= e) return;
+    double y[PANEL];
+#pragma unroll
+    for (int j = 0; j < PANEL; ++j) {
+        const int64_t off = i - (k0 + j);
+        y[j] = (j < P && off <= bw) ? band[(int64_t)(k0 + j) * ld + off] : 0.0;
+    }
+#pragma unroll
+    for (int j = 1; j < PANEL; ++j) {
+        double s = y[j];
+#pragma unroll
+        for (int p = 0; p < j; ++p) s -= y[p] * L[j][p];
+        y[j] = s;
+    }
+#pragma unroll
+    for (int j = 0; j < PANEL; ++j) {
+        const int64_t off = i - (k0 + j);
+        if (j < P && off <= bw) band[(int64_t)(k0 + j) * ld + off] = y[j] / dd[j];
     }
 }
 
@@ -263,13 +309,14 @@ int ldl_factor(ogb_mtrx *m)
         int *st = F.d_int.p + 1;
         for (int k0 = 0; k0 < n; k0 += PANEL) {
             const int k1 = k0 + PANEL < n ? k0 + PANEL : n;
-            k_ldl_panel<<<1, PANEL_THREADS, 0, s>>>(n, bw, F.band.p, k0, k1, st);
+            k_ldl_diag<<<1, PANEL_THREADS, 0, s>>>(n, bw, F.band.p, k0, k1, st);
             count_launch(ctx);
             const int e = (int)std::min<int64_t>((int64_t)n, (int64_t)k1 + bw);
             if (e > k1) {
+                k_ldl_subpanel<<<(unsigned)ceil_div(e - k1, NTHREADS), NTHREADS, 0, s>>>(n, bw, F.band.p, k0, k1, st);
                 const unsigned nt = (unsigned)ceil_div(e - k1, 32);
                 k_ldl_trailing<<<dim3(nt, nt), NTHREADS, 0, s>>>(n, bw, F.band.p, k0, k1, st);
-                count_launch(ctx);
+                count_launch(ctx, 2);
             }
         }
         OGB_CUDA(cudaGetLastError());

@@ -105,8 +105,7 @@ __global__ void k_half_fill(int nrows, const int64_t *__restrict__ sl_ptr, const
     for (; l < endL; l += 32) low[l] = -1;
 }
 
-// Upper values from the full FP32 copy (same lane: both slots belong to row a),
-// written in the half copy's vector layout (half_vidx).
+// Upper values from the full FP32 copy (same lane: both slots belong to row a).
 template <int ND>
 __global__ void k_half_values(int64_t nslots, const int64_t *__restrict__ srcU, const float *__restrict__ full,
                               float *__restrict__ half)
@@ -115,15 +114,15 @@ __global__ void k_half_values(int64_t nslots, const int64_t *__restrict__ srcU, 
     if (t >= nslots) return;
     const int r = (int)(t & 31);
     const int64_t src = srcU[t];
-    float *out = half + (t - r) * (ND * ND);
+    float *out = half + (t - r) * (ND * ND) + r;
     if (src < 0) {
 #pragma unroll
-        for (int e = 0; e < ND * ND; ++e) out[half_vidx<ND>(r, e)] = 0.f;
+        for (int e = 0; e < ND * ND; ++e) out[32 * e] = 0.f;
         return;
     }
     const float *in = full + (src - r) * (ND * ND) + r;
 #pragma unroll
-    for (int e = 0; e < ND * ND; ++e) out[half_vidx<ND>(r, e)] = in[32 * e];
+    for (int e = 0; e < ND * ND; ++e) out[32 * e] = in[32 * e];
 }
 
 }  // namespace

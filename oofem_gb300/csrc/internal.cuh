@@ -133,17 +133,8 @@ struct PcgScal {
 // the block K_ca stored there. The upper values stream from HBM once; the
 // transposed reads come back to the same blocks shortly after (on structured
 // meshes a warp's lanes read neighbouring blocks together) and hit L2. Slots
-// are laid out as in the full copy, slot = sl_ptr[s] + 32 k + r; the values of
-// a group of 32 slots (one k of a slice) start at (slot - r) * ND*ND and hold
-// each lane's block as 16-byte vectors (half_vidx): ND = 3, entries 0-3 of the
-// 32 lanes, then entries 4-7, then entry 8 (three loads per lane and block);
-// ND = 2, entries 0-3 (one load).
-template <int ND>
-__host__ __device__ constexpr int half_vidx(int lane, int e)
-{
-    return ND == 2 ? 4 * lane + e : (e < 4 ? 4 * lane + e : (e < 8 ? 128 + 4 * lane + (e - 4) : 256 + lane));
-}
-
+// are laid out as in the full copy: slot = sl_ptr[s] + 32 k + r, values at
+// (slot - r) * ND*ND + 32 e + r.
 struct HalfSell {
     bool ok = false;
     bool tried = false;          // built or found unsuitable for this structure
