@@ -118,11 +118,10 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   (lsprecond 1) is selected; 0 keeps the scalar diagonal. FP64 solves always
  *   use the reference's scalar DiagPreconditioner. */
 #define OGB_OPT_MIXED_BLOCK_JACOBI 9
-/*   OGB_OPT_HALF_FORM (0..4, default 0): loop form of the half-stored SpMV: the
+/*   OGB_OPT_HALF_FORM (0..3, default 0): loop form of the half-stored SpMV: the
  *   registers per thread bounded for 4 (1), 3 (2) or 2 (3) resident blocks of
- *   256 threads per SM, or (4) the matrix values staged through shared memory
- *   by asynchronous copies; 0 = timed once per matrix by the built-in
- *   autotuner. The forms give bitwise equal results. */
+ *   256 threads per SM; 0 = timed once per matrix by the built-in autotuner. The
+ *   forms give bitwise equal results. */
 #define OGB_OPT_HALF_FORM 12
 /*   OGB_OPT_UPDATE_BLOCKS (0..8, default 0): blocks per SM of the block-Jacobi
  *   vector update of mixed solves; 0 = one wave of the kernel's resident blocks
@@ -139,7 +138,7 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   beyond what the Newton iteration and the CG solve tolerate, hence off by
  *   default. FP64 steps and LinearStatic always use the FP64 element kernels. */
 #define OGB_OPT_TANGENT_TC 11
-/*   OGB_OPT_FUSED_UPDATE (0/1, default 0): mixed solves with the block-Jacobi
+/*   OGB_OPT_FUSED_UPDATE (0/1, default 1): mixed solves with the block-Jacobi
  *   preconditioner run the vector update and the p update of an iteration as
  *   one cooperative launch (z stays in shared memory; the blocks wait for the
  *   iteration's beta with a bounded wait). Same arithmetic and sum order as the

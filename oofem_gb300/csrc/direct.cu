@@ -145,38 +145,45 @@ __global__ void __launch_bounds__(NTHREADS) k_ldl_subpanel(int n, int bw, double
 // Trailing update of panel [k0, k1) on the band rows/columns [k1, e),
 // e = min(n, k1 + bw): A(i, c) -= sum_p L(i, p) d_p L(c, p) for c <= i, both
 // within the band of the panel column p. Tile (ti, tc) of 32 x 32, lower tiles
-// only; the panel rows of the tile are staged in shared memory.
+// only; the panel rows of the tile are staged in shared memory (Li transposed,
+// so the lanes read consecutive words). Lane a takes row i0 + a, so the lanes of
+// a warp read and write 32 consecutive entries of one band column.
 __global__ void __launch_bounds__(NTHREADS) k_ldl_trailing(int n, int bw, double *__restrict__ band, int k0, int k1,
                                                            const int *status)
 {
     if (*status) return;
     const int ti = blockIdx.y, tc = blockIdx.x;
     if (ti < tc) return;
-    __shared__ double Li[32][PANEL + 1];   // L(i, p) * d_p
-    __shared__ double Lc[32][PANEL + 1];   // L(c, p)
+    __shared__ double Li[PANEL][32];       // L(i, p) * d_p, [p][a]
+    __shared__ double Lc[32][PANEL + 1];   // L(c, p), [b][p]
     const int64_t ld = (int64_t)bw + 1;
     const int e = (int)min((int64_t)n, (int64_t)k1 + bw);
     const int i0 = k1 + 32 * ti, c0 = k1 + 32 * tc;
     const int P = k1 - k0;
-    for (int t = threadIdx.x; t < 32 * P; t += blockDim.x) {
+    for (int t = threadIdx.x; t < 32 * PANEL; t += blockDim.x) {
         const int p = t / 32, a = t % 32;
+        if (p >= P) {
+            Li[p][a] = 0.0;
+            Lc[a][p] = 0.0;
+            continue;
+        }
         const int j = k0 + p;
         const double *cjp = band + (int64_t)j * ld;
         const int i = i0 + a, c = c0 + a;
-        Li[a][p] = (i < e && i - j <= bw) ? cjp[i - j] * cjp[0] : 0.0;
+        Li[p][a] = (i < e && i - j <= bw) ? cjp[i - j] * cjp[0] : 0.0;
         Lc[a][p] = (c < e && c - j <= bw) ? cjp[c - j] : 0.0;
     }
     __syncthreads();
-    const int b = threadIdx.x & 31, a0 = threadIdx.x >> 5;
-    const int c = c0 + b;
-    if (c >= e) return;
+    const int a = threadIdx.x & 31, b0 = threadIdx.x >> 5;
+    const int i = i0 + a;
+    if (i >= e) return;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int a = a0 + 8 * q;
-        const int i = i0 + a;
-        if (i >= e || i < c || i - c > bw) continue;
+        const int b = b0 + 8 * q;
+        const int c = c0 + b;
+        if (c >= e || i < c || i - c > bw) continue;
         double s = 0.0;
-        for (int p = 0; p < P; ++p) s += Li[a][p] * Lc[b][p];
+        for (int p = 0; p < P; ++p) s += Li[p][a] * Lc[b][p];
         band[(int64_t)c * ld + (i - c)] -= s;
     }
 }

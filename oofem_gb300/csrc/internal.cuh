@@ -234,7 +234,7 @@ struct ogb_ctx {
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix
     int upd_bps = 0;            // blocks per SM of the block-Jacobi update and p update (0 = its occupancy)
-    bool fused_update = false;  // block-Jacobi update and p update in one cooperative launch
+    bool fused_update = true;   // block-Jacobi update and p update in one cooperative launch
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner

@@ -325,190 +325,6 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
     }
 }
 
-// Asynchronous-copy form of k_half_spmv (same sums in the same order, bitwise
-// equal results). The register-bound forms keep few blocks in flight per warp
-// (the values of a block occupy registers from load to use); here the values
-// travel by cp.async into a two-stage shared-memory ring per warp and hold no
-// registers while in flight. Upper pass: the values and block columns of AG
-// consecutive k-groups of the slice are contiguous (AG x 32 x ND*ND floats,
-// AG x 32 ints), copied as 16-byte pieces (L2 only), the next AG groups issued
-// before the current ones are used. Lower pass: each lane copies the ND*ND
-// entries of its next AG transposed blocks (4-byte pieces) into the other stage
-// while it multiplies the current ones; the lower entries are loaded two chunks
-// ahead. The x gathers stay ordinary loads. 8 warps per CTA, ring of
-// 2 x HALF_ASYNC_STAGE floats per warp.
-constexpr int HALF_AG = 4;
-template <int ND>
-__host__ __device__ constexpr int half_async_stage() { return HALF_AG * 32 * ND * ND + HALF_AG * 32; }
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-                 "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-                 "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-template <int ND, class X, bool DIFF>
-__global__ void __launch_bounds__(NTHREADS, 2) k_half_spmv_async(int nslices, const int64_t *__restrict__ ptrU,
-                                                               const int *__restrict__ wU,
-                                                               const int *__restrict__ colU,
-                                                               const float *__restrict__ val,
-                                                               const int64_t *__restrict__ ptrL,
-                                                               const int *__restrict__ wL, const int *__restrict__ low,
-                                                               const X *__restrict__ x, X *__restrict__ y,
-                                                               double *part, unsigned int *count, PcgScal *sc)
-{
-    if (halted(sc)) return;
-    constexpr int NN = ND * ND, VALS = HALF_AG * 32 * NN, STAGE = half_async_stage<ND>();
-    extern __shared__ __align__(16) float ring_all[];
-    const int warp = threadIdx.x >> 5, r = threadIdx.x & 31;
-    const int s = blockIdx.x * (NTHREADS / 32) + warp;
-    float *ring = ring_all + (size_t)warp * 2 * STAGE;
-    auto gather = [&](int c, float (&v)[ND]) {
-#pragma unroll
-        for (int j = 0; j < ND; ++j) v[j] = (float)__ldg(x + (int64_t)c * ND + j);
-    };
-    double dot = 0.0;
-    if (s < nslices) {
-        const int arow = s * 32 + r;
-        float yy[ND], xa[ND];
-#pragma unroll
-        for (int i = 0; i < ND; ++i) {
-            yy[i] = 0.f;
-            xa[i] = (float)x[(int64_t)arow * ND + i];
-        }
-        {   // upper pass
-            const int64_t base = ptrU[s];
-            const int w = wU[s];
-            auto issue = [&](int k0, int st) {
-                const int ng = min(HALF_AG, w - k0);
-                const float *vsrc = val + (base + 32 * (int64_t)k0) * NN;
-                const int *csrc = colU + base + 32 * (int64_t)k0;
-                float *dst = ring + st * STAGE;
-                for (int q = r; q < ng * 8 * NN; q += 32) cp_async16(dst + 4 * q, vsrc + 4 * q);
-                for (int q = r; q < ng * 8; q += 32) cp_async16(dst + VALS + 4 * q, csrc + 4 * q);
-                cp_async_commit();
-            };
-            if (w > 0) issue(0, 0);
-            int st = 0;
-            for (int k0 = 0; k0 < w; k0 += HALF_AG, st ^= 1) {
-                if (k0 + HALF_AG < w) {
-                    issue(k0 + HALF_AG, st ^ 1);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-                __syncwarp();
-                const float *vs = ring + st * STAGE;
-                const int *cs = reinterpret_cast<const int *>(vs + VALS);
-                float xb[HALF_AG][ND];
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    const int cg = k0 + g < w ? cs[32 * g + r] : arow;
-                    gather(cg, xb[g]);
-#pragma unroll
-                    for (int j = 0; j < ND; ++j)
-                        if (DIFF && cg != arow) xb[g][j] -= xa[j];
-                }
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    if (k0 + g < w) {
-#pragma unroll
-                        for (int i = 0; i < ND; ++i)
-#pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += vs[g * 32 * NN + 32 * (i * ND + j) + r] * xb[g][j];
-                    }
-                }
-                __syncwarp();   // the stage is refilled two chunks later
-            }
-        }
-        {   // lower pass
-            const int64_t base = ptrL[s];
-            const int w = wL[s];
-            const int *lp = low + base + r;
-            auto entries = [&](int k0, int (&e)[HALF_AG]) {
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) e[g] = k0 + g < w ? __ldcs(lp + 32 * (k0 + g)) : -1;
-            };
-            auto issue = [&](const int (&e)[HALF_AG], int st) {
-                float *dst = ring + st * STAGE;
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    if (e[g] >= 0) {
-                        const int c = e[g] >> 6, kk = e[g] & 63;
-                        const float *src = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * NN + (c & 31);
-#pragma unroll
-                        for (int q = 0; q < NN; ++q) cp_async4(dst + g * 32 * NN + 32 * q + r, src + 32 * q);
-                    }
-                }
-                cp_async_commit();
-            };
-            int ec[HALF_AG], en[HALF_AG], ef[HALF_AG];
-            entries(0, ec);
-            entries(HALF_AG, en);
-            if (w > 0) issue(ec, 0);
-            int st = 0;
-            for (int k0 = 0; k0 < w; k0 += HALF_AG, st ^= 1) {
-                entries(k0 + 2 * HALF_AG, ef);
-                if (k0 + HALF_AG < w) {
-                    issue(en, st ^ 1);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-                __syncwarp();
-                const float *vs = ring + st * STAGE;
-                float xb[HALF_AG][ND];
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    gather(ec[g] >= 0 ? (ec[g] >> 6) : arow, xb[g]);
-#pragma unroll
-                    for (int j = 0; j < ND; ++j)
-                        if (DIFF) xb[g][j] -= xa[j];
-                }
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    if (ec[g] >= 0) {
-#pragma unroll
-                        for (int i = 0; i < ND; ++i)
-#pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += vs[g * 32 * NN + 32 * (j * ND + i) + r] * xb[g][j];
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (int g = 0; g < HALF_AG; ++g) {
-                    ec[g] = en[g];
-                    en[g] = ef[g];
-                }
-            }
-        }
-        const int64_t a = (int64_t)s * 32 + r;
-#pragma unroll
-        for (int i = 0; i < ND; ++i) {
-            y[a * ND + i] = (X)yy[i];
-            dot += (double)x[a * ND + i] * (double)yy[i];   // exact in FP64
-        }
-    }
-    double acc[1] = {dot};
-    block_sum<1>(acc);
-    if (publish_partials<1>(acc, part, count)) {
-        double t[1];
-        final_sums<1>(part, t);
-        if (threadIdx.x != 0) return;
-        finish_pq(t[0], count, sc);
-    }
-}
-
 // ---------------------------------------------------------------- vector kernels
 // r = b - Ax (Ax in q), z = D^-1 r, p = z; ||b||^2, ||r||^2, r.z.
 template <class X>
@@ -1649,22 +1465,8 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
 
 // q = K p through the half-stored FP32 copy, fused p.q (mixed solves).
 // Half-stored SpMV forms: 1 = 4 resident blocks per SM (64 registers), 2 = 3
-// blocks (80 registers), 3 = 2 blocks (128 registers), 4 = values staged by
-// asynchronous copies (k_half_spmv_async).
-constexpr int HALF_FORMS = 4;
-
-template <int ND>
-constexpr int half_async_smem() { return (NTHREADS / 32) * 2 * half_async_stage<ND>() * (int)sizeof(float); }
-
-// The asynchronous-copy form's shared-memory limit, raised once per device
-// (before any stream capture: the mixed solve calls it when it picks the form).
-template <int ND, class X, bool DIFF>
-int half_async_ready()
-{
-    static bool attr_set[64] = {};
-    OGB_CUDA(set_smem_limit_once((const void *)k_half_spmv_async<ND, X, DIFF>, half_async_smem<ND>(), attr_set));
-    return OGB_OK;
-}
+// blocks (80 registers), 3 = 2 blocks (128 registers).
+constexpr int HALF_FORMS = 3;
 
 template <int ND, class X, bool DIFF>
 int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, double *part, unsigned int *count,
@@ -1674,16 +1476,9 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     const int grid = (int)ceil_div(S.nslices, NTHREADS / 32);
 #define OGB_HALF_ARGS S.nslices, H.sl_ptrU.p, H.sl_widthU.p, H.colU.p, H.v32.p, H.sl_ptrL.p, H.sl_widthL.p, H.low.p, \
                       x, y, part, count, sc
-    if (form == 4) {
-        OGB_CHECK((half_async_ready<ND, X, DIFF>()));
-        k_half_spmv_async<ND, X, DIFF><<<grid, NTHREADS, half_async_smem<ND>(), s>>>(OGB_HALF_ARGS);
-    } else if (form == 2) {
-        k_half_spmv<ND, X, DIFF, 8, 3><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    } else if (form == 3) {
-        k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    } else {
-        k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    }
+    if (form == 2) k_half_spmv<ND, X, DIFF, 8, 3><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
 }
@@ -2171,8 +1966,6 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     m->last_half = half;
     if (half) {
         if constexpr (sizeof(P) == 4) {
-            if (op.S->nd == 3) OGB_CHECK(diff ? (half_async_ready<3, P, true>()) : (half_async_ready<3, P, false>()));
-            else OGB_CHECK(diff ? (half_async_ready<2, P, true>()) : (half_async_ready<2, P, false>()));
             if (!ctx->half_form) {
                 if (diff) OGB_CHECK((half_autotune<P, true>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc + 1)));
                 else OGB_CHECK((half_autotune<P, false>(ctx, op, p, q, m->w_part.p, m->w_count.p, sc + 1)));
