@@ -22,6 +22,7 @@ E = 30e9), three prescribed-strain load cases each, one batched FP64 PCG to
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -366,12 +367,26 @@ def run_gpu(args):
     value = replicas.job_throughput(nfree, ms * 1e-3)
     ms = replicas.max_over_ranks(ms)
 
-    # end to end through the host API: mesh upload, pattern, assembly, solve, copy back
+    # end to end through the host API: mesh upload, pattern, assembly, solve, copy back;
+    # the inputs and the result buffers live in page-locked host memory
+    keep = []
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        keep.append(t)
+        v = t.numpy()
+        v[...] = a
+        return v
+    mesh_h = dataclasses.replace(mesh, coords=pinned(mesh.coords), conn=pinned(mesh.conn),
+                                 elem_mat=pinned(mesh.elem_mat), bc_mask=pinned(mesh.bc_mask),
+                                 bc_value=pinned(mesh.bc_value), nodal_load=pinned(mesh.nodal_load))
+    out_h = (pinned(np.zeros_like(mesh.bc_value)), pinned(np.zeros_like(mesh.bc_value)))
+
     def e2e_once():
         c2 = native.Context(local)
-        m2 = native.GpuModel(c2, mesh)
+        m2 = native.GpuModel(c2, mesh_h)
         A2 = native.GpuCsrMtrx(c2)
-        uh, rh, info = m2.linear_static(A2, rtol=RTOL, maxit=200000, precision=native.PREC_MIXED)
+        uh, rh, info = m2.linear_static(A2, rtol=RTOL, maxit=200000, precision=native.PREC_MIXED, out=out_h)
         A2.close()
         m2.close()
         c2.close()

@@ -475,12 +475,22 @@ class GpuModel:
         _check(self.lib.ogb_model_commit_state(self.h))
 
     def linear_static(self, A: GpuCsrMtrx, bc_value=None, nodal_load=None, rtol=1e-12,
-                      maxit=100000, precision=PREC_FP64, want_reactions=True):
+                      maxit=100000, precision=PREC_FP64, want_reactions=True, out=None):
+        """out: optional (u, reactions) float64 arrays of the mesh's (nnodes, ndofpn)
+        shape to receive the results (e.g. page-locked host buffers)."""
         m = self.mesh
         bcv = np.ascontiguousarray(m.bc_value if bc_value is None else bc_value, dtype=np.float64)
         ld = np.ascontiguousarray(m.nodal_load if nodal_load is None else nodal_load, dtype=np.float64)
-        u = np.zeros_like(bcv)
-        reac = np.zeros_like(bcv) if want_reactions else None
+        if out is not None:
+            u, reac = out
+            for a in (u, reac):
+                if a is not None and (a.shape != bcv.shape or a.dtype != np.float64 or not a.flags.c_contiguous):
+                    raise ValueError("out arrays must be C-contiguous float64 of shape %s" % (bcv.shape,))
+            if not want_reactions:
+                reac = None
+        else:
+            u = np.zeros_like(bcv)
+            reac = np.zeros_like(bcv) if want_reactions else None
         info = SolveInfo()
         code = self.lib.ogb_linear_static(self.h, A.h, _ptr(bcv), _ptr(ld), rtol, maxit, precision,
                                           _ptr(u), _ptr(reac) if reac is not None else None,
