@@ -15,8 +15,10 @@
 // Application (device): ICSolve (icprecond.C:166-190) is a forward solve by
 // columns and a backward solve by columns. On the device both run by rows,
 // level by level: row i's forward value needs the rows c < i of its transposed
-// column entries, its backward value the rows r > i of its own column. Each
-// level is one launch of one thread per row; the products are accumulated in
+// column entries, its backward value the rows r > i of its own column. A run
+// of levels of up to 4,096 rows each is one launch of one CTA that steps through
+// them with a barrier between levels; a wider level is a launch of its own,
+// one thread per row. The products are accumulated in
 // the reference's order (columns resp. rows ascending, starting from zero) with
 // separate rounded multiply and subtract, so z = M^-1 r is bitwise the
 // reference's.
@@ -38,61 +40,56 @@ namespace ogb {
 
 namespace {
 
-__global__ void k_ic_fwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
-                         const int *__restrict__ col, const double *__restrict__ val,
-                         const double *__restrict__ diag, const double *__restrict__ x, double *__restrict__ w,
-                         const PcgScal *sc)
+// Row i of a level of one triangular solve, in the reference's arithmetic
+// (separately rounded products and differences, entries in stored order):
+//   IC  (KIND 4): out_i = (in_i + sum(-v_e out_c)) / d_i, forward and backward;
+//   ILU (KIND 2): forward out_i = sum(-v_e out_c) + in_i, backward
+//                 out_i = (in_i - v_e out_c - ...) / d_i.
+template <int KIND, bool FWD>
+__device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, const int *__restrict__ col,
+                                        const double *__restrict__ val, const double *__restrict__ diag,
+                                        const double *__restrict__ in, double *out)
 {
-    if (sc && (sc->done || sc->reliable)) return;
-    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= r1) return;
-    const int i = rows[t];
-    double acc = 0.0;
-    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], w[col[e]]));
-    w[i] = __ddiv_rn(__dadd_rn(x[i], acc), diag[i]);
+    double acc = (KIND == 2 && !FWD) ? in[i] : 0.0;
+    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], out[col[e]]));
+    if (KIND == 4) out[i] = __ddiv_rn(__dadd_rn(in[i], acc), diag[i]);
+    else if (FWD) out[i] = __dadd_rn(acc, in[i]);
+    else out[i] = __ddiv_rn(acc, diag[i]);
 }
 
-__global__ void k_ic_bwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
-                         const int *__restrict__ col, const double *__restrict__ val,
-                         const double *__restrict__ diag, const double *__restrict__ w, double *__restrict__ y,
-                         const PcgScal *sc)
+// One wide level: a thread per row, as many blocks as the level needs.
+template <int KIND, bool FWD>
+__global__ void k_tri_level(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
+                            const int *__restrict__ col, const double *__restrict__ val,
+                            const double *__restrict__ diag, const double *__restrict__ in, double *out,
+                            const PcgScal *sc)
 {
     if (sc && (sc->done || sc->reliable)) return;
     const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= r1) return;
-    const int i = rows[t];
-    double acc = 0.0;
-    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], y[col[e]]));
-    y[i] = __ddiv_rn(__dadd_rn(w[i], acc), diag[i]);
+    tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
 }
 
-// ILU: w_i = (sum over c < i, ascending, of -L_ic w_c) + x_i.
-__global__ void k_ilu_fwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
-                          const int *__restrict__ col, const double *__restrict__ val, const double *__restrict__ x,
-                          double *__restrict__ w, const PcgScal *sc)
+// A run of narrow levels [l0, l1) in one CTA: the threads take the rows of a
+// level, then the CTA barrier makes the level's results visible to the next
+// (no launch per level).
+constexpr int TRI_THREADS = 1024;
+template <int KIND, bool FWD>
+__global__ void __launch_bounds__(TRI_THREADS) k_tri_levels(int l0, int l1, const int *__restrict__ lev,
+                                                            const int *__restrict__ rows,
+                                                            const int64_t *__restrict__ ptr,
+                                                            const int *__restrict__ col,
+                                                            const double *__restrict__ val,
+                                                            const double *__restrict__ diag,
+                                                            const double *__restrict__ in, double *out,
+                                                            const PcgScal *sc)
 {
     if (sc && (sc->done || sc->reliable)) return;
-    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= r1) return;
-    const int i = rows[t];
-    double acc = 0.0;
-    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], w[col[e]]));
-    w[i] = __dadd_rn(acc, x[i]);
-}
-
-// ILU: y_i = (w_i - sum over c > i, descending, of U_ic y_c) / U_ii.
-__global__ void k_ilu_bwd(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
-                          const int *__restrict__ col, const double *__restrict__ val,
-                          const double *__restrict__ diag, const double *__restrict__ w, double *__restrict__ y,
-                          const PcgScal *sc)
-{
-    if (sc && (sc->done || sc->reliable)) return;
-    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= r1) return;
-    const int i = rows[t];
-    double acc = w[i];
-    for (int64_t e = ptr[i]; e < ptr[i + 1]; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], y[col[e]]));
-    y[i] = __ddiv_rn(acc, diag[i]);
+    for (int l = l0; l < l1; ++l) {
+        const int r1 = lev[l + 1];
+        for (int t = lev[l] + threadIdx.x; t < r1; t += TRI_THREADS) tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
+        __syncthreads();
+    }
 }
 
 // Rows grouped by level (counting sort, rows ascending within a level).
@@ -151,6 +148,8 @@ int upload_factor(ogb_mtrx *m, int kind, const std::vector<int64_t> &fp, const s
     OGB_CHECK(up(F.diag, dg));
     OGB_CHECK(up(F.frows, frows));
     OGB_CHECK(up(F.brows, brows));
+    OGB_CHECK(up(F.d_flev, F.flev));
+    OGB_CHECK(up(F.d_blev, F.blev));
     OGB_CHECK(F.work.alloc(n > 0 ? n : 1));
     OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
     F.n = n;
@@ -343,31 +342,50 @@ int build_ic(ogb_mtrx *m)
     return upload_factor(m, 4, fp, fc, fv, bp, bc, bv, dg);
 }
 
+// Levels wider than this run as their own multi-block launch; runs of narrower
+// levels go to one single-CTA launch.
+constexpr int TRI_WIDE = 4 * TRI_THREADS;
+
+template <int KIND, bool FWD>
+void tri_solve(cudaStream_t s, const std::vector<int> &lev, const int *d_lev, const int *rows, const int64_t *ptr,
+               const int *col, const double *val, const double *diag, const double *in, double *out,
+               const PcgScal *sc, int &launches)
+{
+    const int nl = (int)lev.size() - 1;
+    int l = 0;
+    while (l < nl) {
+        if (lev[l + 1] - lev[l] > TRI_WIDE) {
+            const int r0 = lev[l], r1 = lev[l + 1];
+            k_tri_level<KIND, FWD><<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, rows, ptr, col,
+                                                                                          val, diag, in, out, sc);
+            ++l;
+        } else {
+            int e = l;
+            while (e < nl && lev[e + 1] - lev[e] <= TRI_WIDE) ++e;
+            k_tri_levels<KIND, FWD><<<1, TRI_THREADS, 0, s>>>(l, e, d_lev, rows, ptr, col, val, diag, in, out, sc);
+            l = e;
+        }
+        ++launches;
+    }
+}
+
 int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
 {
     IcFactor &F = m->ic;
     cudaStream_t s = m->ctx->stream;
-    const int nlf = (int)F.flev.size() - 1, nlb = (int)F.blev.size() - 1;
-    for (int l = 0; l < nlf; ++l) {
-        const int r0 = F.flev[l], r1 = F.flev[l + 1];
-        const unsigned g = (unsigned)ceil_div(r1 - r0, NTHREADS);
-        if (F.kind == 2)
-            k_ilu_fwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, r, F.work.p, sc);
-        else
-            k_ic_fwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p,
-                                            sc);
+    int launches = 0;
+    if (F.kind == 2) {
+        tri_solve<2, true>(s, F.flev, F.d_flev.p, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p, sc,
+                           launches);
+        tri_solve<2, false>(s, F.blev, F.d_blev.p, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
+                            sc, launches);
+    } else {
+        tri_solve<4, true>(s, F.flev, F.d_flev.p, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p, sc,
+                           launches);
+        tri_solve<4, false>(s, F.blev, F.d_blev.p, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
+                            sc, launches);
     }
-    for (int l = 0; l < nlb; ++l) {
-        const int r0 = F.blev[l], r1 = F.blev[l + 1];
-        const unsigned g = (unsigned)ceil_div(r1 - r0, NTHREADS);
-        if (F.kind == 2)
-            k_ilu_bwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
-                                             sc);
-        else
-            k_ic_bwd<<<g, NTHREADS, 0, s>>>(r0, r1, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
-                                            sc);
-    }
-    count_launch(m->ctx, nlf + nlb);
+    count_launch(m->ctx, launches);
     OGB_CUDA(cudaGetLastError());
     return OGB_OK;
 }

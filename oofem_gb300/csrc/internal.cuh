@@ -187,6 +187,7 @@ struct IcFactor {
     DBuf<int> fcol, bcol, frows, brows;
     DBuf<double> fval, bval, diag, work;
     std::vector<int> flev, blev;   // level starts into frows / brows
+    DBuf<int> d_flev, d_blev;      // the same on the device
 };
 
 // LDL^T factor of the direct solver (direct.cu): dense band of n x (bw+1)
