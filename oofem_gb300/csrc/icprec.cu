@@ -17,8 +17,9 @@
 // level by level: row i's forward value needs the rows c < i of its transposed
 // column entries, its backward value the rows r > i of its own column. A run
 // of levels of up to 4,096 rows each is one launch of one CTA that steps through
-// them with a barrier between levels (a warp per row); a wider level is a launch
-// of its own, one thread per row. The products are accumulated in
+// them with a barrier between levels; a wider level is a launch of its own; a
+// thread per row in both, each row's entries loaded in chunks of eight before
+// their differences. The products are accumulated in
 // the reference's order (columns resp. rows ascending, starting from zero) with
 // separate rounded multiply and subtract, so z = M^-1 r is bitwise the
 // reference's.
@@ -88,11 +89,10 @@ __global__ void k_tri_level(int r0, int r1, const int *__restrict__ rows, const 
     tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
 }
 
-// A run of narrow levels [l0, l1) in one CTA: a warp per row -- the lanes load
-// the row's entries and form their products together, then every lane takes
-// the differences in the stored order from the warp's shared buffer -- and a
-// CTA barrier between levels makes a level's results visible to the next (no
-// launch per level).
+// A run of narrow levels [l0, l1) in one CTA: the threads take the rows of a
+// level (a thread per row: the FP64 pipe is narrow, so no row's arithmetic is
+// repeated across lanes), then the CTA barrier makes the level's results
+// visible to the next (no launch per level).
 constexpr int TRI_THREADS = 1024;
 template <int KIND, bool FWD>
 __global__ void __launch_bounds__(TRI_THREADS) k_tri_levels(int l0, int l1, const int *__restrict__ lev,
@@ -105,29 +105,9 @@ __global__ void __launch_bounds__(TRI_THREADS) k_tri_levels(int l0, int l1, cons
                                                             const PcgScal *sc)
 {
     if (sc && (sc->done || sc->reliable)) return;
-    __shared__ double prod[TRI_THREADS];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *pw = prod + 32 * warp;
     for (int l = l0; l < l1; ++l) {
         const int r1 = lev[l + 1];
-        for (int t = lev[l] + warp; t < r1; t += TRI_THREADS / 32) {
-            const int i = rows[t];
-            const int64_t e0 = ptr[i], e1 = ptr[i + 1];
-            double acc = (KIND == 2 && !FWD) ? in[i] : 0.0;
-            for (int64_t c0 = e0; c0 < e1; c0 += 32) {
-                const int64_t e = c0 + lane;
-                const int cnt = (int)min((int64_t)32, e1 - c0);
-                pw[lane] = e < e1 ? __dmul_rn(val[e], out[col[e]]) : 0.0;
-                __syncwarp();
-                for (int k = 0; k < cnt; ++k) acc = __dsub_rn(acc, pw[k]);
-                __syncwarp();
-            }
-            if (lane == 0) {
-                if (KIND == 4) out[i] = __ddiv_rn(__dadd_rn(in[i], acc), diag[i]);
-                else if (FWD) out[i] = __dadd_rn(acc, in[i]);
-                else out[i] = __ddiv_rn(acc, diag[i]);
-            }
-        }
+        for (int t = lev[l] + threadIdx.x; t < r1; t += TRI_THREADS) tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
         __syncthreads();
     }
 }

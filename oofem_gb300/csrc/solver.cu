@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // bounds the registers per thread (4: 64; 3: 80; 2: 128, more loads in flight per
 // warp). The loop and its sum order do not depend on MINB: the forms give
 // bitwise equal results.
-template <int ND, class X, bool DIFF, int G, int MINB = 4>
+template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false>
 __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
                                                         const float *__restrict__ val, const int64_t *__restrict__ ptrL,
@@ -259,14 +259,34 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                     for (int j = 0; j < ND; ++j)
                         if (DIFF && cc[g] != arow) xb[g][j] -= xa[j];
                 }
+                if constexpr (EXPL) {
+                    // every value of the group loaded before the products
+                    float v[G][ND * ND];
 #pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    if (k0 + g < w) {
+                    for (int g = 0; g < G; ++g) {
                         const float *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
 #pragma unroll
-                        for (int i = 0; i < ND; ++i)
+                        for (int q = 0; q < ND * ND; ++q) v[g][q] = k0 + g < w ? __ldcg(vk + 32 * q) : 0.f;
+                    }
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldcg(vk + 32 * (i * ND + j)) * xb[g][j];
+                    for (int g = 0; g < G; ++g) {
+                        if (k0 + g < w) {
+#pragma unroll
+                            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                                for (int j = 0; j < ND; ++j) yy[i] += v[g][i * ND + j] * xb[g][j];
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        if (k0 + g < w) {
+                            const float *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                                for (int j = 0; j < ND; ++j) yy[i] += __ldcg(vk + 32 * (i * ND + j)) * xb[g][j];
+                        }
                     }
                 }
             }
@@ -297,13 +317,31 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                     for (int j = 0; j < ND; ++j)
                         if (DIFF) xb[g][j] -= xa[j];
                 }
+                if constexpr (EXPL) {
+                    float v[G][ND * ND];
 #pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    if (e[g] >= 0) {
+                    for (int g = 0; g < G; ++g)
 #pragma unroll
-                        for (int i = 0; i < ND; ++i)
+                        for (int q = 0; q < ND * ND; ++q) v[g][q] = e[g] >= 0 ? __ldcs(vk[g] + 32 * q) : 0.f;
 #pragma unroll
-                            for (int j = 0; j < ND; ++j) yy[i] += __ldcs(vk[g] + 32 * (j * ND + i)) * xb[g][j];
+                    for (int g = 0; g < G; ++g) {
+                        if (e[g] >= 0) {
+#pragma unroll
+                            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                                for (int j = 0; j < ND; ++j) yy[i] += v[g][j * ND + i] * xb[g][j];
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        if (e[g] >= 0) {
+#pragma unroll
+                            for (int i = 0; i < ND; ++i)
+#pragma unroll
+                                for (int j = 0; j < ND; ++j)
+                                    yy[i] += __ldcs(vk[g] + 32 * (j * ND + i)) * xb[g][j];
+                        }
                     }
                 }
             }
@@ -1478,6 +1516,8 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
                       x, y, part, count, sc
     if (form == 2) k_half_spmv<ND, X, DIFF, 8, 3><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 5) k_half_spmv<ND, X, DIFF, 8, 2, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
