@@ -42,7 +42,9 @@ SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns pref
 HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers for 3 blocks per SM (80)",
               3: "registers for 2 blocks per SM (128)",
               4: "all values of 4 blocks loaded before their products, 3 blocks per SM (80)",
-              5: "all values of 8 blocks loaded before their products, 2 blocks per SM (128)"}
+              5: "all values of 3 blocks loaded before their products, 4 blocks per SM (64)",
+              6: "all values of 5 blocks loaded before their products, 3 blocks per SM (80)",
+              7: "all values of 6 blocks loaded before their products, 2 blocks per SM (128)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -860,7 +862,7 @@ def main():
     ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
-    ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3, 4, 5),
+    ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3, 4, 5, 6, 7),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
     ap.add_argument("--fused-update", type=int, default=-1, choices=(-1, 0, 1),

@@ -1517,7 +1517,9 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     if (form == 2) k_half_spmv<ND, X, DIFF, 8, 3><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 5) k_half_spmv<ND, X, DIFF, 8, 2, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 5) k_half_spmv<ND, X, DIFF, 3, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 6) k_half_spmv<ND, X, DIFF, 5, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 7) k_half_spmv<ND, X, DIFF, 6, 2, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
