@@ -43,8 +43,10 @@ HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers for 3 block
               3: "registers for 2 blocks per SM (128)",
               4: "all values of 4 blocks loaded before their products, 3 blocks per SM (80)",
               5: "all values of 3 blocks loaded before their products, 4 blocks per SM (64)",
-              6: "all values of 5 blocks loaded before their products, 3 blocks per SM (80)",
-              7: "all values of 6 blocks loaded before their products, 2 blocks per SM (128)"}
+              6: "all values of 3 blocks loaded before their products, 5 blocks per SM (48)",
+              7: "all values of 2 blocks loaded before their products, 5 blocks per SM (48)",
+              8: "all values of 2 blocks loaded before their products, 6 blocks per SM (40)",
+              9: "all values of 2 blocks loaded before their products, 4 blocks per SM (56)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -824,9 +826,23 @@ def run_solvers(args):
         u, reac, info = model.linear_static(A, rtol=RTOL, maxit=1000000, precision=pr)
         ctx.synchronize()
         dt = time.perf_counter() - t0
-        print(json.dumps({"mesh": f"{nx}x{ny}x{nz}", "free_dofs": mesh.nfree, "solver": name, "step_ms": 1e3 * dt,
-                          "iterations": info.iterations, "achieved": info.achieved, "status": info.status}),
-              flush=True)
+        rec = {"mesh": f"{nx}x{ny}x{nz}", "free_dofs": mesh.nfree, "solver": name, "step_ms": 1e3 * dt,
+               "iterations": info.iterations, "achieved": info.achieved, "status": info.status}
+        if lstype == 1:
+            # the same matrix again, its preconditioner kept (same version): the
+            # iterations alone, per iteration
+            neq = A.neq
+            sol = native.GpuPcgSolver(lstol=RTOL, lsiter=1000000, precision=pr, lsprecond=prec)
+            bb = np.ones(neq)
+            xx = np.zeros(neq)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            sol.solve(A, bb, xx)
+            ctx.synchronize()
+            ds = time.perf_counter() - t0
+            if sol.last.iterations > 0:
+                rec["ms_per_iteration_kept_preconditioner"] = 1e3 * ds / sol.last.iterations
+        print(json.dumps(rec), flush=True)
         A.close()
         model.close()
         ctx.close()
@@ -862,7 +878,7 @@ def main():
     ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
-    ap.add_argument("--half-form", type=int, default=-1, choices=(-1, 0, 1, 2, 3, 4, 5, 6, 7),
+    ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 10)),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
     ap.add_argument("--fused-update", type=int, default=-1, choices=(-1, 0, 1),

@@ -822,8 +822,9 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
 // UNR nodes of the block's node range per pass (nodes a, a + 256, ...), all their
 // loads issued before the arithmetic; the grid is one wave of resident blocks.
 // XS: the solution accumulator, double (the FP64 solution, x += alpha p) or
-// float (the FP32 increment since the last residual replacement, folded into the
-// FP64 solution by the host loop).
+// float (the FP32 increment of the current batch of iterations, folded into the
+// FP64 solution after each batch; the thread's dot-product terms are then summed
+// in FP32 before the FP64 block sums, so no FP64 work is done per node).
 // FUSE: the p update of the same iteration follows in this kernel. The blocks
 // keep their z in shared memory (zcap nodes; a larger range writes z to memory
 // and reads it back), the last block publishes beta and advances *epoch, and
@@ -851,6 +852,7 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__
     block_range(nnodes, lo, hi);
     const bool zsm = FUSE && hi - lo <= zcap;
     double v[2] = {0.0, 0.0};
+    float vf[2] = {0.f, 0.f};   // FP32 increment form: the thread's sums in FP32 (no FP64 work per node)
     for (int64_t a0 = lo + threadIdx.x; a0 < hi; a0 += (int64_t)UNR * NTHREADS) {
         float rr[UNR][ND], bb[UNR][NSYM], pp[UNR][ND];
         XS xx[UNR][ND];
@@ -887,9 +889,18 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__
                 s0 = fmaf(rr[u][d], rr[u][d], s0);
                 s1 = fmaf(rr[u][d], zz, s1);
             }
-            v[0] += (double)s0;
-            v[1] += (double)s1;
+            if constexpr (sizeof(XS) == 8) {
+                v[0] += (double)s0;
+                v[1] += (double)s1;
+            } else {
+                vf[0] += s0;
+                vf[1] += s1;
+            }
         }
+    }
+    if constexpr (sizeof(XS) == 4) {
+        v[0] = (double)vf[0];
+        v[1] = (double)vf[1];
     }
     if constexpr (!FUSE) {
         finish_update32(v, part, count, sc, maxit);
@@ -1518,8 +1529,10 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 5) k_half_spmv<ND, X, DIFF, 3, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 6) k_half_spmv<ND, X, DIFF, 5, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 7) k_half_spmv<ND, X, DIFF, 6, 2, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 6) k_half_spmv<ND, X, DIFF, 3, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 7) k_half_spmv<ND, X, DIFF, 2, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 8) k_half_spmv<ND, X, DIFF, 2, 6, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 9) k_half_spmv<ND, X, DIFF, 2, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
@@ -2060,6 +2073,13 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             }
             count_launch(ctx, bj && fuse ? 1 : 2);
         }
+        if constexpr (F32) {
+            if (!ctx->mixed_x64) {
+                // fold the FP32 increment of these iterations into the FP64 solution
+                k_fold_increment<<<num_sms() * 8, NTHREADS, 0, s>>>(n, x, d);
+                count_launch(ctx);
+            }
+        }
         OGB_CUDA(cudaGetLastError());
         return OGB_OK;
     };
@@ -2130,7 +2150,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
             if (res.done || res.reliable) break;
             if (ctx->use_graphs) {
                 OGB_CHECK(graph.launch(ctx));
-                count_launch(ctx, (bj && fuse ? 2 : 3) * BATCH);
+                count_launch(ctx, (bj && fuse ? 2 : 3) * BATCH + (F32 && !ctx->mixed_x64 ? 1 : 0));
             } else {
                 OGB_CHECK(batch());
             }
