@@ -39,14 +39,12 @@ sys.path.insert(0, ROOT)
 METRIC = "DOF/s to 1e-8 rel residual, mixed-prec+IR vs FP64 GPU; assembly+SpMV HBM GB/s"
 SPMV_FORMS = {1: "plain loop", 2: "columns prefetched 1 ahead", 3: "columns prefetched 4 ahead", 4: "TMA-staged",
               8: "half-stored: upper blocks streamed, lower blocks applied as transposes"}
-HALF_FORMS = {1: "registers for 4 blocks per SM (64)", 2: "registers for 3 blocks per SM (80)",
-              3: "registers for 2 blocks per SM (128)",
-              4: "all values of 4 blocks loaded before their products, 3 blocks per SM (80)",
-              5: "all values of 3 blocks loaded before their products, 4 blocks per SM (64)",
-              6: "all values of 3 blocks loaded before their products, 5 blocks per SM (48)",
-              7: "all values of 2 blocks loaded before their products, 5 blocks per SM (48)",
-              8: "all values of 2 blocks loaded before their products, 6 blocks per SM (40)",
-              9: "all values of 2 blocks loaded before their products, 4 blocks per SM (56)"}
+HALF_FORMS = {1: "groups of 8 blocks, registers for 4 blocks per SM (64)",
+              2: "groups of 8 blocks, registers for 3 blocks per SM (80)",
+              3: "groups of 8 blocks, registers for 2 blocks per SM (128)",
+              4: "values of 4 blocks loaded before their products, 3 blocks per SM (80)",
+              5: "values of 3 blocks loaded before their products, 4 blocks per SM (64)",
+              6: "values of 2 blocks loaded before their products, 5 blocks per SM (48)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -878,7 +876,7 @@ def main():
     ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
-    ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 10)),
+    ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 7)),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
     ap.add_argument("--fused-update", type=int, default=-1, choices=(-1, 0, 1),

@@ -93,7 +93,8 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 /*   OGB_OPT_MIXED_P32 (0/1): mixed solves keep p and q = K p in FP32 only. */
 #define OGB_OPT_MIXED_P32 5
 /*   OGB_OPT_MIXED_X64 (0/1): with FP32 vectors, accumulate the solution in FP64
- *   directly (default 1; 0 accumulates an FP32 increment between replacements).
+ *   every iteration (1), or as an FP32 increment folded into the FP64 solution
+ *   after every 16 iterations and at each residual replacement (0).
  *   Single-matrix solves only: batched solves always accumulate in FP64. */
 #define OGB_OPT_MIXED_X64 6
 /*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
@@ -118,10 +119,12 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   (lsprecond 1) is selected; 0 keeps the scalar diagonal. FP64 solves always
  *   use the reference's scalar DiagPreconditioner. */
 #define OGB_OPT_MIXED_BLOCK_JACOBI 9
-/*   OGB_OPT_HALF_FORM (0..3, default 0): loop form of the half-stored SpMV: the
- *   registers per thread bounded for 4 (1), 3 (2) or 2 (3) resident blocks of
- *   256 threads per SM; 0 = timed once per matrix by the built-in autotuner. The
- *   forms give bitwise equal results. */
+/*   OGB_OPT_HALF_FORM (0..6, default 0): loop form of the half-stored SpMV:
+ *   groups of 8 blocks with the registers per thread bounded for 4 (1), 3 (2)
+ *   or 2 (3) resident blocks of 256 threads per SM, or every value of a group
+ *   loaded before its products with groups of 4 at 3 blocks per SM (4), of 3 at
+ *   4 (5), of 2 at 5 (6); 0 = timed once per matrix by the built-in autotuner.
+ *   The forms give bitwise equal results. */
 #define OGB_OPT_HALF_FORM 12
 /*   OGB_OPT_UPDATE_BLOCKS (0..8, default 0): blocks per SM of the block-Jacobi
  *   vector update of mixed solves; 0 = one wave of the kernel's resident blocks

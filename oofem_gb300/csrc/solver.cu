@@ -208,9 +208,11 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // DIFF: the diagonal slot holds the block row sum and the off-diagonal blocks
 // act on x_c - x_a. The sum order is fixed (upper list, then lower list).
 // MINB: minimum resident blocks of 256 threads per SM asked of the compiler, which
-// bounds the registers per thread (4: 64; 3: 80; 2: 128, more loads in flight per
-// warp). The loop and its sum order do not depend on MINB: the forms give
-// bitwise equal results.
+// bounds the registers per thread (6: 40; 5: 48; 4: 64; 3: 80; 2: 128). EXPL: all
+// values of a group of G blocks are loaded into registers before the group's
+// products (with G = 3 at 4 blocks per SM the loads of three blocks are in
+// flight together: the fastest form on the 3M-DOF cantilever). The sums and
+// their order depend on neither: the forms give bitwise equal results.
 template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false>
 __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
@@ -1513,9 +1515,14 @@ int apply_op(ogb_ctx *ctx, const Op &op, const V *val, const X *x, X *y, double 
 }
 
 // q = K p through the half-stored FP32 copy, fused p.q (mixed solves).
-// Half-stored SpMV forms: 1 = 4 resident blocks per SM (64 registers), 2 = 3
-// blocks (80 registers), 3 = 2 blocks (128 registers).
-constexpr int HALF_FORMS = 3;
+// Half-stored SpMV forms: groups of 8 blocks, 1 = 4 resident blocks per SM (64
+// registers), 2 = 3 blocks (80), 3 = 2 blocks (128); every value of the group
+// loaded before its products: 4 = groups of 4 at 3 blocks per SM (80), 5 =
+// groups of 3 at 4 blocks (64), 6 = groups of 2 at 5 blocks (48). The
+// autotuner times them in HALF_ORDER (the first is kept unless a later one is
+// 2 % faster).
+constexpr int HALF_FORMS = 6;
+constexpr int HALF_ORDER[HALF_FORMS] = {5, 6, 4, 1, 2, 3};
 
 template <int ND, class X, bool DIFF>
 int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, double *part, unsigned int *count,
@@ -1529,10 +1536,7 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     else if (form == 3) k_half_spmv<ND, X, DIFF, 8, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 5) k_half_spmv<ND, X, DIFF, 3, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 6) k_half_spmv<ND, X, DIFF, 3, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 7) k_half_spmv<ND, X, DIFF, 2, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 8) k_half_spmv<ND, X, DIFF, 2, 6, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 9) k_half_spmv<ND, X, DIFF, 2, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
+    else if (form == 6) k_half_spmv<ND, X, DIFF, 2, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
@@ -1550,8 +1554,9 @@ int half_autotune(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, un
     OGB_CUDA(cudaEventCreate(&e0));
     OGB_CUDA(cudaEventCreate(&e1));
     float best = 0.f;
-    int best_f = 1;
-    for (int f = 1; f <= HALF_FORMS; ++f) {
+    int best_f = HALF_ORDER[0];
+    for (int fi = 0; fi < HALF_FORMS; ++fi) {
+        const int f = HALF_ORDER[fi];
         auto launch = [&]() {
             cudaMemsetAsync(sc, 0, sizeof(PcgScal), s);
             return S.nd == 3 ? launch_half<3, X, DIFF>(s, f, S, x, y, part, count, sc)
@@ -1570,7 +1575,7 @@ int half_autotune(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, un
             cudaEventDestroy(e1);
             return cuda_fail(e, "half-stored SpMV autotune");
         }
-        if (f == 1 || ms < 0.98f * best) {
+        if (fi == 0 || ms < 0.98f * best) {
             best = ms;
             best_f = f;
         }
@@ -1585,7 +1590,7 @@ template <class X, bool DIFF>
 int apply_half(ogb_ctx *ctx, const Op &op, const X *x, X *y, double *part, unsigned int *count, PcgScal *sc)
 {
     const SellMat &S = *op.S;
-    const int form = ctx->half_form ? ctx->half_form : (S.half.form ? S.half.form : 1);
+    const int form = ctx->half_form ? ctx->half_form : (S.half.form ? S.half.form : HALF_ORDER[0]);
     cudaStream_t s = ctx->stream;
     prof_begin(ctx);
     OGB_CHECK((S.nd == 3 ? launch_half<3, X, DIFF>(s, form, S, x, y, part, count, sc)
