@@ -15,11 +15,11 @@
 // Application (device): ICSolve (icprecond.C:166-190) is a forward solve by
 // columns and a backward solve by columns. On the device both run by rows,
 // level by level: row i's forward value needs the rows c < i of its transposed
-// column entries, its backward value the rows r > i of its own column. A run
-// of levels of up to 4,096 rows each is one launch of one CTA that steps through
-// them with a barrier between levels; a wider level is a launch of its own; a
-// thread per row in both, each row's entries loaded in chunks of eight before
-// their differences. The products are accumulated in
+// column entries, its backward value the rows r > i of its own column. Each
+// solve is one cooperative launch over all SMs that steps through the levels
+// with a grid barrier between them (rows of a level spread over the SMs, a
+// thread per row, each row's entries loaded in chunks of eight before their
+// differences). The products are accumulated in
 // the reference's order (columns resp. rows ascending, starting from zero) with
 // separate rounded multiply and subtract, so z = M^-1 r is bitwise the
 // reference's.
@@ -46,11 +46,13 @@ namespace {
 //   IC  (KIND 4): out_i = (in_i + sum(-v_e out_c)) / d_i, forward and backward;
 //   ILU (KIND 2): forward out_i = sum(-v_e out_c) + in_i, backward
 //                 out_i = (in_i - v_e out_c - ...) / d_i.
-template <int KIND, bool FWD>
+template <int KIND, bool FWD, bool L2 = false>
 __device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, const int *__restrict__ col,
                                         const double *__restrict__ val, const double *__restrict__ diag,
                                         const double *__restrict__ in, double *out)
 {
+    // L2: out[] is written by other SMs in this launch, so it is read from L2
+    auto rd = [&](int c) { return L2 ? __ldcg(out + c) : out[c]; };
     double acc = (KIND == 2 && !FWD) ? in[i] : 0.0;
     // the entries of a chunk are loaded before the chunk's differences, which
     // keep the stored order
@@ -66,49 +68,76 @@ __device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, 
             vv[k] = val[e + k];
         }
 #pragma unroll
-        for (int k = 0; k < CH; ++k) oo[k] = out[cc[k]];
+        for (int k = 0; k < CH; ++k) oo[k] = rd(cc[k]);
 #pragma unroll
         for (int k = 0; k < CH; ++k) acc = __dsub_rn(acc, __dmul_rn(vv[k], oo[k]));
     }
-    for (; e < e1; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], out[col[e]]));
+    for (; e < e1; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], rd(col[e])));
     if (KIND == 4) out[i] = __ddiv_rn(__dadd_rn(in[i], acc), diag[i]);
     else if (FWD) out[i] = __dadd_rn(acc, in[i]);
     else out[i] = __ddiv_rn(acc, diag[i]);
 }
 
-// One wide level: a thread per row, as many blocks as the level needs.
-template <int KIND, bool FWD>
-__global__ void k_tri_level(int r0, int r1, const int *__restrict__ rows, const int64_t *__restrict__ ptr,
-                            const int *__restrict__ col, const double *__restrict__ val,
-                            const double *__restrict__ diag, const double *__restrict__ in, double *out,
-                            const PcgScal *sc)
+// Grid-wide barrier of the cooperative level solve: the last block to arrive
+// resets the count and advances the epoch; the others wait for the advance.
+// The wait is bounded (about a second): past it, or once another block has
+// given up, the block sets *status and the caller returns.
+__device__ __forceinline__ bool grid_wait(unsigned int *count, unsigned int *epoch, int *status)
 {
-    if (sc && (sc->done || sc->reliable)) return;
-    const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= r1) return;
-    tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int e0 = *(volatile unsigned int *)epoch;
+        __threadfence();
+        const unsigned int t = atomicAdd(count, 1u);
+        if (t == gridDim.x - 1) {
+            *(volatile unsigned int *)count = 0u;
+            __threadfence();
+            atomicAdd(epoch, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*(volatile unsigned int *)epoch == e0) {
+                if (*(volatile int *)status) {
+                    ok = 0;
+                    break;
+                }
+                if (clock64() - t0 > 2000000000LL) {
+                    atomicCAS(status, 0, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
 }
 
-// A run of narrow levels [l0, l1) in one CTA: the threads take the rows of a
-// level (a thread per row: the FP64 pipe is narrow, so no row's arithmetic is
-// repeated across lanes), then the CTA barrier makes the level's results
-// visible to the next (no launch per level).
-constexpr int TRI_THREADS = 1024;
+// Every level of one triangular solve in one cooperative launch over all SMs:
+// the rows of a level go round-robin over the blocks first (one row per SM
+// where the level allows, so the narrow FP64 pipes share the work), a thread
+// per row, and a grid barrier separates the levels.
+constexpr int TRI_THREADS = 64;
 template <int KIND, bool FWD>
-__global__ void __launch_bounds__(TRI_THREADS) k_tri_levels(int l0, int l1, const int *__restrict__ lev,
-                                                            const int *__restrict__ rows,
-                                                            const int64_t *__restrict__ ptr,
-                                                            const int *__restrict__ col,
-                                                            const double *__restrict__ val,
-                                                            const double *__restrict__ diag,
-                                                            const double *__restrict__ in, double *out,
-                                                            const PcgScal *sc)
+__global__ void __launch_bounds__(TRI_THREADS) k_tri_coop(int nlev, const int *__restrict__ lev,
+                                                          const int *__restrict__ rows,
+                                                          const int64_t *__restrict__ ptr,
+                                                          const int *__restrict__ col,
+                                                          const double *__restrict__ val,
+                                                          const double *__restrict__ diag,
+                                                          const double *__restrict__ in, double *out,
+                                                          unsigned int *bar, int *status, const PcgScal *sc)
 {
     if (sc && (sc->done || sc->reliable)) return;
-    for (int l = l0; l < l1; ++l) {
-        const int r1 = lev[l + 1];
-        for (int t = lev[l] + threadIdx.x; t < r1; t += TRI_THREADS) tri_row<KIND, FWD>(rows[t], ptr, col, val, diag, in, out);
-        __syncthreads();
+    const int stride = gridDim.x * blockDim.x, q0 = threadIdx.x * gridDim.x + blockIdx.x;
+    for (int l = 0; l < nlev; ++l) {
+        const int r0 = lev[l], w = lev[l + 1] - r0;
+        for (int q = q0; q < w; q += stride) tri_row<KIND, FWD, true>(rows[r0 + q], ptr, col, val, diag, in, out);
+        if (l + 1 < nlev && !grid_wait(bar, bar + 1, status)) return;
     }
 }
 
@@ -170,6 +199,10 @@ int upload_factor(ogb_mtrx *m, int kind, const std::vector<int64_t> &fp, const s
     OGB_CHECK(up(F.brows, brows));
     OGB_CHECK(up(F.d_flev, F.flev));
     OGB_CHECK(up(F.d_blev, F.blev));
+    OGB_CHECK(F.bar.alloc(2));
+    OGB_CHECK(F.status.alloc(1));
+    OGB_CUDA(cudaMemsetAsync(F.bar.p, 0, 2 * sizeof(unsigned int), s));
+    OGB_CUDA(cudaMemsetAsync(F.status.p, 0, sizeof(int), s));
     OGB_CHECK(F.work.alloc(n > 0 ? n : 1));
     OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
     F.n = n;
@@ -362,51 +395,51 @@ int build_ic(ogb_mtrx *m)
     return upload_factor(m, 4, fp, fc, fv, bp, bc, bv, dg);
 }
 
-// Levels wider than this run as their own multi-block launch; runs of narrower
-// levels go to one single-CTA launch.
-constexpr int TRI_WIDE = 4 * TRI_THREADS;
-
 template <int KIND, bool FWD>
-void tri_solve(cudaStream_t s, const std::vector<int> &lev, const int *d_lev, const int *rows, const int64_t *ptr,
-               const int *col, const double *val, const double *diag, const double *in, double *out,
-               const PcgScal *sc, int &launches)
+int tri_solve(cudaStream_t s, const IcFactor &F, bool fwd_data, const double *in, double *out, const PcgScal *sc)
 {
-    const int nl = (int)lev.size() - 1;
-    int l = 0;
-    while (l < nl) {
-        if (lev[l + 1] - lev[l] > TRI_WIDE) {
-            const int r0 = lev[l], r1 = lev[l + 1];
-            k_tri_level<KIND, FWD><<<(unsigned)ceil_div(r1 - r0, NTHREADS), NTHREADS, 0, s>>>(r0, r1, rows, ptr, col,
-                                                                                          val, diag, in, out, sc);
-            ++l;
-        } else {
-            int e = l;
-            while (e < nl && lev[e + 1] - lev[e] <= TRI_WIDE) ++e;
-            k_tri_levels<KIND, FWD><<<1, TRI_THREADS, 0, s>>>(l, e, d_lev, rows, ptr, col, val, diag, in, out, sc);
-            l = e;
-        }
-        ++launches;
-    }
+    const std::vector<int> &lev = fwd_data ? F.flev : F.blev;
+    int nlev = (int)lev.size() - 1;
+    const int *d_lev = fwd_data ? F.d_flev.p : F.d_blev.p;
+    const int *rows = fwd_data ? F.frows.p : F.brows.p;
+    const int64_t *ptr = fwd_data ? F.fptr.p : F.bptr.p;
+    const int *col = fwd_data ? F.fcol.p : F.bcol.p;
+    const double *val = fwd_data ? F.fval.p : F.bval.p;
+    const double *diag = F.diag.p;
+    unsigned int *bar = F.bar.p;
+    int *status = F.status.p;
+    void *args[] = {&nlev, &d_lev, &rows, &ptr, &col, &val, &diag, &in, &out, &bar, &status, &sc};
+    OGB_CUDA(cudaLaunchCooperativeKernel((const void *)k_tri_coop<KIND, FWD>, dim3(num_sms()), dim3(TRI_THREADS), args,
+                                         0, s));
+    return OGB_OK;
 }
 
 int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
 {
     IcFactor &F = m->ic;
     cudaStream_t s = m->ctx->stream;
-    int launches = 0;
     if (F.kind == 2) {
-        tri_solve<2, true>(s, F.flev, F.d_flev.p, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p, sc,
-                           launches);
-        tri_solve<2, false>(s, F.blev, F.d_blev.p, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
-                            sc, launches);
+        OGB_CHECK((tri_solve<2, true>(s, F, true, r, F.work.p, sc)));
+        OGB_CHECK((tri_solve<2, false>(s, F, false, F.work.p, z, sc)));
     } else {
-        tri_solve<4, true>(s, F.flev, F.d_flev.p, F.frows.p, F.fptr.p, F.fcol.p, F.fval.p, F.diag.p, r, F.work.p, sc,
-                           launches);
-        tri_solve<4, false>(s, F.blev, F.d_blev.p, F.brows.p, F.bptr.p, F.bcol.p, F.bval.p, F.diag.p, F.work.p, z,
-                            sc, launches);
+        OGB_CHECK((tri_solve<4, true>(s, F, true, r, F.work.p, sc)));
+        OGB_CHECK((tri_solve<4, false>(s, F, false, F.work.p, z, sc)));
     }
-    count_launch(m->ctx, launches);
+    count_launch(m->ctx, 2);
     OGB_CUDA(cudaGetLastError());
+    return OGB_OK;
+}
+
+// Error status of the level solves since the factor was built (a grid wait
+// that ran out of time).
+int ic_status(ogb_mtrx *m)
+{
+    IcFactor &F = m->ic;
+    if (!F.status.p) return OGB_OK;
+    int h = 0;
+    OGB_CUDA(cudaMemcpyAsync(&h, F.status.p, sizeof(int), cudaMemcpyDeviceToHost, m->ctx->stream));
+    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    if (h) return fail(OGB_E_CUDA, "IC/ILU triangular solve: a grid-wide wait ran out of time");
     return OGB_OK;
 }
 

@@ -1896,9 +1896,9 @@ int pcg_ic_core(ogb_mtrx *m, const Op &op, const double *b, double *x, double rt
     k_ic_init<<<gb, NTHREADS, 0, s>>>(op.n, b, q, r, m->w_part.p, m->w_count.p, sc, rtol);
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
-    // iterations per captured graph: each holds one launch per level of both solves
-    const int per_it = (int)(m->ic.flev.size() + m->ic.blev.size()) + 4;
-    const int nb_it = std::max(1, std::min(BATCH, 8192 / per_it));
+    // iterations per captured graph (two cooperative solve launches and four
+    // vector/SpMV launches each)
+    const int nb_it = BATCH;
     auto batch = [&]() -> int {
         for (int k = 0; k < nb_it; ++k) {
             OGB_CHECK(launch_ic_solve(m, r, z, sc));
@@ -1921,7 +1921,7 @@ int pcg_ic_core(ogb_mtrx *m, const Op &op, const double *b, double *x, double rt
         if (ctx->use_graphs) OGB_CHECK(graph.launch(ctx));
         else OGB_CHECK(batch());
     }
-    return OGB_OK;
+    return ic_status(m);
 }
 
 // Mixed precision with FP64 residual replacement (see file header). X is the

@@ -340,6 +340,25 @@ def test_iml_preconditioners(case, ctx, native_lib, oracle):
         A.set_preconditioner(3)
 
 
+@pytest.mark.parametrize("pc", [4, 2])
+def test_iml_preconditioners_many_levels(pc, native_lib, oracle):
+    """The level-scheduled solves (one cooperative launch per triangular solve,
+    grid barrier between levels) on a mesh with ~150 levels per solve: IC and
+    ILU CG against the oracle's IML CG with the same preconditioner, iterations
+    within one and solutions within 1e-9."""
+    from oofem_gb300 import meshgen as mg
+    mesh = mg.hex_cantilever(20, 4, 4, jitter=0.2, seed=7)
+    c = native_lib.Context(0)
+    model = native_lib.GpuModel(c, mesh)
+    A = native_lib.GpuCsrMtrx(c)
+    A.set_preconditioner(pc)
+    u, reac, info = model.linear_static(A, rtol=1e-10)
+    assert info.status == 0
+    ref = oracle.linear_static(oracle.mesh_dict(mesh), rtol=1e-10, precond=pc)
+    assert abs(info.iterations - ref["iters"]) <= 1, (info.iterations, ref["iters"])
+    assert rel(u, ref["u"]) < 1e-9
+
+
 @pytest.mark.parametrize("kind", ["hex", "quad", "tet"])
 def test_block_jacobi_mixed_solve(kind, native_lib, oracle):
     """Mixed solves preconditioned by the FP32 inverses of the node diagonal
