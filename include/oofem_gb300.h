@@ -147,6 +147,11 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   iteration's beta with a bounded wait). Same arithmetic and sum order as the
  *   two-launch form: bitwise equal iterates. */
 #define OGB_OPT_FUSED_UPDATE 14
+/*   OGB_OPT_BATCH_FORM (0..2, default 0): FP32 SpMV of batched mixed solves:
+ *   1 = values loaded among the products, 2 = every value of a group of blocks
+ *   loaded before the group's products; 0 = timed once per matrix. Bitwise equal
+ *   results. */
+#define OGB_OPT_BATCH_FORM 15
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA

@@ -146,7 +146,9 @@ __device__ __forceinline__ void gather_row(const double *__restrict__ src, doubl
 // alpha for running pairs. DIFF: the FP32 difference form (the diagonal slot
 // holds the block row sum, off-diagonal products act on x_B - x_A). skip: the
 // inst_skip mode (0 = never). Block columns are prefetched one group ahead.
-template <int ND, int NR, bool DOT, class V, class X, bool DIFF>
+// EXPL: all values of a group are loaded before its products (more loads in
+// flight per warp; same products in the same order).
+template <int ND, int NR, bool DOT, class V, class X, bool DIFF, bool EXPL = false>
 __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *__restrict__ sl_ptr,
                                                     const int *__restrict__ sl_width, const int *__restrict__ col,
                                                     const V *__restrict__ val, const X *__restrict__ x,
@@ -195,18 +197,40 @@ __global__ void __launch_bounds__(NTHREADS) k_bspmv(int nslices, const int64_t *
 #pragma unroll
                     for (int j = 0; j < W; ++j) xb[g][j] -= xa[j];
             }
+            if constexpr (EXPL) {
+                // every value of the group loaded before the group's products
+                V vv[G][ND * ND];
 #pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (k0 + g < w) {
-                    const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+                for (int g = 0; g < G; ++g)
 #pragma unroll
-                    for (int i = 0; i < ND; ++i)
+                    for (int q = 0; q < ND * ND; ++q)
+                        vv[g][q] = k0 + g < w ? __ldcs(vp + (int64_t)(k0 + g) * (32 * ND * ND) + 32 * q) : (V)0;
 #pragma unroll
-                        for (int j = 0; j < ND; ++j) {
-                            const V v = __ldcs(vk + 32 * (i * ND + j));
+                for (int g = 0; g < G; ++g) {
+                    if (k0 + g < w) {
 #pragma unroll
-                            for (int c = 0; c < NR; ++c) yy[i][c] = fma(v, xb[g][j * NR + c], yy[i][c]);
-                        }
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j)
+#pragma unroll
+                                for (int c = 0; c < NR; ++c)
+                                    yy[i][c] = fma(vv[g][i * ND + j], xb[g][j * NR + c], yy[i][c]);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (k0 + g < w) {
+                        const V *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
+#pragma unroll
+                        for (int i = 0; i < ND; ++i)
+#pragma unroll
+                            for (int j = 0; j < ND; ++j) {
+                                const V v = __ldcs(vk + 32 * (i * ND + j));
+#pragma unroll
+                                for (int c = 0; c < NR; ++c) yy[i][c] = fma(v, xb[g][j * NR + c], yy[i][c]);
+                            }
+                    }
                 }
             }
         }
@@ -742,15 +766,49 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         const double drop2 = ctx->mixed_drop * ctx->mixed_drop;
         // one iteration: q = K p (FP32), the updates (pairs whose recursive residual
         // dropped by the drop factor pause), p = z + beta p for the running pairs
-        iteration = [&, diff, drop2]() {
-            if (diff)
-                k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(
-                    S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
-                    w.sinst.p, w.sptr.p, 1);
-            else
-                k_bspmv<ND, NR, true, float, float, false><<<nsu, NTHREADS, 0, st>>>(
-                    S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, w.sc.p,
-                    w.sinst.p, w.sptr.p, 1);
+        // FP32 SpMV form, timed once per matrix (the launches recompute q, p.q and
+        // alpha of the same p: no state changes)
+        auto spmv32 = [&, diff](int form) {
+#define OGB_BSPMV_ARGS S.nslices, S.sl_ptr.p, S.sl_width.p, S.col.p, S.v32.p, w.p32.p, w.q32.p, w.part.p, w.cnt.p, \
+                       w.sc.p, w.sinst.p, w.sptr.p, 1
+            if (diff && form == 2) k_bspmv<ND, NR, true, float, float, true, true><<<nsu, NTHREADS, 0, st>>>(OGB_BSPMV_ARGS);
+            else if (diff) k_bspmv<ND, NR, true, float, float, true><<<nsu, NTHREADS, 0, st>>>(OGB_BSPMV_ARGS);
+            else if (form == 2) k_bspmv<ND, NR, true, float, float, false, true><<<nsu, NTHREADS, 0, st>>>(OGB_BSPMV_ARGS);
+            else k_bspmv<ND, NR, true, float, float, false><<<nsu, NTHREADS, 0, st>>>(OGB_BSPMV_ARGS);
+#undef OGB_BSPMV_ARGS
+        };
+        SellMat &Sm = const_cast<SellMat &>(S);
+        if (ctx->batch_form) Sm.bform32 = ctx->batch_form;
+        if (!Sm.bform32) {
+            cudaEvent_t e0, e1;
+            OGB_CUDA(cudaEventCreate(&e0));
+            OGB_CUDA(cudaEventCreate(&e1));
+            float best = 0.f;
+            for (int f = 1; f <= 2; ++f) {
+                spmv32(f);
+                cudaEventRecord(e0, st);
+                for (int k = 0; k < 3; ++k) spmv32(f);
+                cudaEventRecord(e1, st);
+                count_launch(ctx, 4);
+                float ms = 0.f;
+                cudaError_t e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return cuda_fail(e, "batched SpMV autotune");
+                }
+                if (f == 1 || ms < 0.98f * best) {
+                    best = ms;
+                    Sm.bform32 = f;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        const int bform = Sm.bform32;
+        iteration = [&, drop2, bform]() {
+            spmv32(bform);
             k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
                                                       w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, drop2);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);

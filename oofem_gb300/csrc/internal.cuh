@@ -171,6 +171,7 @@ struct SellMat {
     int ninst = 1;          // independent instances (block-diagonal batch)
     int group[2] = {0, 0};  // tuned SpMV variant for FP64 / FP32 values (0 = not yet)
     int force_split = 0;    // warps per slice forced by OGB_OPT_SPMV_VARIANT 5 / 6 (0 = rule)
+    int bform32 = 0;        // batched FP32 SpMV form timed for this matrix: 1 plain, 2 values of a group first
     std::vector<int64_t> inst_row_base;   // first node-space row of each instance (+ total)
     HalfSell half;                        // half-stored FP32 copy (built on first use)
     int64_t nns() const { return (int64_t)nslices * 32 * nd; }
@@ -238,6 +239,7 @@ struct ogb_ctx {
     int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix
     int upd_bps = 0;            // blocks per SM of the block-Jacobi update and p update (0 = its occupancy)
     bool fused_update = true;   // block-Jacobi update and p update in one cooperative launch
+    int batch_form = 0;         // batched FP32 SpMV form forced (1, 2) or 0 = timed per matrix
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner

@@ -676,6 +676,7 @@ int build_sell(ogb_model *md, ogb_mtrx *m)
     SellMat &S = m->sell;
     S.nd = nd;
     S.group[0] = S.group[1] = 0;   // the SpMV autotuner runs again for the new structure
+    S.bform32 = 0;
     S.half.reset();                 // and the half-stored copy is rebuilt on first use
     DBuf<int64_t> flag;
     OGB_CHECK(flag.alloc(nn + 1));

@@ -96,6 +96,31 @@ def test_batch_is_deterministic(ctx, native_lib):
     assert np.array_equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("kind", ["quad", "tet"])
+def test_batched_spmv_forms_are_bitwise_equal(kind, native_lib):
+    """Batched mixed solves with the FP32 SpMV values loaded among the products
+    (form 1) or every value of a group loaded first (form 2), and timed (0):
+    the same sums in the same order, bitwise equal solutions."""
+    from oofem_gb300 import meshgen as mg
+    if kind == "quad":
+        meshes = mg.rve_batch(4, seed=5, side_min=8, side_max=40)
+        big, ns = mg.concat_meshes(meshes)
+        bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
+    else:
+        meshes = [mg.tet_cube_linear(6, jitter=0.1, seed=s) for s in (1, 2)]
+        big, ns = mg.concat_meshes(meshes)
+        bcv = big.bc_value[None]
+    out = {}
+    for form in (1, 2, 0):
+        c = native_lib.Context(0)
+        c.set_option(native_lib.OPT_BATCH_FORM, form)
+        model = native_lib.GpuModel(c, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(c)
+        out[form] = model.batch_linear_static(A, bcv, rtol=1e-9, precision=native_lib.PREC_MIXED)[0]
+    assert np.array_equal(out[1], out[2]) and np.array_equal(out[1], out[0])
+
+
 def test_set_instances_rejects_coupled_and_late(ctx, native_lib):
     from oofem_gb300 import meshgen as mg
     m = mg.quad_rve(6, seed=1)
