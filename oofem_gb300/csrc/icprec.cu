@@ -16,10 +16,10 @@
 // columns and a backward solve by columns. On the device both run by rows,
 // level by level: row i's forward value needs the rows c < i of its transposed
 // column entries, its backward value the rows r > i of its own column. Each
-// solve is one cooperative launch over all SMs that steps through the levels
-// with a grid barrier between them (rows of a level spread over the SMs, a
-// thread per row, each row's entries loaded in chunks of eight before their
-// differences). The products are accumulated in
+// solve is one launch of one thread-block cluster that steps through the levels
+// with the cluster barrier between them (rows of a level spread over the
+// cluster's SMs, a thread per row, each row's entries loaded in chunks before
+// their differences). The products are accumulated in
 // the reference's order (columns resp. rows ascending, starting from zero) with
 // separate rounded multiply and subtract, so z = M^-1 r is bitwise the
 // reference's.
@@ -56,7 +56,7 @@ __device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, 
     double acc = (KIND == 2 && !FWD) ? in[i] : 0.0;
     // the entries of a chunk are loaded before the chunk's differences, which
     // keep the stored order
-    constexpr int CH = 8;
+    constexpr int CH = 16;
     int64_t e = ptr[i];
     const int64_t e1 = ptr[i + 1];
     for (; e + CH <= e1; e += CH) {
@@ -78,66 +78,31 @@ __device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, 
     else out[i] = __ddiv_rn(acc, diag[i]);
 }
 
-// Grid-wide barrier of the cooperative level solve: the last block to arrive
-// resets the count and advances the epoch; the others wait for the advance.
-// The wait is bounded (about a second): past it, or once another block has
-// given up, the block sets *status and the caller returns.
-__device__ __forceinline__ bool grid_wait(unsigned int *count, unsigned int *epoch, int *status)
-{
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        const unsigned int e0 = *(volatile unsigned int *)epoch;
-        __threadfence();
-        const unsigned int t = atomicAdd(count, 1u);
-        if (t == gridDim.x - 1) {
-            *(volatile unsigned int *)count = 0u;
-            __threadfence();
-            atomicAdd(epoch, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*(volatile unsigned int *)epoch == e0) {
-                if (*(volatile int *)status) {
-                    ok = 0;
-                    break;
-                }
-                if (clock64() - t0 > 2000000000LL) {
-                    atomicCAS(status, 0, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// Every level of one triangular solve in one cooperative launch over all SMs:
-// the rows of a level go round-robin over the blocks first (one row per SM
-// where the level allows, so the narrow FP64 pipes share the work), a thread
-// per row, and a grid barrier separates the levels.
-constexpr int TRI_THREADS = 64;
+// Every level of one triangular solve in one launch of one thread-block
+// cluster (TRI_CLUSTER CTAs on as many SMs): the rows of a level go round-robin
+// over the CTAs first (the narrow FP64 pipes of several SMs share the work), a
+// thread per row, and the cluster's hardware barrier (release / acquire at
+// cluster scope) separates the levels; out[] is read from L2, where the other
+// SMs' stores of the previous levels are.
+constexpr int TRI_THREADS = 256;
+constexpr int TRI_CLUSTER = 8;
 template <int KIND, bool FWD>
-__global__ void __launch_bounds__(TRI_THREADS) k_tri_coop(int nlev, const int *__restrict__ lev,
-                                                          const int *__restrict__ rows,
-                                                          const int64_t *__restrict__ ptr,
-                                                          const int *__restrict__ col,
-                                                          const double *__restrict__ val,
-                                                          const double *__restrict__ diag,
-                                                          const double *__restrict__ in, double *out,
-                                                          unsigned int *bar, int *status, const PcgScal *sc)
+__global__ void __launch_bounds__(TRI_THREADS) k_tri_cluster(int nlev, const int *__restrict__ lev,
+                                                             const int *__restrict__ rows,
+                                                             const int64_t *__restrict__ ptr,
+                                                             const int *__restrict__ col,
+                                                             const double *__restrict__ val,
+                                                             const double *__restrict__ diag,
+                                                             const double *__restrict__ in, double *out,
+                                                             const PcgScal *sc)
 {
-    if (sc && (sc->done || sc->reliable)) return;
-    const int stride = gridDim.x * blockDim.x, q0 = threadIdx.x * gridDim.x + blockIdx.x;
+    if (sc && (sc->done || sc->reliable)) return;   // the same for every CTA of the cluster
+    const int stride = TRI_CLUSTER * TRI_THREADS, q0 = threadIdx.x * TRI_CLUSTER + (int)blockIdx.x;
     for (int l = 0; l < nlev; ++l) {
         const int r0 = lev[l], w = lev[l + 1] - r0;
         for (int q = q0; q < w; q += stride) tri_row<KIND, FWD, true>(rows[r0 + q], ptr, col, val, diag, in, out);
-        if (l + 1 < nlev && !grid_wait(bar, bar + 1, status)) return;
+        asm volatile("barrier.cluster.arrive.release.aligned;\n"
+                     "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
     }
 }
 
@@ -199,10 +164,6 @@ int upload_factor(ogb_mtrx *m, int kind, const std::vector<int64_t> &fp, const s
     OGB_CHECK(up(F.brows, brows));
     OGB_CHECK(up(F.d_flev, F.flev));
     OGB_CHECK(up(F.d_blev, F.blev));
-    OGB_CHECK(F.bar.alloc(2));
-    OGB_CHECK(F.status.alloc(1));
-    OGB_CUDA(cudaMemsetAsync(F.bar.p, 0, 2 * sizeof(unsigned int), s));
-    OGB_CUDA(cudaMemsetAsync(F.status.p, 0, sizeof(int), s));
     OGB_CHECK(F.work.alloc(n > 0 ? n : 1));
     OGB_CUDA(cudaStreamSynchronize(s));   // the host arrays are freed on return
     F.n = n;
@@ -399,18 +360,24 @@ template <int KIND, bool FWD>
 int tri_solve(cudaStream_t s, const IcFactor &F, bool fwd_data, const double *in, double *out, const PcgScal *sc)
 {
     const std::vector<int> &lev = fwd_data ? F.flev : F.blev;
-    int nlev = (int)lev.size() - 1;
-    const int *d_lev = fwd_data ? F.d_flev.p : F.d_blev.p;
-    const int *rows = fwd_data ? F.frows.p : F.brows.p;
-    const int64_t *ptr = fwd_data ? F.fptr.p : F.bptr.p;
-    const int *col = fwd_data ? F.fcol.p : F.bcol.p;
-    const double *val = fwd_data ? F.fval.p : F.bval.p;
-    const double *diag = F.diag.p;
-    unsigned int *bar = F.bar.p;
-    int *status = F.status.p;
-    void *args[] = {&nlev, &d_lev, &rows, &ptr, &col, &val, &diag, &in, &out, &bar, &status, &sc};
-    OGB_CUDA(cudaLaunchCooperativeKernel((const void *)k_tri_coop<KIND, FWD>, dim3(num_sms()), dim3(TRI_THREADS), args,
-                                         0, s));
+    const int nlev = (int)lev.size() - 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(TRI_CLUSTER);
+    cfg.blockDim = dim3(TRI_THREADS);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = TRI_CLUSTER;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    OGB_CUDA(cudaLaunchKernelEx(&cfg, k_tri_cluster<KIND, FWD>, nlev, (const int *)(fwd_data ? F.d_flev.p : F.d_blev.p),
+                                (const int *)(fwd_data ? F.frows.p : F.brows.p),
+                                (const int64_t *)(fwd_data ? F.fptr.p : F.bptr.p),
+                                (const int *)(fwd_data ? F.fcol.p : F.bcol.p),
+                                (const double *)(fwd_data ? F.fval.p : F.bval.p), (const double *)F.diag.p, in, out,
+                                sc));
     return OGB_OK;
 }
 
@@ -427,19 +394,6 @@ int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc)
     }
     count_launch(m->ctx, 2);
     OGB_CUDA(cudaGetLastError());
-    return OGB_OK;
-}
-
-// Error status of the level solves since the factor was built (a grid wait
-// that ran out of time).
-int ic_status(ogb_mtrx *m)
-{
-    IcFactor &F = m->ic;
-    if (!F.status.p) return OGB_OK;
-    int h = 0;
-    OGB_CUDA(cudaMemcpyAsync(&h, F.status.p, sizeof(int), cudaMemcpyDeviceToHost, m->ctx->stream));
-    OGB_CUDA(cudaStreamSynchronize(m->ctx->stream));
-    if (h) return fail(OGB_E_CUDA, "IC/ILU triangular solve: a grid-wide wait ran out of time");
     return OGB_OK;
 }
 

@@ -189,8 +189,6 @@ struct IcFactor {
     DBuf<double> fval, bval, diag, work;
     std::vector<int> flev, blev;   // level starts into frows / brows
     DBuf<int> d_flev, d_blev;      // the same on the device
-    DBuf<unsigned int> bar;        // grid barrier of the level solves: count, epoch
-    DBuf<int> status;              // nonzero: a grid wait ran out of time
 };
 
 // LDL^T factor of the direct solver (direct.cu): dense band of n x (bw+1)
@@ -378,7 +376,6 @@ int build_half(ogb_ctx *ctx, SellMat &S);
 // (device, level-scheduled; kernels skip once sc reports done).
 int build_ic(ogb_mtrx *m);
 int launch_ic_solve(ogb_mtrx *m, const double *r, double *z, const PcgScal *sc);
-int ic_status(ogb_mtrx *m);
 int refresh_half(ogb_ctx *ctx, SellMat &S);
 
 // element.cu

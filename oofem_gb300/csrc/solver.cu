@@ -1896,8 +1896,8 @@ int pcg_ic_core(ogb_mtrx *m, const Op &op, const double *b, double *x, double rt
     k_ic_init<<<gb, NTHREADS, 0, s>>>(op.n, b, q, r, m->w_part.p, m->w_count.p, sc, rtol);
     count_launch(ctx);
     OGB_CUDA(cudaGetLastError());
-    // iterations per captured graph (two cooperative solve launches and four
-    // vector/SpMV launches each)
+    // iterations per captured graph (two cluster launches for the triangular
+    // solves and four vector/SpMV launches each)
     const int nb_it = BATCH;
     auto batch = [&]() -> int {
         for (int k = 0; k < nb_it; ++k) {
@@ -1921,7 +1921,7 @@ int pcg_ic_core(ogb_mtrx *m, const Op &op, const double *b, double *x, double rt
         if (ctx->use_graphs) OGB_CHECK(graph.launch(ctx));
         else OGB_CHECK(batch());
     }
-    return ic_status(m);
+    return OGB_OK;
 }
 
 // Mixed precision with FP64 residual replacement (see file header). X is the
