@@ -83,9 +83,13 @@ __device__ __forceinline__ void tri_row(int i, const int64_t *__restrict__ ptr, 
 // over the CTAs first (the narrow FP64 pipes of several SMs share the work), a
 // thread per row, and the cluster's hardware barrier (release / acquire at
 // cluster scope) separates the levels; out[] is read from L2, where the other
-// SMs' stores of the previous levels are.
+// SMs' stores of the previous levels are. What a row needs besides out[] (its
+// index, entry range, first TRI_PRE columns and values, in_i, d_i) is loaded
+// before the barrier that precedes its level, so after the barrier a row costs
+// one round of out[] loads and its chain of differences.
 constexpr int TRI_THREADS = 256;
 constexpr int TRI_CLUSTER = 8;
+constexpr int TRI_PRE = 40;
 template <int KIND, bool FWD>
 __global__ void __launch_bounds__(TRI_THREADS) k_tri_cluster(int nlev, const int *__restrict__ lev,
                                                              const int *__restrict__ rows,
@@ -98,9 +102,47 @@ __global__ void __launch_bounds__(TRI_THREADS) k_tri_cluster(int nlev, const int
 {
     if (sc && (sc->done || sc->reliable)) return;   // the same for every CTA of the cluster
     const int stride = TRI_CLUSTER * TRI_THREADS, q0 = threadIdx.x * TRI_CLUSTER + (int)blockIdx.x;
-    for (int l = 0; l < nlev; ++l) {
+    int row = -1;
+    int64_t e0 = 0, e1 = 0;
+    int cc[TRI_PRE];
+    double vv[TRI_PRE];
+    double xin = 0.0, dg = 1.0;
+    auto fetch = [&](int l) {
+        row = -1;
+        if (l >= nlev) return;
         const int r0 = lev[l], w = lev[l + 1] - r0;
-        for (int q = q0; q < w; q += stride) tri_row<KIND, FWD, true>(rows[r0 + q], ptr, col, val, diag, in, out);
+        if (q0 >= w) return;
+        row = rows[r0 + q0];
+        e0 = ptr[row];
+        e1 = ptr[row + 1];
+#pragma unroll
+        for (int k = 0; k < TRI_PRE; ++k) {
+            cc[k] = e0 + k < e1 ? col[e0 + k] : 0;
+            vv[k] = e0 + k < e1 ? val[e0 + k] : 0.0;
+        }
+        xin = in[row];
+        dg = (KIND == 4 || !FWD) ? diag[row] : 1.0;
+    };
+    fetch(0);
+    for (int l = 0; l < nlev; ++l) {
+        if (row >= 0) {
+            double acc = (KIND == 2 && !FWD) ? xin : 0.0;
+            const int n = (int)min(e1 - e0, (int64_t)TRI_PRE);
+            double oo[TRI_PRE];
+#pragma unroll
+            for (int k = 0; k < TRI_PRE; ++k) oo[k] = k < n ? __ldcg(out + cc[k]) : 0.0;
+#pragma unroll
+            for (int k = 0; k < TRI_PRE; ++k)
+                if (k < n) acc = __dsub_rn(acc, __dmul_rn(vv[k], oo[k]));
+            for (int64_t e = e0 + TRI_PRE; e < e1; ++e) acc = __dsub_rn(acc, __dmul_rn(val[e], __ldcg(out + col[e])));
+            if (KIND == 4) out[row] = __ddiv_rn(__dadd_rn(xin, acc), dg);
+            else if (FWD) out[row] = __dadd_rn(acc, xin);
+            else out[row] = __ddiv_rn(acc, dg);
+        }
+        // rows of a level wider than the cluster's threads
+        const int r0 = lev[l], w = lev[l + 1] - r0;
+        for (int q = q0 + stride; q < w; q += stride) tri_row<KIND, FWD, true>(rows[r0 + q], ptr, col, val, diag, in, out);
+        fetch(l + 1);
         asm volatile("barrier.cluster.arrive.release.aligned;\n"
                      "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
     }
