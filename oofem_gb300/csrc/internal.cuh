@@ -232,6 +232,7 @@ struct ogb_ctx {
     bool mixed_orth = false;    // restore r.p = 0 after a residual replacement
     bool mixed_p32 = false;     // mixed solve keeps p and q = K p in FP32 (x, r, z FP64)
     bool mixed_x64 = true;      // with FP32 vectors: update the FP64 solution directly
+    bool mixed_sum32 = false;   // ... with the update's dot-product terms summed per thread in FP32
     int spmv_group = 0;         // SELL SpMV loop variant forced (1..4) or 0 = tuned per matrix
     int spmv_half = 1;          // half-stored FP32 copy in mixed solves: 0 never, 1 one-warp-per-slice matrices, 2 always
     int half_form = 0;          // half-stored SpMV form forced (1..3) or 0 = timed per matrix

@@ -835,7 +835,7 @@ __global__ void __launch_bounds__(NTHREADS) k_update_rz32(int64_t n, double *__r
 // bounded: past about a second the block sets done = 5 and returns.
 constexpr int DONE_WAIT_TIMEOUT = 5;
 
-template <int ND, class XS, bool FUSE, int UNR = 2>
+template <int ND, class XS, bool FUSE, bool SUM32 = (sizeof(XS) == 4), int UNR = 2>
 __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__restrict__ x,
                                                           float *__restrict__ r, float *__restrict__ z,
                                                           float *__restrict__ p, const float *__restrict__ q,
@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__
     block_range(nnodes, lo, hi);
     const bool zsm = FUSE && hi - lo <= zcap;
     double v[2] = {0.0, 0.0};
-    float vf[2] = {0.f, 0.f};   // FP32 increment form: the thread's sums in FP32 (no FP64 work per node)
+    float vf[2] = {0.f, 0.f};   // SUM32: the thread's sums in FP32 (no FP64 work per node for them)
     for (int64_t a0 = lo + threadIdx.x; a0 < hi; a0 += (int64_t)UNR * NTHREADS) {
         float rr[UNR][ND], bb[UNR][NSYM], pp[UNR][ND];
         XS xx[UNR][ND];
@@ -891,7 +891,7 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__
                 s0 = fmaf(rr[u][d], rr[u][d], s0);
                 s1 = fmaf(rr[u][d], zz, s1);
             }
-            if constexpr (sizeof(XS) == 8) {
+            if constexpr (!SUM32) {
                 v[0] += (double)s0;
                 v[1] += (double)s1;
             } else {
@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(NTHREADS) k_update_bj32(int64_t nnodes, XS *__
             }
         }
     }
-    if constexpr (sizeof(XS) == 4) {
+    if constexpr (SUM32) {
         v[0] = (double)vf[0];
         v[1] = (double)vf[1];
     }
@@ -946,15 +946,21 @@ __global__ void __launch_bounds__(NTHREADS) k_pupdate_f32(int64_t n, const float
     for (int64_t row = lo + threadIdx.x; row < hi; row += NTHREADS) p[row] = fmaf(zc, z[row], beta * p[row]);
 }
 
-// The block-Jacobi update of a node size, solution type and form.
-const void *bj_update_fn(int nd, bool x64, bool fuse)
+// The block-Jacobi update of a node size, solution accumulation and form:
+// mode 1 = FP64 solution with FP64 sums per node, 2 = FP64 solution with FP32
+// sums per thread, 0 = FP32 increment (FP32 sums per thread).
+template <int ND>
+const void *bj_update_nd(int mode, bool fuse)
 {
-    if (nd == 3) {
-        if (x64) return fuse ? (const void *)k_update_bj32<3, double, true> : (const void *)k_update_bj32<3, double, false>;
-        return fuse ? (const void *)k_update_bj32<3, float, true> : (const void *)k_update_bj32<3, float, false>;
-    }
-    if (x64) return fuse ? (const void *)k_update_bj32<2, double, true> : (const void *)k_update_bj32<2, double, false>;
-    return fuse ? (const void *)k_update_bj32<2, float, true> : (const void *)k_update_bj32<2, float, false>;
+    if (mode == 1) return fuse ? (const void *)k_update_bj32<ND, double, true> : (const void *)k_update_bj32<ND, double, false>;
+    if (mode == 2)
+        return fuse ? (const void *)k_update_bj32<ND, double, true, true> : (const void *)k_update_bj32<ND, double, false, true>;
+    return fuse ? (const void *)k_update_bj32<ND, float, true> : (const void *)k_update_bj32<ND, float, false>;
+}
+
+const void *bj_update_fn(int nd, int mode, bool fuse)
+{
+    return nd == 3 ? bj_update_nd<3>(mode, fuse) : bj_update_nd<2>(mode, fuse);
 }
 
 // Launch of bj_update_fn's kernel; xs is the FP64 solution or the FP32 increment
@@ -1941,7 +1947,7 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // each block takes an equal contiguous share of the nodes
     // (the fused form is a cooperative launch: at most its occupancy per SM)
     const bool fuse = ctx->fused_update && op.sell;
-    const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64, fuse) : nullptr;
+    const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64 ? (ctx->mixed_sum32 ? 2 : 1) : 0, fuse) : nullptr;
     int upd_bps = ctx->upd_bps;
     if (op.sell) {
         int occ = 0;
