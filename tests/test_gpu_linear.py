@@ -409,15 +409,16 @@ def mixed_solve(native_lib, mesh, rtol, **opts):
 def test_fused_update_and_fp32_increment(kind, native_lib, oracle):
     """The block-Jacobi update with the p update in the same cooperative launch
     gives bitwise the iterates of the two-launch form (same sums, same order) in
-    one launch fewer per iteration; with the solution accumulated as an FP32
-    increment folded into the FP64 solution at each residual replacement the
-    solve still converges on the FP64 residual to the oracle's solution."""
+    one launch fewer per iteration; with the update's dot-product terms summed
+    per thread in FP32, or the solution accumulated as an FP32 increment folded
+    into the FP64 solution after every batch of iterations, the solve still
+    converges on the FP64 residual to the oracle's solution."""
     from oofem_gb300 import meshgen as mg
     mesh = {"hex": lambda: mg.hex_cantilever(30, 6, 6, jitter=0.2, seed=4),
             "quad": lambda: mg.quad_rve(40, seed=6),
             "tet": lambda: mg.tet_cube_linear(8, jitter=0.1, seed=2)}[kind]()
     ref = oracle.linear_static(oracle.mesh_dict(mesh), rtol=1e-13)
-    for x64 in (1, 0):
+    for x64 in (1, 2, 0):
         it0, u0, l0 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=0)
         it1, u1, l1 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=1)
         assert it0 == it1 and np.array_equal(u0, u1), (x64, it0, it1)
