@@ -428,6 +428,49 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
     }
 }
 
+// Block Jacobi for two DOFs per node: node a's 2 x 2 diagonal block inverted in
+// FP64, row d of the inverse stored (FP32) with node row 2a + d. The blocks of
+// prescribed DOFs hold a unit diagonal with zeroed couplings (identity rows).
+__global__ void k_bbinv2(int nrows, const int64_t *__restrict__ diag, const double *__restrict__ val,
+                         float2 *__restrict__ binv, int *zero_diag)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nrows) return;
+    const int64_t slot = diag[a];
+    const int r = (int)(slot & 31);
+    const double *vb = val + (slot - r) * 4 + r;
+    const double d00 = vb[0], d01 = vb[32], d10 = vb[64], d11 = vb[96];
+    const double det = d00 * d11 - d01 * d10;
+    if (!(det != 0.0) || !isfinite(det)) {
+        atomicExch(zero_diag, 1);
+        binv[2 * (int64_t)a] = make_float2(0.f, 0.f);
+        binv[2 * (int64_t)a + 1] = make_float2(0.f, 0.f);
+        return;
+    }
+    const double inv = 1.0 / det;
+    binv[2 * (int64_t)a] = make_float2((float)(d11 * inv), (float)(-d01 * inv));
+    binv[2 * (int64_t)a + 1] = make_float2((float)(-d10 * inv), (float)(d00 * inv));
+}
+
+// z of one row from the preconditioner: the scalar inverse diagonal, or (BJ2)
+// the row of its node's 2 x 2 block inverse applied to the node's two residual
+// entries (the partner row is the neighbouring lane: node rows 2a, 2a + 1 sit
+// on an even and the following odd lane). Called by every lane of the warp.
+template <bool BJ2>
+__device__ __forceinline__ float bprecond(float rf, const float *__restrict__ dinv, const float2 *__restrict__ binv,
+                                         int64_t row)
+{
+    if constexpr (!BJ2) {
+        return rf * dinv[row];
+    } else {
+        const float ro = __shfl_xor_sync(0xffffffffu, rf, 1);
+        const bool odd = row & 1;
+        const float r0 = odd ? ro : rf, r1 = odd ? rf : ro;
+        const float2 b = binv[row];
+        return fmaf(b.y, r1, b.x * r0);
+    }
+}
+
 // ---- mixed precision: FP32 matrix (difference form) and FP32 r, z, p, q per
 // pair, FP64 solution x. A pair whose recursive residual has dropped by the drop
 // factor since its last replacement, or reached half the tolerance, or the
@@ -445,9 +488,10 @@ __global__ void k_bdiag(int nrows, const int64_t *__restrict__ diag, const doubl
 // init) for the pending p = z + beta p (k_bpupdate32 in replacement mode).
 // Pairs that are still running are left alone: their p already holds this
 // iteration's update, so replacing their r and z would break the recurrence.
-template <int NR>
+template <int NR, bool BJ2 = false>
 __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict__ b, const double *__restrict__ q64,
-                                                       const float *__restrict__ dinv, float *__restrict__ r,
+                                                       const float *__restrict__ dinv,
+                                                       const float2 *__restrict__ binv, float *__restrict__ r,
                                                        float *__restrict__ z, double *part, unsigned int *cnt,
                                                        BatchScal *sc, const int *__restrict__ unit_inst,
                                                        const int64_t *__restrict__ unit_ptr, double rtol, int maxit,
@@ -468,15 +512,14 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
-        const float di = dinv[row];
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
-            if (!live[c]) continue;
+            if (!live[c]) continue;   // the same for the whole warp (one instance)
             const int64_t k = row * NR + c;
             const double bb = b[k];
             const double r6 = bb - q64[k];
             const float rf = (float)r6;
-            const float zf = rf * di;
+            const float zf = bprecond<BJ2>(rf, dinv, binv, row);
             r[k] = rf;
             z[k] = zf;
             v[c] += bb * bb;
@@ -532,10 +575,11 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
 // x64 += alpha p, r -= alpha q, z = D^-1 r for running pairs (FP32 but x);
 // per pair ||r||^2 and r.z (FP32 per thread and warp, FP64 above), the pause
 // test and beta.
-template <int NR>
+template <int NR, bool BJ2 = false>
 __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, float *__restrict__ r,
                                                         float *__restrict__ z, const float *__restrict__ p,
                                                         const float *__restrict__ q, const float *__restrict__ dinv,
+                                                        const float2 *__restrict__ binv,
                                                         double *part, unsigned int *cnt, BatchScal *sc,
                                                         const int *__restrict__ unit_inst,
                                                         const int64_t *__restrict__ unit_ptr, double rtol, int maxit,
@@ -557,15 +601,14 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         const int64_t row = (int64_t)blockIdx.x * UNIT + j * NTHREADS + threadIdx.x;
-        const float di = dinv[row];
 #pragma unroll
         for (int c = 0; c < NR; ++c) {
-            if (!run[c]) continue;
+            if (!run[c]) continue;   // the same for the whole warp (one instance)
             const int64_t k = row * NR + c;
             const float pp = p[k];
             x[k] = fma(alpha[c], (double)pp, x[k]);
             const float rr = fmaf(-(float)alpha[c], q[k], r[k]);
-            const float zz = rr * di;
+            const float zz = bprecond<BJ2>(rr, dinv, binv, row);
             r[k] = rr;
             z[k] = zz;
             v[c] = fmaf(rr, rr, v[c]);
@@ -663,6 +706,7 @@ struct BatchWork {
     DBuf<BatchScal> sc;
     DBuf<double> part, r, z, p, q, dinv, q64;
     DBuf<float> r32, z32, p32, q32, dinv32;
+    DBuf<float2> binv2;   // block Jacobi rows (two DOFs per node)
     DBuf<unsigned int> cnt;
 };
 
@@ -754,13 +798,30 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             w.sptr.p, skip);
     };
     std::function<void()> iteration;
+    // mixed preconditioner: FP32 block Jacobi of the 2 x 2 node blocks (two DOFs
+    // per node) where the option allows it, else the scalar diagonal
+    const bool bj2 = mixed && ND == 2 && ctx->mixed_bj;
+    auto replace = [&, bj2](int init) {
+        if (bj2)
+            k_breplace<NR, true><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.binv2.p, w.r32.p, w.z32.p,
+                                                           w.part.p, w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit,
+                                                           init);
+        else
+            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, nullptr, w.r32.p, w.z32.p, w.part.p,
+                                                     w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, init);
+    };
     if (mixed) {
-        k_bdiag<ND, float><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv32.p, w.zero.p);
+        m->last_bj = bj2;
+        if (bj2) {
+            OGB_CHECK(w.binv2.alloc(nrows));
+            k_bbinv2<<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.binv2.p, w.zero.p);
+        } else {
+            k_bdiag<ND, float><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv32.p, w.zero.p);
+        }
         residual_spmv(w.q64.p, 2);
         // p starts at zero: the init pass's p = z + 0 p is z
         OGB_CUDA(cudaMemsetAsync(w.p32.p, 0, nv * sizeof(float), st));
-        k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p, w.sc.p,
-                                                 w.vinst.p, w.vptr.p, rtol, maxit, 1);
+        replace(1);
         k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
         const bool diff = ctx->mixed_diff;
         const double drop2 = ctx->mixed_drop * ctx->mixed_drop;
@@ -807,10 +868,16 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             cudaEventDestroy(e1);
         }
         const int bform = Sm.bform32;
-        iteration = [&, drop2, bform]() {
+        iteration = [&, drop2, bform, bj2]() {
             spmv32(bform);
-            k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, w.part.p,
-                                                      w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, drop2);
+            if (bj2)
+                k_bupdate32<NR, true><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p,
+                                                                w.binv2.p, w.part.p, w.cnt.p, w.sc.p, w.vinst.p,
+                                                                w.vptr.p, rtol, maxit, drop2);
+            else
+                k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, nullptr,
+                                                          w.part.p, w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit,
+                                                          drop2);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);
         };
     } else {
@@ -852,8 +919,7 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             // iterations (instances without one skip every kernel): residual, r, z,
             // beta, and their p = z + beta p
             residual_spmv(w.q64.p, 3);
-            k_breplace<NR><<<nvu, NTHREADS, 0, st>>>(b, w.q64.p, w.dinv32.p, w.r32.p, w.z32.p, w.part.p, w.cnt.p,
-                                                     w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit, 0);
+            replace(0);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 1);
             count_launch(ctx, 3);
             OGB_CUDA(cudaGetLastError());
