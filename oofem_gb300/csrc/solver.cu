@@ -40,7 +40,6 @@ namespace ogb {
 namespace {
 
 constexpr int GRID_MULT = 8;   // blocks per SM for the vector kernels
-constexpr double RELIABLE_DROP = 0.1;
 
 __device__ __forceinline__ bool halted(const PcgScal *sc) { return sc->done || sc->reliable; }
 
@@ -407,56 +406,10 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_init(int nchunks, const double
     }
 }
 
-// FP64 drop-in update (x += alpha p etc.) with the IML convergence test.
-template <class X>
-__global__ void __launch_bounds__(NTHREADS) k_pcg_update(int nchunks, X *__restrict__ x, X *__restrict__ r,
-                                                         X *__restrict__ z, const X *__restrict__ p,
-                                                         const X *__restrict__ q, const X *__restrict__ dinv,
-                                                         double *part, unsigned int *count, PcgScal *sc, double rtol,
-                                                         int maxit)
-{
-    if (halted(sc)) return;
-    const X alpha = (X)sc->alpha;
-    double v[2] = {0, 0};
-    for (int c = blockIdx.x; c < nchunks; c += gridDim.x)
-        for (int i = threadIdx.x; i < CHUNK; i += NTHREADS) {
-            int row = c * CHUNK + i;
-            x[row] += alpha * p[row];
-            X rr = r[row] - alpha * q[row];
-            X zz = rr * dinv[row];
-            r[row] = rr;
-            z[row] = zz;
-            v[0] += (double)rr * (double)rr;
-            v[1] += (double)rr * (double)zz;
-        }
-    block_sum<2>(v);
-    if (publish_partials<2>(v, part, count)) {
-        double t[2];
-        final_sums<2>(part, t);
-        if (threadIdx.x != 0) return;
-        *count = 0;
-        sc->rnorm2 = t[0];
-        sc->iters += 1;
-        double normb = sqrt(sc->bnorm2);
-        if (normb == 0.0) normb = 1.0;
-        if (sqrt(t[0]) / normb <= rtol) {
-            sc->done = 1;
-        } else if (!isfinite(t[1]) || !(t[1] > 0.0)) {
-            sc->done = 2;
-        } else if (sc->iters >= maxit) {
-            sc->done = 4;
-        } else {
-            sc->beta = t[1] / sc->rho;
-            sc->rho_old = sc->rho;
-            sc->rho = t[1];
-            sc->zcoef = 1.0;
-        }
-    }
-}
-
 // Mixed update: d += alpha p (FP32 increment), r -= alpha q, z = D^-1 r. Asks
-// for an FP64 residual replacement once ||r|| fell by RELIABLE_DROP since the
-// last one or below the tolerance; then rho is left for the replacement.
+// for an FP64 residual replacement once ||r||^2 fell below drop2 times its value
+// at the last one (the context's drop factor, squared) or below the tolerance;
+// then rho is left for the replacement.
 template <class X, class P>
 __global__ void __launch_bounds__(NTHREADS) k_mixed_update(int nchunks, X *__restrict__ d, X *__restrict__ r,
                                                            X *__restrict__ z, const P *__restrict__ p,
