@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // products (with G = 3 at 4 blocks per SM the loads of three blocks are in
 // flight together: the fastest form on the 3M-DOF cantilever). The sums and
 // their order depend on neither: the forms give bitwise equal results.
-template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false, bool PF = false>
+template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false>
 __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
                                                         const float *__restrict__ val, const int64_t *__restrict__ ptrL,
@@ -245,21 +245,7 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
             int cn[G];
 #pragma unroll
             for (int g = 0; g < G; ++g) cn[g] = g < w ? __ldcs(cp + 32 * g) : arow;
-            // PF: the value lines of a group are prefetched into L1 one group ahead
-            // (no registers held while in flight) and then read through L1
-            auto prefetch_group = [&](int k) {
-#pragma unroll
-                for (int g = 0; g < G; ++g)
-                    if (k + g < w) {
-                        const float *vk = vp + (int64_t)(k + g) * (32 * ND * ND);
-#pragma unroll
-                        for (int q = 0; q < ND * ND; ++q)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(vk + 32 * q));
-                    }
-            };
-            if constexpr (PF) prefetch_group(0);
             for (int k0 = 0; k0 < w; k0 += G) {
-                if constexpr (PF) prefetch_group(k0 + G);
                 int cc[G];
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
@@ -281,8 +267,7 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                     for (int g = 0; g < G; ++g) {
                         const float *vk = vp + (int64_t)(k0 + g) * (32 * ND * ND);
 #pragma unroll
-                        for (int q = 0; q < ND * ND; ++q)
-                            v[g][q] = k0 + g < w ? (PF ? __ldca(vk + 32 * q) : __ldcg(vk + 32 * q)) : 0.f;
+                        for (int q = 0; q < ND * ND; ++q) v[g][q] = k0 + g < w ? __ldcg(vk + 32 * q) : 0.f;
                     }
 #pragma unroll
                     for (int g = 0; g < G; ++g) {
@@ -1511,9 +1496,6 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 5) k_half_spmv<ND, X, DIFF, 3, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 6) k_half_spmv<ND, X, DIFF, 2, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 7) k_half_spmv<ND, X, DIFF, 3, 4, true, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 8) k_half_spmv<ND, X, DIFF, 2, 5, true, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 9) k_half_spmv<ND, X, DIFF, 4, 3, true, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
