@@ -867,10 +867,10 @@ def main():
     ap.add_argument("--rve-count", type=int, default=256)
     ap.add_argument("--spmv-variant", type=int, default=0,
                     help="profiling only: force a node-block SpMV form (OGB_OPT_SPMV_VARIANT)")
-    ap.add_argument("--mixed-x64", type=int, default=-1, choices=(-1, 0, 1, 2),
+    ap.add_argument("--mixed-x64", type=int, default=-1, choices=(-1, 0, 1, 2, 3),
                     help="single mixed solves: 1 accumulate the solution in FP64 every iteration (2: with the "
-                         "update's dot-product terms summed per thread in FP32), 0 as an FP32 increment folded "
-                         "after every batch of iterations (OGB_OPT_MIXED_X64; -1 = library default)")
+                         "update's dot-product terms summed per thread in FP32), 0 / 3 as an FP32 increment folded "
+                         "after every batch of iterations (3: FP64 sums) (OGB_OPT_MIXED_X64; -1 = library default)")
     ap.add_argument("--block-jacobi", type=int, default=-1, choices=(-1, 0, 1),
                     help="mixed solves: 1 block-Jacobi, 0 scalar Jacobi preconditioner "
                          "(OGB_OPT_MIXED_BLOCK_JACOBI; -1 = library default)")

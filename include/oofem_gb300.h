@@ -92,12 +92,13 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 #define OGB_OPT_MIXED_DROP_PPM 4
 /*   OGB_OPT_MIXED_P32 (0/1): mixed solves keep p and q = K p in FP32 only. */
 #define OGB_OPT_MIXED_P32 5
-/*   OGB_OPT_MIXED_X64 (0/1/2): with FP32 vectors, accumulate the solution in
+/*   OGB_OPT_MIXED_X64 (0..3): with FP32 vectors, accumulate the solution in
  *   FP64 every iteration (1; 2: the same with the update's r.r and r.z terms
  *   summed per thread in FP32 before the FP64 block sums), or as an FP32
  *   increment folded into the FP64 solution after every 16 iterations and at
- *   each residual replacement (0). Single-matrix solves only: batched solves
- *   always accumulate in FP64. */
+ *   each residual replacement (0: terms summed per thread in FP32; 3: summed
+ *   per node in FP64). Single-matrix solves only: batched solves always
+ *   accumulate in FP64. */
 #define OGB_OPT_MIXED_X64 6
 /*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
  *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 = values and columns

@@ -371,9 +371,9 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
     case OGB_OPT_MIXED_ORTH: ctx->mixed_orth = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_P32: ctx->mixed_p32 = value != 0; return OGB_OK;
     case OGB_OPT_MIXED_X64:
-        if (value < 0 || value > 2) return fail(OGB_E_ARG, "OGB_OPT_MIXED_X64 must be 0, 1 or 2");
-        ctx->mixed_x64 = value != 0;
-        ctx->mixed_sum32 = value == 2;
+        if (value < 0 || value > 3) return fail(OGB_E_ARG, "OGB_OPT_MIXED_X64 must be 0, 1, 2 or 3");
+        ctx->mixed_x64 = value == 1 || value == 2;
+        ctx->mixed_sum32 = value == 0 || value == 2;
         return OGB_OK;
     case OGB_OPT_SPMV_VARIANT:
         if (value < 0 || value > 6) return fail(OGB_E_ARG, "SpMV variant must be 0 (tuned) or 1..6");

@@ -901,13 +901,16 @@ __global__ void __launch_bounds__(NTHREADS) k_pupdate_f32(int64_t n, const float
 
 // The block-Jacobi update of a node size, solution accumulation and form:
 // mode 1 = FP64 solution with FP64 sums per node, 2 = FP64 solution with FP32
-// sums per thread, 0 = FP32 increment (FP32 sums per thread).
+// sums per thread, 0 = FP32 increment with FP32 sums per thread, 3 = FP32
+// increment with FP64 sums per node.
 template <int ND>
 const void *bj_update_nd(int mode, bool fuse)
 {
     if (mode == 1) return fuse ? (const void *)k_update_bj32<ND, double, true> : (const void *)k_update_bj32<ND, double, false>;
     if (mode == 2)
         return fuse ? (const void *)k_update_bj32<ND, double, true, true> : (const void *)k_update_bj32<ND, double, false, true>;
+    if (mode == 3)
+        return fuse ? (const void *)k_update_bj32<ND, float, true, false> : (const void *)k_update_bj32<ND, float, false, false>;
     return fuse ? (const void *)k_update_bj32<ND, float, true> : (const void *)k_update_bj32<ND, float, false>;
 }
 
@@ -1900,7 +1903,8 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     // each block takes an equal contiguous share of the nodes
     // (the fused form is a cooperative launch: at most its occupancy per SM)
     const bool fuse = ctx->fused_update && op.sell;
-    const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64 ? (ctx->mixed_sum32 ? 2 : 1) : 0, fuse) : nullptr;
+    const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64 ? (ctx->mixed_sum32 ? 2 : 1) : (ctx->mixed_sum32 ? 0 : 3), fuse)
+                              : nullptr;
     int upd_bps = ctx->upd_bps;
     if (op.sell) {
         int occ = 0;

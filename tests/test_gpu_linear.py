@@ -418,7 +418,7 @@ def test_fused_update_and_fp32_increment(kind, native_lib, oracle):
             "quad": lambda: mg.quad_rve(40, seed=6),
             "tet": lambda: mg.tet_cube_linear(8, jitter=0.1, seed=2)}[kind]()
     ref = oracle.linear_static(oracle.mesh_dict(mesh), rtol=1e-13)
-    for x64 in (1, 2, 0):
+    for x64 in (1, 2, 0, 3):
         it0, u0, l0 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=0)
         it1, u1, l1 = mixed_solve(native_lib, mesh, 1e-10, mixed_x64=x64, fused_update=1)
         assert it0 == it1 and np.array_equal(u0, u1), (x64, it0, it1)
