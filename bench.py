@@ -133,6 +133,8 @@ def apply_options(ctx):
         ctx.set_option(native.OPT_UPDATE_BLOCKS, ARGS.update_blocks)
     if ARGS is not None and ARGS.fused_update >= 0:
         ctx.set_option(native.OPT_FUSED_UPDATE, ARGS.fused_update)
+    if ARGS is not None and ARGS.batch_x64 >= 0:
+        ctx.set_option(native.OPT_BATCH_X64, ARGS.batch_x64)
 
 
 def profile_traffic(form: int):
@@ -880,6 +882,9 @@ def main():
     ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 7)),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
+    ap.add_argument("--batch-x64", type=int, default=-1, choices=(-1, 0, 1),
+                    help="batched mixed solves: 1 FP64 solution every iteration, 0 FP32 increment folded after "
+                         "every batch of iterations (OGB_OPT_BATCH_X64; -1 = library default)")
     ap.add_argument("--fused-update", type=int, default=-1, choices=(-1, 0, 1),
                     help="block-Jacobi update and p update in one cooperative launch "
                          "(OGB_OPT_FUSED_UPDATE; -1 = library default)")

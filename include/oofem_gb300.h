@@ -155,6 +155,10 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   loaded before the group's products; 0 = timed once per matrix. Bitwise equal
  *   results. */
 #define OGB_OPT_BATCH_FORM 15
+/*   OGB_OPT_BATCH_X64 (0/1, default 1): batched mixed solves accumulate the
+ *   solution in FP64 every iteration (1) or as an FP32 increment folded into
+ *   the FP64 solution after every 16 iterations (0). */
+#define OGB_OPT_BATCH_X64 16
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)
  * are bracketed by CUDA events on the context stream -- every launch outside CUDA

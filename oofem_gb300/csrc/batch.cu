@@ -21,6 +21,8 @@
 #include <functional>
 #include <vector>
 
+#include <memory>
+
 #include "internal.cuh"
 #include "reduce.cuh"
 
@@ -575,8 +577,8 @@ __global__ void __launch_bounds__(NTHREADS) k_breplace(const double *__restrict_
 // x64 += alpha p, r -= alpha q, z = D^-1 r for running pairs (FP32 but x);
 // per pair ||r||^2 and r.z (FP32 per thread and warp, FP64 above), the pause
 // test and beta.
-template <int NR, bool BJ2 = false>
-__global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, float *__restrict__ r,
+template <int NR, bool BJ2 = false, class XS = double>
+__global__ void __launch_bounds__(NTHREADS) k_bupdate32(XS *__restrict__ x, float *__restrict__ r,
                                                         float *__restrict__ z, const float *__restrict__ p,
                                                         const float *__restrict__ q, const float *__restrict__ dinv,
                                                         const float2 *__restrict__ binv,
@@ -606,7 +608,8 @@ __global__ void __launch_bounds__(NTHREADS) k_bupdate32(double *__restrict__ x, 
             if (!run[c]) continue;   // the same for the whole warp (one instance)
             const int64_t k = row * NR + c;
             const float pp = p[k];
-            x[k] = fma(alpha[c], (double)pp, x[k]);
+            if constexpr (sizeof(XS) == 8) x[k] = fma(alpha[c], (double)pp, x[k]);
+            else x[k] = fmaf((float)alpha[c], pp, x[k]);   // FP32 increment of the current batch
             const float rr = fmaf(-(float)alpha[c], q[k], r[k]);
             const float zz = bprecond<BJ2>(rr, dinv, binv, row);
             r[k] = rr;
@@ -675,6 +678,16 @@ __global__ void __launch_bounds__(NTHREADS) k_bpupdate32(const float *__restrict
     }
 }
 
+// x64 += d, d = 0: the FP32 increment of a batch of iterations folded into the
+// FP64 solution.
+__global__ void k_bfold(int64_t n, double *__restrict__ x, float *__restrict__ d)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += (double)d[i];
+        d[i] = 0.f;
+    }
+}
+
 // x = 0 for the pairs that ended stalled with a residual above their starting
 // one (or not finite): their FP64 pass must not start from diverged iterates.
 template <int NR>
@@ -707,6 +720,7 @@ struct BatchWork {
     DBuf<double> part, r, z, p, q, dinv, q64;
     DBuf<float> r32, z32, p32, q32, dinv32;
     DBuf<float2> binv2;   // block Jacobi rows (two DOFs per node)
+    DBuf<float> d32;      // FP32 solution increment of the current batch (batch_x64 off)
     DBuf<unsigned int> cnt;
 };
 
@@ -868,17 +882,35 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
             cudaEventDestroy(e1);
         }
         const int bform = Sm.bform32;
-        iteration = [&, drop2, bform, bj2]() {
+        // solution accumulation: FP64 every iteration, or an FP32 increment folded
+        // into the FP64 solution after every batch of BBATCH iterations (before any
+        // FP64 residual replacement reads x)
+        const bool x64 = ctx->batch_x64;
+        if (!x64) {
+            OGB_CHECK(w.d32.alloc(nv));
+            OGB_CUDA(cudaMemsetAsync(w.d32.p, 0, nv * sizeof(float), st));
+        }
+        auto calls = std::make_shared<int>(0);
+        iteration = [&, drop2, bform, bj2, x64, calls]() {
             spmv32(bform);
-            if (bj2)
+            if (bj2 && x64)
                 k_bupdate32<NR, true><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p,
                                                                 w.binv2.p, w.part.p, w.cnt.p, w.sc.p, w.vinst.p,
                                                                 w.vptr.p, rtol, maxit, drop2);
-            else
+            else if (bj2)
+                k_bupdate32<NR, true, float><<<nvu, NTHREADS, 0, st>>>(w.d32.p, w.r32.p, w.z32.p, w.p32.p, w.q32.p,
+                                                                       w.dinv32.p, w.binv2.p, w.part.p, w.cnt.p, w.sc.p,
+                                                                       w.vinst.p, w.vptr.p, rtol, maxit, drop2);
+            else if (x64)
                 k_bupdate32<NR><<<nvu, NTHREADS, 0, st>>>(x, w.r32.p, w.z32.p, w.p32.p, w.q32.p, w.dinv32.p, nullptr,
                                                           w.part.p, w.cnt.p, w.sc.p, w.vinst.p, w.vptr.p, rtol, maxit,
                                                           drop2);
+            else
+                k_bupdate32<NR, false, float><<<nvu, NTHREADS, 0, st>>>(w.d32.p, w.r32.p, w.z32.p, w.p32.p, w.q32.p,
+                                                                        w.dinv32.p, nullptr, w.part.p, w.cnt.p, w.sc.p,
+                                                                        w.vinst.p, w.vptr.p, rtol, maxit, drop2);
             k_bpupdate32<NR><<<nvu, NTHREADS, 0, st>>>(w.z32.p, w.p32.p, w.sc.p, w.vinst.p, 0);
+            if (!x64 && ++*calls % BBATCH == 0) k_bfold<<<num_sms() * 4, NTHREADS, 0, st>>>(nv, x, w.d32.p);
         };
     } else {
         k_bdiag<ND, double><<<gd, NTHREADS, 0, st>>>(nr, S.diag.p, S.v64.p, w.dinv.p, w.zero.p);
@@ -930,7 +962,7 @@ int run_batch(ogb_mtrx *m, const double *b, double *x, double rtol, int maxit, b
         } else {
             for (int k = 0; k < BBATCH; ++k) iteration();
         }
-        count_launch(ctx, 3 * BBATCH);
+        count_launch(ctx, 3 * BBATCH + (mixed && !ctx->batch_x64 ? 1 : 0));
         OGB_CUDA(cudaGetLastError());
         it += BBATCH;
     }

@@ -394,6 +394,7 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->half_form = (int)value;
         return OGB_OK;
     case OGB_OPT_FUSED_UPDATE: ctx->fused_update = value != 0; return OGB_OK;
+    case OGB_OPT_BATCH_X64: ctx->batch_x64 = value != 0; return OGB_OK;
     case OGB_OPT_BATCH_FORM:
         if (value < 0 || value > 2) return fail(OGB_E_ARG, "batched SpMV form must be 0 (timed), 1 or 2");
         ctx->batch_form = (int)value;

@@ -41,6 +41,7 @@ OPT_UPDATE_BLOCKS = 13
 OPT_TANGENT_TC = 11
 OPT_FUSED_UPDATE = 14
 OPT_BATCH_FORM = 15
+OPT_BATCH_X64 = 16
 # linear solver types (the reference's lstype numbers)
 LS_DIRECT = 0
 LS_IML = 1
