@@ -97,8 +97,8 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   summed per thread in FP32 before the FP64 block sums), or as an FP32
  *   increment folded into the FP64 solution after every 16 iterations and at
  *   each residual replacement (0: terms summed per thread in FP32; 3: summed
- *   per node in FP64). Single-matrix solves only: batched solves always
- *   accumulate in FP64. */
+ *   per node in FP64). Single-matrix solves only (batched solves: see
+ *   OGB_OPT_BATCH_X64). */
 #define OGB_OPT_MIXED_X64 6
 /*   OGB_OPT_SPMV_VARIANT: node-block SpMV form, 1 = plain unrolled loop,
  *   2 / 3 = block columns loaded 1 / 4 blocks ahead, 4 = values and columns
@@ -155,9 +155,10 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
  *   loaded before the group's products; 0 = timed once per matrix. Bitwise equal
  *   results. */
 #define OGB_OPT_BATCH_FORM 15
-/*   OGB_OPT_BATCH_X64 (0/1, default 1): batched mixed solves accumulate the
+/*   OGB_OPT_BATCH_X64 (0/1, default 0): batched mixed solves accumulate the
  *   solution in FP64 every iteration (1) or as an FP32 increment folded into
- *   the FP64 solution after every 16 iterations (0). */
+ *   the FP64 solution after every 16 iterations (0: 24 fewer bytes per row and
+ *   no FP64 work per iteration; the same iteration counts on the RVE batch). */
 #define OGB_OPT_BATCH_X64 16
 OGB_API int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value);
 /* Kernel timing: when enabled, SpMV launches (the dominant kernel of the solve)

@@ -239,7 +239,7 @@ struct ogb_ctx {
     int upd_bps = 0;            // blocks per SM of the block-Jacobi update and p update (0 = its occupancy)
     bool fused_update = true;   // block-Jacobi update and p update in one cooperative launch
     int batch_form = 0;         // batched FP32 SpMV form forced (1, 2) or 0 = timed per matrix
-    bool batch_x64 = true;      // batched mixed solves: FP64 solution every iteration (else FP32 increment per batch)
+    bool batch_x64 = false;     // batched mixed solves: FP64 solution every iteration (else FP32 increment per batch)
     int spmv_split = 0;         // warps per slice forced (1, 2, 4) or 0 = the slice-count rule
     double mixed_drop = 0.1;    // residual drop between FP64 replacements
     bool mixed_bj = true;       // mixed solves on node-block operators: block-Jacobi preconditioner

@@ -154,8 +154,9 @@ def test_batched_block_jacobi(native_lib):
 
 def test_batched_fp32_increment(native_lib):
     """Batched mixed solves with the solution accumulated as an FP32 increment
-    folded into the FP64 solution after every batch of iterations converge on the
-    FP64 residual to the FP64 batched solution."""
+    folded into the FP64 solution after every batch of iterations (the default)
+    or in FP64 every iteration converge on the FP64 residual to the FP64 batched
+    solution."""
     from oofem_gb300 import meshgen as mg
     meshes = mg.rve_batch(4, seed=3, side_min=8, side_max=40)
     big, ns = mg.concat_meshes(meshes)
@@ -165,14 +166,15 @@ def test_batched_fp32_increment(native_lib):
     model.set_instances(ns)
     A = native_lib.GpuCsrMtrx(c)
     ref = model.batch_linear_static(A, bcv, rtol=1e-10)[0]
-    c = native_lib.Context(0)
-    c.set_option(native_lib.OPT_BATCH_X64, 0)
-    model = native_lib.GpuModel(c, big)
-    model.set_instances(ns)
-    A = native_lib.GpuCsrMtrx(c)
-    u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-9, precision=native_lib.PREC_MIXED)
-    assert (st == 0).all() and (ach <= 1e-9).all()
-    assert rel(u, ref) < 1e-6, rel(u, ref)
+    for x64 in (0, 1):
+        c = native_lib.Context(0)
+        c.set_option(native_lib.OPT_BATCH_X64, x64)
+        model = native_lib.GpuModel(c, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(c)
+        u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-9, precision=native_lib.PREC_MIXED)
+        assert (st == 0).all() and (ach <= 1e-9).all()
+        assert rel(u, ref) < 1e-6, (x64, rel(u, ref))
 
 
 def test_set_instances_rejects_coupled_and_late(ctx, native_lib):
