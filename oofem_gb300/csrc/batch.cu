@@ -16,6 +16,11 @@
 // instance's partials in a fixed order and updates its pairs' scalars. Sums do
 // not depend on block scheduling (bitwise reproducible, no floating-point
 // atomics), and the per-instance epilogues run in parallel across the grid.
+//
+// Mixed precision (FP32 matrix and vectors, FP64 residual replacements) keeps
+// the solution as an FP32 increment of the current batch of captured
+// iterations, folded into the FP64 solution after each batch, and, for two DOFs
+// per node, preconditions with the 2 x 2 node-block inverses.
 #include <math.h>
 
 #include <functional>
