@@ -48,9 +48,11 @@ def test_mixed_matches_fp64_and_is_reproducible(full, native_lib):
     u2, r2, i2 = model.linear_static(A, rtol=1e-10, maxit=200000, precision=native_lib.PREC_MIXED)
     assert i1.status == 0 and i1.achieved <= 1e-10
     assert np.array_equal(u1, u2) and i1.iterations == i2.iterations
+    # displacements and reactions within 1e-8 of the FP64 drop-in's (both solves
+    # to ||f - K u|| / ||f|| <= 1e-10 on the FP64 residual)
     scale = np.abs(full["u64"]).max()
-    assert np.abs(u1 - full["u64"]).max() / scale < 1e-5
-    assert np.abs(r1 - full["r64"]).max() / np.abs(full["r64"]).max() < 1e-5
+    assert np.abs(u1 - full["u64"]).max() / scale < 1e-8
+    assert np.abs(r1 - full["r64"]).max() / np.abs(full["r64"]).max() < 1e-8
 
 
 def test_linearity_in_the_load(full, native_lib):
