@@ -26,10 +26,14 @@
 // residual has dropped by a factor 10 (or reached the tolerance) it is replaced
 // by the true FP64 residual r = b - A64 x64, keeping the search direction
 // (reliable updates), so x converges to the solution of the FP64 system;
-// convergence is decided on that FP64 residual. Accumulating x itself in FP32
-// between replacements (OGB_OPT_MIXED_X64 0) or an FP32 operator not in
-// difference form (OGB_OPT_MIXED_DIFF 0) triples the iteration count on the
-// ill-conditioned cantilever; both stay selectable for study.
+// convergence is decided on that FP64 residual. On node-block matrices the
+// SpMV reads the half-stored FP32 copy (halfsell.cu), the preconditioner is the
+// FP32 block Jacobi of the node blocks, and the update and p update are one
+// cooperative launch. An FP32 operator not in difference form
+// (OGB_OPT_MIXED_DIFF 0) triples the iteration count on the ill-conditioned
+// cantilever; accumulating x as an FP32 increment (OGB_OPT_MIXED_X64 0 / 3,
+// folded after every batch of iterations) makes an iteration cheaper but the
+// solve a few per cent longer there; both stay selectable.
 #include <math.h>
 
 #include "internal.cuh"
