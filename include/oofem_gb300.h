@@ -131,7 +131,8 @@ OGB_API int64_t ogb_ctx_kernel_launches(ogb_ctx *ctx);
 #define OGB_OPT_HALF_FORM 12
 /*   OGB_OPT_UPDATE_BLOCKS (0..8, default 0): blocks per SM of the block-Jacobi
  *   vector update of mixed solves; 0 = one wave of the kernel's resident blocks
- *   (its occupancy). */
+ *   (its occupancy), fewer when that would leave a block fewer than about 2,048
+ *   nodes. */
 #define OGB_OPT_UPDATE_BLOCKS 13
 /*   OGB_OPT_TANGENT_TC (0/1/2, default 0): element tangents of mixed-precision
  *   Newton steps (ogb_nonlinear_step, ogb_batch_nonlinear_step with

@@ -1909,13 +1909,19 @@ int pcg_mixed_core(ogb_mtrx *m, const Op &op, const double *v64, const float *v3
     const bool fuse = ctx->fused_update && op.sell;
     const void *ufn = op.sell ? bj_update_fn(op.S->nd, ctx->mixed_x64 ? (ctx->mixed_sum32 ? 2 : 1) : (ctx->mixed_sum32 ? 0 : 3), fuse)
                               : nullptr;
+    // (at most the occupancy, and no more blocks per SM than give each block about
+    // 2,048 nodes: below that the per-block reductions and the grid-wide wait
+    // outweigh the bandwidth of more blocks)
     int upd_bps = ctx->upd_bps;
     if (op.sell) {
         int occ = 0;
         const cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ufn, NTHREADS, 0);
         if (oe != cudaSuccess) return cuda_fail(oe, "occupancy of the block-Jacobi update");
         if (occ < 1) occ = 1;
-        if (!upd_bps) upd_bps = occ > 8 ? 8 : occ;
+        if (!upd_bps) {
+            const int64_t by_size = (op.n / op.S->nd) / ((int64_t)num_sms() * 2048);
+            upd_bps = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(occ, 8), by_size));
+        }
         if (fuse && upd_bps > occ) upd_bps = occ;
     }
     const int gu = upd_bps ? (nch < num_sms() * upd_bps ? nch : num_sms() * upd_bps) : gb;
