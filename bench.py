@@ -44,9 +44,7 @@ HALF_FORMS = {1: "groups of 8 blocks, registers for 4 blocks per SM (64)",
               3: "groups of 8 blocks, registers for 2 blocks per SM (128)",
               4: "values of 4 blocks loaded before their products, 3 blocks per SM (80)",
               5: "values of 3 blocks loaded before their products, 4 blocks per SM (64)",
-              6: "values of 2 blocks loaded before their products, 5 blocks per SM (48)",
-              7: "values of 3 upper / 4 lower blocks loaded before their products, 4 blocks per SM (64)",
-              8: "values of 3 upper / 2 lower blocks loaded before their products, 4 blocks per SM (64)"}
+              6: "values of 2 blocks loaded before their products, 5 blocks per SM (48)"}
 WORKLOAD = dict(nx=290, ny=58, nz=58, h=0.05, jitter=0.2, seed=0)
 RTOL = 1e-8
 
@@ -881,7 +879,7 @@ def main():
     ap.add_argument("--tangent-tc", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="mixed Newton tangents: 0 FP64 CUDA cores, 1 tensor cores, 2 the faster "
                          "(OGB_OPT_TANGENT_TC; -1 = library default)")
-    ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 9)),
+    ap.add_argument("--half-form", type=int, default=-1, choices=tuple(range(-1, 7)),
                     help="half-stored SpMV loop form (OGB_OPT_HALF_FORM; -1 = library default, timed)")
     ap.add_argument("--update-blocks", type=int, default=-1, help="OGB_OPT_UPDATE_BLOCKS (-1 = library default)")
     ap.add_argument("--batch-x64", type=int, default=-1, choices=(-1, 0, 1),

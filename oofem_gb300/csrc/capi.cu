@@ -390,7 +390,7 @@ int ogb_ctx_set_option(ogb_ctx *ctx, int option, int64_t value)
         ctx->upd_bps = (int)value;
         return OGB_OK;
     case OGB_OPT_HALF_FORM:
-        if (value < 0 || value > 8) return fail(OGB_E_ARG, "half-stored SpMV form must be 0 (timed) or 1..8");
+        if (value < 0 || value > 6) return fail(OGB_E_ARG, "half-stored SpMV form must be 0 (timed) or 1..6");
         ctx->half_form = (int)value;
         return OGB_OK;
     case OGB_OPT_FUSED_UPDATE: ctx->fused_update = value != 0; return OGB_OK;

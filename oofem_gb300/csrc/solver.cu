@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(NTHREADS) k_sell_spmv(int nslices, const int64
 // products (with G = 3 at 4 blocks per SM the loads of three blocks are in
 // flight together: the fastest form on the 3M-DOF cantilever). The sums and
 // their order depend on neither: the forms give bitwise equal results.
-template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false, int GL = G>
+template <int ND, class X, bool DIFF, int G, int MINB = 4, bool EXPL = false>
 __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const int64_t *__restrict__ ptrU,
                                                         const int *__restrict__ wU, const int *__restrict__ colU,
                                                         const float *__restrict__ val, const int64_t *__restrict__ ptrL,
@@ -300,20 +300,20 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
             const int64_t base = ptrL[s];
             const int w = wL[s];
             const int *lp = low + base + r;
-            int en[GL];
+            int en[G];
 #pragma unroll
-            for (int g = 0; g < GL; ++g) en[g] = g < w ? __ldcs(lp + 32 * g) : -1;
-            for (int k0 = 0; k0 < w; k0 += GL) {
-                int e[GL];
+            for (int g = 0; g < G; ++g) en[g] = g < w ? __ldcs(lp + 32 * g) : -1;
+            for (int k0 = 0; k0 < w; k0 += G) {
+                int e[G];
 #pragma unroll
-                for (int g = 0; g < GL; ++g) {
+                for (int g = 0; g < G; ++g) {
                     e[g] = en[g];
-                    en[g] = k0 + GL + g < w ? __ldcs(lp + 32 * (k0 + GL + g)) : -1;
+                    en[g] = k0 + G + g < w ? __ldcs(lp + 32 * (k0 + G + g)) : -1;
                 }
-                const float *vk[GL];
-                float xb[GL][ND];
+                const float *vk[G];
+                float xb[G][ND];
 #pragma unroll
-                for (int g = 0; g < GL; ++g) {
+                for (int g = 0; g < G; ++g) {
                     const int c = e[g] >= 0 ? (e[g] >> 6) : arow;
                     const int kk = e[g] >= 0 ? (e[g] & 63) : 0;
                     vk[g] = val + (__ldg(ptrU + (c >> 5)) + 32 * (int64_t)kk) * (ND * ND) + (c & 31);
@@ -323,13 +323,13 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                         if (DIFF) xb[g][j] -= xa[j];
                 }
                 if constexpr (EXPL) {
-                    float v[GL][ND * ND];
+                    float v[G][ND * ND];
 #pragma unroll
-                    for (int g = 0; g < GL; ++g)
+                    for (int g = 0; g < G; ++g)
 #pragma unroll
                         for (int q = 0; q < ND * ND; ++q) v[g][q] = e[g] >= 0 ? __ldcs(vk[g] + 32 * q) : 0.f;
 #pragma unroll
-                    for (int g = 0; g < GL; ++g) {
+                    for (int g = 0; g < G; ++g) {
                         if (e[g] >= 0) {
 #pragma unroll
                             for (int i = 0; i < ND; ++i)
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(NTHREADS, MINB) k_half_spmv(int nslices, const
                     }
                 } else {
 #pragma unroll
-                    for (int g = 0; g < GL; ++g) {
+                    for (int g = 0; g < G; ++g) {
                         if (e[g] >= 0) {
 #pragma unroll
                             for (int i = 0; i < ND; ++i)
@@ -1503,8 +1503,6 @@ int launch_half(cudaStream_t s, int form, const SellMat &S, const X *x, X *y, do
     else if (form == 4) k_half_spmv<ND, X, DIFF, 4, 3, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 5) k_half_spmv<ND, X, DIFF, 3, 4, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else if (form == 6) k_half_spmv<ND, X, DIFF, 2, 5, true><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 7) k_half_spmv<ND, X, DIFF, 3, 4, true, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
-    else if (form == 8) k_half_spmv<ND, X, DIFF, 3, 4, true, 2><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
     else k_half_spmv<ND, X, DIFF, 8, 4><<<grid, NTHREADS, 0, s>>>(OGB_HALF_ARGS);
 #undef OGB_HALF_ARGS
     return OGB_OK;
