@@ -461,3 +461,17 @@ def test_half_stored_forms_are_bitwise_equal(kind, native_lib):
         out[f] = (u, info.iterations)
     for f in (2, 3, 4, 5, 6, 0):
         assert np.array_equal(out[f][0], out[1][0]) and out[f][1] == out[1][1]
+
+
+def test_option_ranges_are_checked(native_lib):
+    """Tuning options outside their documented ranges are refused with OGB_E_ARG
+    and leave the context usable."""
+    c = native_lib.Context(0)
+    for opt, bad in ((native_lib.OPT_HALF_FORM, 7), (native_lib.OPT_MIXED_X64, 4), (native_lib.OPT_BATCH_FORM, 3),
+                     (native_lib.OPT_UPDATE_BLOCKS, 9), (native_lib.OPT_SPMV_HALF, 3), (native_lib.OPT_TANGENT_TC, 3)):
+        with pytest.raises(native_lib.OgbError) as e:
+            c.set_option(opt, bad)
+        assert e.value.code == -1, (opt, e.value.code)
+    for opt, good in ((native_lib.OPT_HALF_FORM, 6), (native_lib.OPT_MIXED_X64, 3), (native_lib.OPT_BATCH_FORM, 2),
+                      (native_lib.OPT_UPDATE_BLOCKS, 8), (native_lib.OPT_FUSED_UPDATE, 0), (native_lib.OPT_BATCH_X64, 1)):
+        c.set_option(opt, good)
