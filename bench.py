@@ -409,6 +409,25 @@ def run_gpu(args):
         e2e_s = (time.perf_counter() - t0) / n_e2e
     if not args.no_e2e:
         e2e_s = replicas.max_over_ranks(e2e_s)
+    # where the end-to-end time goes: one more call, outside the timed runs, with the host
+    # clock read after each phase (every phase below returns with its work finished)
+    phases = None
+    if not args.no_e2e:
+        t = [time.perf_counter()]
+        c2 = native.Context(local)
+        t.append(time.perf_counter())
+        m2 = native.GpuModel(c2, mesh_h)
+        A2 = native.GpuCsrMtrx(c2)
+        c2.synchronize()
+        t.append(time.perf_counter())
+        m2.linear_static(A2, rtol=RTOL, maxit=200000, precision=native.PREC_MIXED, out=out_h)
+        t.append(time.perf_counter())
+        A2.close()
+        m2.close()
+        c2.close()
+        t.append(time.perf_counter())
+        phases = {k: (t[i + 1] - t[i]) * 1e3 for i, k in enumerate(
+            ("context", "mesh_upload", "assemble_solve_copy_back", "release"))}
     h2d = (mesh.coords.nbytes + mesh.conn.nbytes + mesh.elem_mat.nbytes + mesh.material_table().nbytes
            + mesh.bc_mask.nbytes + mesh.bc_value.nbytes + mesh.nodal_load.nbytes)
     d2h = 2 * mesh.bc_value.nbytes
@@ -464,7 +483,7 @@ def run_gpu(args):
         "clocks": clk,
         "gpu_launches": int(launches),
         "e2e": {"value": ws * nfree / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "seconds": e2e_s},
+                "d2h_bytes_per_step": int(d2h), "seconds": e2e_s, "phases_ms": phases},
         "cpu_baseline": cb,
     }
     print(json.dumps(out))
