@@ -152,6 +152,34 @@ def test_batched_block_jacobi(native_lib):
     assert tot[1] <= 1.05 * tot[0], tot
 
 
+def test_batched_kernel_timing_keeps_the_solve(native_lib):
+    """With kernel timing on, a batched mixed solve times one more SpMV launch
+    (every pair running), which recomputes q, p.q and alpha of the same search
+    directions: the solution is bitwise that of the untimed solve, and the
+    sample is reported with its time and algorithmic bytes."""
+    from oofem_gb300 import meshgen as mg
+    meshes = mg.rve_batch(3, seed=7, side_min=8, side_max=32)
+    big, ns = mg.concat_meshes(meshes)
+    bcv = np.stack([np.concatenate([mg.rve_bc_values(m, lc) for m in meshes]) for lc in range(3)])
+    out = []
+    for prof in (False, True):
+        c = native_lib.Context(0)
+        c.set_option(native_lib.OPT_BATCH_FORM, 1)
+        if prof:
+            c.profile(True)
+            c.profile_read()
+        model = native_lib.GpuModel(c, big)
+        model.set_instances(ns)
+        A = native_lib.GpuCsrMtrx(c)
+        u, reac, its, ach, st = model.batch_linear_static(A, bcv, rtol=1e-9, precision=native_lib.PREC_MIXED)
+        assert (st == 0).all()
+        out.append(u)
+        if prof:
+            ms, n, by = c.profile_read()
+            assert n == 1 and ms > 0 and by > 0, (ms, n, by)
+    assert np.array_equal(out[0], out[1])
+
+
 def test_batched_fp32_increment(native_lib):
     """Batched mixed solves with the solution accumulated as an FP32 increment
     folded into the FP64 solution after every batch of iterations (the default)
