@@ -1,7 +1,8 @@
 /*
  * CPU oracle for the OOFEM structural hot path -- TEST INFRASTRUCTURE ONLY.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
- * and only as the checker / the timed CPU reference; the product never calls it.
+ * and only as the reference results are compared with / the timed CPU
+ * baseline; the product never calls it.
  *
  * Each function restates one piece of the reference algorithm and cites the
  * reference file:line it follows (paths relative to the OOFEM source tree).

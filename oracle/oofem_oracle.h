@@ -2,7 +2,8 @@
  * CPU oracle for the OOFEM structural hot path -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference algorithm, used by the test suite,
- * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, as the reference
+ * the GPU results are compared with.
  * The product (liboofem_gb300.so) never links, loads or calls anything here.
  *
  * Parity pin: this restatement is checked against golden vectors produced by
