@@ -4,9 +4,10 @@ Workload (one step): the 290x58x58 LSpace hex cantilever (h = 0.05 m, interior
 nodes jittered +-0.2h, seed 0; E = 210e9, nu = 0.3; x = 0 face fixed; 1e5 N in
 -z over the x = L face), 3,028,470 free DOFs. A step is the LinearStatic
 sequence on the GPU: element stiffness + deterministic assembly, load vector
-(f_ext - f_int of the prescribed field), mixed-precision Jacobi-PCG with FP64
-iterative refinement to ||f - K u||/||f|| <= 1e-8 (FP64 residual), solution
-scatter and reactions. value = free DOFs / step time (DOF/s).
+(f_ext - f_int of the prescribed field), mixed-precision PCG (half-stored FP32
+operator, FP32 block Jacobi) with FP64 residual replacements to
+||f - K u||/||f|| <= 1e-8 (FP64 residual), solution scatter and reactions; the
+FP64 drop-in solve is timed beside it. value = free DOFs / step time (DOF/s).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -16,8 +17,13 @@ N > 1 runs independent replicas, one per GPU (the path has no exchange step).
 
 measures the batched solve instead: 256 PlaneStress2d RVEs (sides uniform in
 32..256 from seed 0, inclusions E = 300e9 at area fraction 0.3 in a matrix
-E = 30e9), three prescribed-strain load cases each, one batched FP64 PCG to
-1e-8 for all 768 (RVE, load case) pairs; value = free DOFs x load cases / step.
+E = 30e9), three prescribed-strain load cases each, one batched mixed-precision
+PCG to 1e-8 for all 768 (RVE, load case) pairs (the batched FP64 PCG beside it);
+value = free DOFs x load cases / step. `--workload mises_block` (J2 plasticity,
+10 NonLinearStatic increments), `--workload idm1_batch` (IDM1 damage on tets, a
+batch of seeds), `--workload solvers` (every linear solver of the reference on
+smaller cantilevers) and `--workload spmv_forms` (every SpMV loop form) are
+described in their functions.
 """
 from __future__ import annotations
 
